@@ -1,0 +1,239 @@
+"""Seeded synthetic initial conditions for the benchmark problems.
+
+The reference builds its initial data with separate generator executables
+that write .h5part files (app/id_generators/*).  Those need HDF5 and are not
+part of the per-step path, so the problems are restated here from their
+physical description, with every choice recorded in the returned ``meta``.
+
+Smoothing length convention (app/id_generators/sodtube/main.cc:538-539):
+h = sph_eta * kernel_width * (m/rho)^(1/D), kernel_width = 2 for the
+Wendland kernels (include/physics/kernels.h:753-756).
+"""
+import math
+
+import numpy as np
+
+from .abi import EOS_IDEAL, EOS_POLYTROPIC, KERNEL_WENDLAND_C6, Params, new_state
+
+KERNEL_WIDTH = 2.0
+
+
+def _lattice(nx, ny, nz, lo, dx):
+    """Cell-centred cubic lattice, x fastest; returns (N,3) positions."""
+    ix = (np.arange(nx) + 0.5) * dx + lo[0]
+    iy = (np.arange(ny) + 0.5) * dx + lo[1]
+    iz = (np.arange(nz) + 0.5) * dx + lo[2]
+    Z, Y, X = np.meshgrid(iz, iy, ix, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+
+
+def _wendland_c6_3d(r, h):
+    q = r / h
+    w = (1365.0 / (64.0 * math.pi)) / h**3 * (1 - q) ** 8 * (1 + 8 * q + 25 * q**2 + 32 * q**3)
+    return np.where(q < 1.0, w, 0.0)
+
+
+def sod3d(nx=80, ny=20, nz=20, gamma=1.4, eta=1.5, seed=None):
+    """3D Sod shock tube on a cubic lattice, dx = 1/nx over x in [-0.5, 0.5].
+
+    Left (x < 0): rho=1, P=1; right: rho=0.125, P=0.1, densities set by the
+    particle mass on one uniform lattice; v = 0; ideal gas; Wendland C6;
+    h = eta*2*dx (h = 3 dx for eta = 1.5, about 97 neighbours).  The y and z
+    extents follow from the cubic spacing: ny*dx and nz*dx, centred on 0.
+    """
+    dx = 1.0 / nx
+    lo = (-0.5, -0.5 * ny * dx, -0.5 * nz * dx)
+    pos = _lattice(nx, ny, nz, lo, dx)
+    n = len(pos)
+    s = new_state(n)
+    left = pos[:, 0] < 0.0
+    rho = np.where(left, 1.0, 0.125)
+    P = np.where(left, 1.0, 0.1)
+    s["x"][:], s["y"][:], s["z"][:] = pos[:, 0], pos[:, 1], pos[:, 2]
+    s["m"][:] = rho * dx**3
+    s["rho"][:] = rho
+    s["P"][:] = P
+    s["u"][:] = P / ((gamma - 1.0) * rho)
+    s["h"][:] = eta * KERNEL_WIDTH * dx
+    params = Params.defaults(dimension=3, sph_kernel=KERNEL_WENDLAND_C6,
+                             eos_type=EOS_IDEAL, poly_gamma=gamma, sph_eta=eta,
+                             adaptive_timestep=1, timestep_cfl_factor=0.25,
+                             initial_dt=1.0e-12)
+    meta = dict(problem="sod3d", n=n, dx=dx, box=[[lo[0], -lo[0]], [lo[1], -lo[1]], [lo[2], -lo[2]]],
+                lattice=[nx, ny, nz])
+    return s, params, meta
+
+
+def sedov3d(n1d=128, gamma=5.0 / 3.0, eta=1.44, jitter=0.01, seed=12345,
+            energy=1.0, u0=1.0e-5):
+    """3D Sedov blast on a jittered cubic lattice in [-0.5, 0.5]^3.
+
+    rho = 1 (m = dx^3), u = u0, per-axis N(0, jitter*dx) jitter from
+    numpy's PCG64(seed); energy E deposited as u_b += E w_b / sum(m w) with
+    w_b = W_C6(r_b, 2h), i.e. kernel-weighted over particles within 2h of
+    the origin.  eta = 1.44 gives h = 2.88 dx, about 100 neighbours.
+    """
+    dx = 1.0 / n1d
+    pos = _lattice(n1d, n1d, n1d, (-0.5, -0.5, -0.5), dx)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = pos + rng.normal(0.0, jitter * dx, size=pos.shape)
+    n = len(pos)
+    s = new_state(n)
+    s["x"][:], s["y"][:], s["z"][:] = pos[:, 0], pos[:, 1], pos[:, 2]
+    m = dx**3
+    h = eta * KERNEL_WIDTH * dx
+    s["m"][:] = m
+    s["rho"][:] = 1.0
+    s["h"][:] = h
+    r = np.sqrt((pos**2).sum(axis=1))
+    w = _wendland_c6_3d(r, 2.0 * h)
+    u = np.full(n, u0)
+    u += energy * w / (m * w.sum())
+    s["u"][:] = u
+    s["P"][:] = (gamma - 1.0) * 1.0 * u
+    params = Params.defaults(dimension=3, sph_kernel=KERNEL_WENDLAND_C6,
+                             eos_type=EOS_IDEAL, poly_gamma=gamma, sph_eta=eta,
+                             adaptive_timestep=1, timestep_cfl_factor=0.25,
+                             initial_dt=1.0e-6)
+    meta = dict(problem="sedov3d", n=n, dx=dx, seed=seed, jitter=jitter, eta=eta,
+                energy=energy, u0=u0, box=[[-0.5, 0.5]] * 3)
+    return s, params, meta
+
+
+def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0):
+    """n=1 polytrope: rho(r) = rho_c sin(pi r)/(pi r), R = 1, M = 1, G = 1.
+
+    Radii by inverse-CDF sampling of M(r) ~ sin(pi r) - pi r cos(pi r)
+    (bisection in FP64), isotropic directions, m = M/n, rho_c = pi M/(4 R^3)
+    (so the enclosed mass is M), polytropic EOS with gamma = 2 and
+    K = 2 G R^2 / pi (hydrostatic equilibrium), v = 0, h from the local
+    density.  The density is the analytic profile (the SPH sum recomputes it
+    in the first density pass).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = rng.random(n)
+    # invert F(r) = (sin(pi r) - pi r cos(pi r)) / pi on [0, 1] by bisection
+    lo = np.zeros(n)
+    hi = np.ones(n)
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        F = (np.sin(np.pi * mid) - np.pi * mid * np.cos(np.pi * mid)) / np.pi
+        mask = F < t
+        lo = np.where(mask, mid, lo)
+        hi = np.where(mask, hi, mid)
+    r = 0.5 * (lo + hi) * R
+    cth = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    sth = np.sqrt(1.0 - cth**2)
+    s = new_state(n)
+    s["x"][:] = r * sth * np.cos(phi)
+    s["y"][:] = r * sth * np.sin(phi)
+    s["z"][:] = r * cth
+    rho_c = math.pi * M / (4.0 * R**3)
+    pr = np.pi * r / R
+    rho = rho_c * np.where(pr > 1e-12, np.sin(pr) / np.maximum(pr, 1e-300), 1.0)
+    rho = np.maximum(rho, 1e-3 * rho_c)
+    K = 2.0 * G * R**2 / math.pi
+    m = M / n
+    s["m"][:] = m
+    s["rho"][:] = rho
+    s["P"][:] = K * rho**2
+    s["K"][:] = K
+    s["u"][:] = K * rho  # P / ((gamma-1) rho) with gamma = 2
+    s["h"][:] = eta * KERNEL_WIDTH * np.cbrt(m / rho)
+    params = Params.defaults(dimension=3, sph_kernel=KERNEL_WENDLAND_C6,
+                             eos_type=EOS_POLYTROPIC, poly_gamma=2.0, sph_eta=eta,
+                             enable_fmm=1, fmm_macangle=0.5, gravitational_constant=G,
+                             gravity_order=2, adaptive_timestep=1,
+                             initial_dt=1.0e-6)
+    meta = dict(problem="polytrope3d", n=n, seed=seed, K=K, rho_c=rho_c, eta=eta)
+    return s, params, meta
+
+
+def kh3d(n1d=256, gamma=5.0 / 3.0, eta=1.44, amp=0.01, seed=7):
+    """Kelvin-Helmholtz in the periodic unit box, cubic lattice n1d^3.
+
+    The band |y| < 0.25 read periodically (y in [0,0.25) or (0.75,1)) has
+    rho = 2, vx = +0.5; elsewhere rho = 1, vx = -0.5; density by particle
+    mass on one lattice; P = 2.5; vy = amp sin(4 pi x).  `seed` is recorded
+    but unused: the perturbation is deterministic.
+    """
+    dx = 1.0 / n1d
+    pos = _lattice(n1d, n1d, n1d, (0.0, 0.0, 0.0), dx)
+    n = len(pos)
+    s = new_state(n)
+    s["x"][:], s["y"][:], s["z"][:] = pos[:, 0], pos[:, 1], pos[:, 2]
+    y = pos[:, 1]
+    band = (y < 0.25) | (y > 0.75)
+    rho = np.where(band, 2.0, 1.0)
+    s["m"][:] = rho * dx**3
+    s["rho"][:] = rho
+    s["P"][:] = 2.5
+    s["u"][:] = 2.5 / ((gamma - 1.0) * rho)
+    s["vx"][:] = np.where(band, 0.5, -0.5)
+    s["vy"][:] = amp * np.sin(4.0 * np.pi * pos[:, 0])
+    s["h"][:] = eta * KERNEL_WIDTH * dx
+    params = Params.defaults(dimension=3, sph_kernel=KERNEL_WENDLAND_C6,
+                             eos_type=EOS_IDEAL, poly_gamma=gamma, sph_eta=eta,
+                             periodic_boundary_x=1, periodic_boundary_y=1,
+                             periodic_boundary_z=1, box_length=1.0, box_width=1.0,
+                             box_height=1.0, adaptive_timestep=1, initial_dt=1e-6)
+    meta = dict(problem="kh3d", n=n, dx=dx, seed=seed, band="y<0.25 or y>0.75")
+    return s, params, meta
+
+
+def sod2d(nx=200, ny=20, gamma=1.4, eta=1.5):
+    """2D Sod tube on a square lattice dx = 1/nx, x in [-0.5,0.5]."""
+    dx = 1.0 / nx
+    ix = (np.arange(nx) + 0.5) * dx - 0.5
+    iy = (np.arange(ny) + 0.5) * dx - 0.5 * ny * dx
+    Y, X = np.meshgrid(iy, ix, indexing="ij")
+    x, y = X.ravel(), Y.ravel()
+    n = len(x)
+    s = new_state(n)
+    left = x < 0
+    rho = np.where(left, 1.0, 0.125)
+    P = np.where(left, 1.0, 0.1)
+    s["x"][:], s["y"][:] = x, y
+    s["m"][:] = rho * dx**2
+    s["rho"][:] = rho
+    s["P"][:] = P
+    s["u"][:] = P / ((gamma - 1.0) * rho)
+    s["h"][:] = eta * KERNEL_WIDTH * dx
+    params = Params.defaults(dimension=2, sph_kernel=KERNEL_WENDLAND_C6,
+                             poly_gamma=gamma, sph_eta=eta, adaptive_timestep=1,
+                             initial_dt=1.0e-12)
+    return s, params, dict(problem="sod2d", n=n, dx=dx)
+
+
+def noh2d(n1d=100, gamma=5.0 / 3.0, eta=1.5, P0=1e-6):
+    """2D Noh implosion: disc of radius 0.5, rho=1, P=1e-6, v = -r_hat."""
+    dx = 1.0 / n1d
+    ix = (np.arange(n1d) + 0.5) * dx - 0.5
+    Y, X = np.meshgrid(ix, ix, indexing="ij")
+    x, y = X.ravel(), Y.ravel()
+    r = np.sqrt(x * x + y * y)
+    keep = r < 0.5
+    x, y, r = x[keep], y[keep], r[keep]
+    n = len(x)
+    s = new_state(n)
+    s["x"][:], s["y"][:] = x, y
+    s["m"][:] = dx**2
+    s["rho"][:] = 1.0
+    s["P"][:] = P0
+    s["u"][:] = P0 / (gamma - 1.0)
+    rr = np.maximum(r, 1e-12)
+    s["vx"][:] = -x / rr
+    s["vy"][:] = -y / rr
+    s["h"][:] = eta * KERNEL_WIDTH * dx
+    params = Params.defaults(dimension=2, sph_kernel=KERNEL_WENDLAND_C6,
+                             poly_gamma=gamma, sph_eta=eta, adaptive_timestep=1,
+                             initial_dt=1.0e-6)
+    return s, params, dict(problem="noh2d", n=n, dx=dx)
+
+
+def shuffled(state, seed=99):
+    """The same particles in a seeded random order (ids travel along)."""
+    n = len(state["x"])
+    perm = np.random.Generator(np.random.PCG64(seed)).permutation(n)
+    return {k: np.ascontiguousarray(v[perm]) for k, v in state.items()}

@@ -1,0 +1,268 @@
+/*
+ * fsph.h -- C ABI of the GB300 SPH hot path (libfsph_gb300.so).
+ *
+ * The entry points replace the call surface FleCSPH's evolution drivers use
+ * on the per-step particle path (app/drivers/hydro/main_driver.cc:98-279 and
+ * app/drivers/newtonian/main_driver.cc:98-298):
+ *
+ *   body_system<T,D>   (mpisph/bodies_system.h)
+ *     update_iteration()              :152-229  -> fsph_update_iteration
+ *     reset_ghosts()                  :273-275  -> fsph_reset_ghosts
+ *     apply_in_smoothinglength(f)     :304-307  -> fsph_density_pressure_soundspeed,
+ *                                                  fsph_acceleration, fsph_dudt, fsph_dedt
+ *     apply_all(f)                    :318-324  -> fsph_eos_init, fsph_set_total_energy,
+ *                                                  fsph_save_velocityhalf, fsph_leapfrog_*,
+ *                                                  fsph_recompute_pressure_soundspeed[_thermokinetic],
+ *                                                  fsph_compute_dt, fsph_check_nans,
+ *                                                  fsph_check_negativity
+ *     get_all(f)                      :335-338  -> fsph_set_adaptive_timestep,
+ *                                                  fsph_compute_smoothinglength,
+ *                                                  fsph_compute_average_smoothinglength
+ *     gravitation_fmm()               :282-288  -> fsph_gravitation
+ *     setMacangle(double)             :70-72    -> fsph_params.fmm_macangle
+ *   physics::advance_time()  include/physics/default_physics.h:853-860 -> fsph_advance_time
+ *   the whole do{...}while body of mpi_init_task              -> fsph_step
+ *
+ * All arrays crossing this boundary are host (or device, where stated)
+ * pointers owned by the caller; plain C types only.  Every call returns an
+ * fsph_status; nothing throws across the boundary.  A context owns one CUDA
+ * stream on one device and is not re-entrant: use one context per host
+ * thread.  Calls enqueue work asynchronously except where documented as
+ * synchronous (download, neighbour export, reductions, status reads).
+ *
+ * Particle order: after fsph_update_iteration the particles are held sorted
+ * by (Morton key, id), as the reference keeps its bodies vector sorted in
+ * place (mpisph/bodies_system.h:195-206); fsph_download returns that order,
+ * with ids, so the caller can map back.
+ */
+#ifndef FSPH_H
+#define FSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSPH_ABI_VERSION 1
+
+/* Status codes.  They replace the reference's assert()/mpi_assert() aborts
+ * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
+ * mpisph/utils.h:34-38). */
+typedef enum fsph_status {
+  FSPH_OK = 0,
+  FSPH_ERR_ARG = 1,            /* bad argument / unsupported parameter value */
+  FSPH_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  FSPH_ERR_NAN = 3,            /* check_nans found a NaN */
+  FSPH_ERR_NEG_DENSITY = 4,    /* compute_density: rho not > 0 */
+  FSPH_ERR_NEG_ENERGY = 5,     /* recover_internal_energy / compute_dt: u not > 0 */
+  FSPH_ERR_NEGATIVITY = 6,     /* check_negativity: rho, P or u < 0 */
+  FSPH_ERR_LIST_OVERFLOW = 7,  /* a neighbour list exceeded max_neighbors */
+  FSPH_ERR_STACK_OVERFLOW = 8, /* a tree-walk stack exceeded its capacity */
+  FSPH_ERR_TIMEOUT = 9,        /* a bounded device loop gave up */
+  FSPH_ERR_DUPLICATE_KEY = 10, /* two particles share a full Morton key */
+  FSPH_ERR_DT = 11,            /* compute_dt energy-positivity loop did not converge */
+  FSPH_ERR_STATE = 12,         /* call made before the state it needs exists */
+  FSPH_ERR_NO_DEVICE = 13,     /* no CUDA device / extension not usable */
+  FSPH_ERR_OOM = 14            /* device allocation failed */
+} fsph_status;
+
+/* Same numbering as param::sph_kernel_keyword (include/params.h:128-137). */
+enum fsph_kernel {
+  FSPH_KERNEL_CUBIC_SPLINE = 0,
+  FSPH_KERNEL_QUINTIC_SPLINE = 1,
+  FSPH_KERNEL_WENDLAND_C2 = 2,
+  FSPH_KERNEL_WENDLAND_C4 = 3,
+  FSPH_KERNEL_WENDLAND_C6 = 4
+};
+/* Same numbering as param::eos_type_keyword (include/params.h:139-145). */
+enum fsph_eos { FSPH_EOS_IDEAL = 0, FSPH_EOS_POLYTROPIC = 1 };
+/* param::sph_viscosity_keyword (include/params.h:148-152): only visc_constant. */
+enum fsph_viscosity { FSPH_VISC_CONSTANT = 0 };
+enum fsph_precision {
+  FSPH_PRECISION_FP64 = 0,  /* every pair term in FP64 (plain method) */
+  FSPH_PRECISION_MIXED = 1  /* FP32 pair math with compensated sums; FP64 state */
+};
+
+/* Physics and run parameters.  Names and defaults follow param:: in
+ * include/params.h (line of each DECLARE_PARAM in brackets); the last block
+ * is specific to this implementation. */
+typedef struct fsph_params {
+  int32_t dimension;                 /* gdimension: 2 or 3 */
+  int32_t sph_kernel;                /* [227] wendland_c4 */
+  int32_t eos_type;                  /* [468] eos_ideal */
+  int32_t sph_viscosity;             /* [495] visc_constant */
+  double poly_gamma;                 /* [478] 1.4 */
+  double sph_eta;                    /* [212] 1.5 */
+  double sph_viscosity_alpha;        /* [501] 1.0 */
+  double sph_viscosity_beta;         /* [506] 2.0 */
+  double sph_viscosity_epsilon;      /* [511] 0.01 */
+  double timestep_cfl_factor;        /* [183] 0.25 */
+  double initial_dt;                 /* [178] 0.001 */
+  double initial_time;               /* [169] 0 */
+  double final_time;                 /* [173] 0 */
+  double out_screen_dt;              /* [339] 0 */
+  double out_scalar_dt;              /* [350] 0 */
+  double out_h5data_dt;              /* [366] 0 */
+  double fmm_macangle;               /* [542] 0.0 */
+  double gravitational_constant;     /* [628] 1 */
+  double box_length;                 /* [258] 3.0 */
+  double box_width;                  /* [262] 1.0 */
+  double box_height;                 /* [266] 1.0 */
+  int64_t initial_iteration;         /* [160] 0 */
+  int64_t final_iteration;           /* [165] 0 */
+  int32_t adaptive_timestep;         /* [188] false */
+  int32_t thermokinetic_formulation; /* [591] true */
+  int32_t evolve_internal_energy;    /* [584] true */
+  int32_t pressure_updates_number;   /* [194] 1 */
+  int32_t sph_variable_h;            /* [244] false */
+  int32_t sph_update_uniform_h;      /* [238] false */
+  int32_t relaxation_steps;          /* [563] 0 (only 0 is supported) */
+  int32_t enable_fmm;                /* [537] false */
+  int32_t periodic_boundary_x;       /* [292] false */
+  int32_t periodic_boundary_y;       /* [296] false */
+  int32_t periodic_boundary_z;       /* [300] false */
+  /* implementation-specific */
+  int32_t precision_mode;            /* enum fsph_precision, default FP64 */
+  int32_t max_neighbors;             /* neighbour-list capacity per particle, default 256 */
+  int32_t gravity_order;             /* multipole order of fsph_gravitation: 1 or 2 (default 2) */
+  int32_t reserved[8];
+} fsph_params;
+
+/* Structure-of-arrays view of the particle state, FP64 throughout.  On
+ * upload every pointer marked (in) must be non-NULL; (opt) pointers may be
+ * NULL and then start at zero.  On download NULL pointers are skipped.
+ * 2D runs ignore the z components.  Field names follow body_u
+ * (include/physics/body.h:221-251). */
+typedef struct fsph_soa_view {
+  int64_t n;
+  double *x, *y, *z;       /* (in)  coordinates */
+  double *vx, *vy, *vz;    /* (in)  velocity */
+  double *vhx, *vhy, *vhz; /* (opt) velocity at the half step */
+  double *ax, *ay, *az;    /* (opt) hydro acceleration */
+  double *gax, *gay, *gaz; /* (opt) gravitational acceleration */
+  double *gpot;            /* (opt) gravitational potential */
+  double *m;               /* (in)  mass */
+  double *h;               /* (in)  smoothing length (entity radius) */
+  double *rho;             /* (opt) density */
+  double *P;               /* (opt) pressure */
+  double *cs;              /* (opt) sound speed */
+  double *u;               /* (opt) specific internal energy */
+  double *e;               /* (opt) specific total (thermokinetic) energy */
+  double *dudt;            /* (opt) */
+  double *dedt;            /* (opt) */
+  double *K;               /* (opt) adiabatic invariant */
+  double *alpha;           /* (opt) viscosity alpha (unused by visc_constant) */
+  double *vsig;            /* (opt) signal speed */
+  double *dt;              /* (opt) per-particle timestep estimate */
+  int64_t *id;             /* (in)  particle id (sort tie-break) */
+  uint64_t *key;           /* (out) Morton key, download only */
+} fsph_soa_view;
+
+/* Conserved totals over all particles (include/physics/analysis.h:56-214),
+ * FP64 reductions on the device. */
+typedef struct fsph_conserved {
+  double mass;
+  double energy;        /* sum m*e (thermokinetic) or m*(u + v^2/2), plus grav. */
+  double momentum[3];
+  double angular_momentum[3];
+} fsph_conserved;
+
+/* Per-kernel device time accumulated since the last reset (CUDA events on
+ * the context's stream).  Indices: see FSPH_TIMER_* below. */
+enum {
+  FSPH_TIMER_RANGE_KEYS = 0,
+  FSPH_TIMER_SORT = 1,
+  FSPH_TIMER_TREE = 2,
+  FSPH_TIMER_NEIGHBORS = 3,
+  FSPH_TIMER_DENSITY = 4,
+  FSPH_TIMER_VSIG = 5,
+  FSPH_TIMER_ACCEL = 6,
+  FSPH_TIMER_ENERGY = 7,
+  FSPH_TIMER_INTEGRATE = 8,
+  FSPH_TIMER_DT = 9,
+  FSPH_TIMER_GRAVITY = 10,
+  FSPH_TIMER_COUNT = 16
+};
+
+typedef struct fsph_ctx fsph_ctx;
+
+/* -- lifetime ------------------------------------------------------------ */
+void fsph_params_default(fsph_params * p);
+int32_t fsph_abi_version(void);
+/* Creates a context on `device` able to hold `capacity` particles. */
+fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
+  fsph_status * status);
+void fsph_destroy(fsph_ctx * ctx);
+const char * fsph_status_string(int32_t status);
+/* Last error detail of this context (CUDA error string etc.). */
+const char * fsph_last_error(const fsph_ctx * ctx);
+
+/* -- data movement ------------------------------------------------------- */
+/* Host -> device copy of a full particle set (mpisph/bodies_system.h:83-89
+ * read_bodies analogue); resets iteration/time to the params' initial ones. */
+fsph_status fsph_upload(fsph_ctx * ctx, const fsph_soa_view * host);
+/* Device -> host copy, current (sorted) order.  Synchronous. */
+fsph_status fsph_download(fsph_ctx * ctx, fsph_soa_view * host);
+fsph_status fsph_get_time(fsph_ctx * ctx, double * dt, double * totaltime,
+  int64_t * iteration);
+fsph_status fsph_set_time(fsph_ctx * ctx, double dt, double totaltime,
+  int64_t iteration);
+/* Range [min0,min1,(min2),max0,max1,(max2)] of the last update_iteration. */
+fsph_status fsph_get_range(fsph_ctx * ctx, double * range);
+
+/* -- body_system --------------------------------------------------------- */
+fsph_status fsph_update_iteration(fsph_ctx * ctx);
+fsph_status fsph_reset_ghosts(fsph_ctx * ctx);
+/* apply_in_smoothinglength(...) */
+fsph_status fsph_density_pressure_soundspeed(fsph_ctx * ctx);
+fsph_status fsph_acceleration(fsph_ctx * ctx);
+fsph_status fsph_dudt(fsph_ctx * ctx);
+fsph_status fsph_dedt(fsph_ctx * ctx);
+/* apply_all(...) */
+fsph_status fsph_eos_init(fsph_ctx * ctx);
+fsph_status fsph_set_total_energy(fsph_ctx * ctx);
+fsph_status fsph_save_velocityhalf(fsph_ctx * ctx);
+fsph_status fsph_leapfrog_kick_v(fsph_ctx * ctx);
+fsph_status fsph_leapfrog_kick_u(fsph_ctx * ctx);
+fsph_status fsph_leapfrog_kick_e(fsph_ctx * ctx);
+fsph_status fsph_leapfrog_drift(fsph_ctx * ctx);
+fsph_status fsph_recompute_pressure_soundspeed(fsph_ctx * ctx);
+fsph_status fsph_recompute_pressure_soundspeed_thermokinetic(fsph_ctx * ctx);
+fsph_status fsph_compute_dt(fsph_ctx * ctx);
+fsph_status fsph_check_nans(fsph_ctx * ctx);
+fsph_status fsph_check_negativity(fsph_ctx * ctx);
+/* get_all(...) */
+fsph_status fsph_set_adaptive_timestep(fsph_ctx * ctx);
+fsph_status fsph_compute_smoothinglength(fsph_ctx * ctx);
+fsph_status fsph_compute_average_smoothinglength(fsph_ctx * ctx);
+/* gravitation_fmm(): multipole tree gravity, order params.gravity_order,
+ * opening angle params.fmm_macangle; adds into g-acceleration/potential. */
+fsph_status fsph_gravitation(fsph_ctx * ctx);
+/* physics::advance_time() */
+fsph_status fsph_advance_time(fsph_ctx * ctx);
+
+/* One whole driver iteration (the initial one when iteration ==
+ * initial_iteration, else a leapfrog step), including advance_time. */
+fsph_status fsph_step(fsph_ctx * ctx);
+/* Synchronises and returns the first error any kernel raised since the
+ * last call (device error words), then clears it. */
+fsph_status fsph_sync(fsph_ctx * ctx);
+
+/* -- inspection ---------------------------------------------------------- */
+/* Neighbour lists of the last update_iteration in CSR form over the sorted
+ * particle index: offsets[n+1], indices[total].  Pass indices == NULL to
+ * query the total in offsets[n].  Each list is sorted ascending.  Sync. */
+fsph_status fsph_get_neighbors(fsph_ctx * ctx, int64_t * offsets,
+  int64_t * indices, int64_t capacity);
+fsph_status fsph_conserved_sums(fsph_ctx * ctx, fsph_conserved * out);
+fsph_status fsph_timers(fsph_ctx * ctx, double * ms, int32_t count,
+  int64_t * launches);
+fsph_status fsph_timers_reset(fsph_ctx * ctx);
+/* Number of kernel launches this context has issued (all kinds). */
+int64_t fsph_launch_count(const fsph_ctx * ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSPH_H */

@@ -1,0 +1,1551 @@
+/*
+ * fsph_oracle.c -- plain-C restatement of FleCSPH's per-step particle path.
+ *
+ * TEST INFRASTRUCTURE: the CPU oracle the GPU library is checked against and
+ * the timed CPU baseline.  It is never linked into, loaded by or called from
+ * the GPU product path (flecsph_gb300/).
+ *
+ * What it restates (paths inside the laristra/flecsph tree):
+ *   range              mpisph/bodies_system.h:231-268
+ *   Morton keys        include/tree_topology/filling_curve.h:503-525
+ *   sort (key, id)     mpisph/bodies_system.h:195-206, mpisph/psort.h:247-253
+ *   octree + COM data  include/tree_topology/tree_topology.h:878-997,1894-1970
+ *                      include/physics/default_physics.h:59-119
+ *   groups + walk      include/tree_topology/tree_topology.h:212-442
+ *   geometry tests     include/tree_topology/tree_geometry.h:152-366
+ *   physics            include/physics/default_physics.h, kernels.h,
+ *                      viscosity.h, eos/eos.h, integration.h
+ *   driver step        app/drivers/hydro/main_driver.cc:98-279
+ *
+ * Every floating-point expression keeps the reference's operand order; build
+ * with -ffp-contract=off so no multiply-add is fused (the reference's x86
+ * build has no FMA).  The result: neighbour lists in the reference's own
+ * order and bit-identical FP64 fields on the same input (up to ulp-level
+ * differences of libm pow/sqrt/cbrt between platforms).
+ *
+ * Two implementation choices keep results identical while allowing threads:
+ *  - the reference walks groups in descending Morton order and, inside the
+ *    density pass, computes the signal speed of a particle right after its
+ *    own sound speed, so a neighbour b already visited (sorted index
+ *    b > a) contributes its new sound speed and any other neighbour its old
+ *    one (default_physics.h:236-265,309-320, tree_topology.h:220-235,
+ *    401-408).  This file evaluates that rule explicitly instead of relying
+ *    on visiting order;
+ *  - the reference's compressed chains of single-child nodes are kept
+ *    implicitly: a node records the top and bottom level of its chain and
+ *    the COM/radius/lap of the chain's top node are derived with the same
+ *    arithmetic compute_cofm applies to a one-child node.
+ */
+#include "fsph_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define GROUP_MAX 128 /* tree_topology.h:2121 sub_entities_ */
+static const double TINY = 1e10 * DBL_MIN; /* kernels.h:64, viscosity.h:36 */
+
+/* ---------------------------------------------------------------- tree -- */
+typedef struct {
+  int64_t s, e;      /* particle range [s, e) in sorted order */
+  int ltop, lbot;    /* level of the chain's top node and of the branching node */
+  double com[3], mass, radius, lap;          /* branching (bottom) node */
+  double tcom[3], tmass, tradius, tlap;      /* chain top node */
+  double bmin[3], bmax[3];
+  int64_t sub;
+  int nchild;
+  int64_t child[8]; /* >= 0: node index; < 0: ~particle index */
+} onode;
+
+typedef struct {
+  int64_t * q;
+  int64_t * nq;
+  int64_t qcap;
+  int64_t ** nb; /* per member neighbour lists */
+  int64_t * nbn;
+  int64_t * nbcap;
+} scratch;
+
+struct orc_ctx {
+  fsph_params p;
+  int D;
+  int64_t n, cap;
+  double *x[3], *v[3], *vh[3], *a[3], *ga[3];
+  double *gpot, *m, *h, *rho, *P, *cs, *u, *e, *dudt, *dedt, *K, *alpha, *vsig,
+    *dtp;
+  int64_t * id;
+  uint64_t * key;
+  double * csnew;
+  /* time (physics:: globals, default_physics.h:32-39) */
+  double dt, dt_saved, totaltime, totaltime_next;
+  double t_screen, t_scalar, t_h5;
+  int64_t iteration;
+  double range[2][3];
+  double kernel_width;
+  /* tree */
+  onode * nodes;
+  int64_t nnodes, node_cap;
+  int * edepth;
+  int64_t * groups;
+  int64_t ngroups;
+  int tree_ok;
+  int nthreads;
+  int err;
+};
+
+static int max_depth_of(int D) { return 63 / D; }
+
+static int digit_of(const orc_ctx * c, uint64_t key, int level) {
+  int md = max_depth_of(c->D);
+  return (int)((key >> ((md - level) * c->D)) & ((1u << c->D) - 1));
+}
+
+static int lcp_levels(const orc_ctx * c, uint64_t a, uint64_t b) {
+  int md = max_depth_of(c->D);
+  int l = 0;
+  while(l < md && digit_of(c, a, l + 1) == digit_of(c, b, l + 1))
+    ++l;
+  return l;
+}
+
+/* ------------------------------------------------------ small helpers -- */
+static inline double dmax_(double a, double b) { return (a < b) ? b : a; } /* std::max */
+static inline double dmin_(double a, double b) { return (b < a) ? b : a; } /* std::min */
+
+static double dist_pts(int D, const double * a, const double * b) {
+  /* flecsi::distance (space_vector.h:47-58) */
+  double sum = 0;
+  for(int d = 0; d < D; ++d)
+    sum += (a[d] - b[d]) * (a[d] - b[d]);
+  return sqrt(sum);
+}
+
+static void getx(const orc_ctx * c, int64_t i, double * o) {
+  for(int d = 0; d < c->D; ++d)
+    o[d] = c->x[d][i];
+}
+
+/* ------------------------------------------------------------ kernels -- */
+static const double cubic_sigma[3] = {4. / 3., 40. / (7. * M_PI), 8. / M_PI};
+static const double wc2_sigma[3] = {1.25, 7. / M_PI, 21. / (2. * M_PI)};
+static const double wc4_sigma[3] = {1.5, 9. / M_PI, 495. / (32. * M_PI)};
+static const double wc6_sigma[3] = {55. / 32., 78. / (7. * M_PI),
+  1365. / (64. * M_PI)};
+
+/* kernel<K,D>(r, h): kernels.h:106-121 (cubic), :282-312 (C2), :375-410
+ * (C4), :477-512 (C6). */
+static double kfun(const orc_ctx * c, double r, double h) {
+  const int D = c->D;
+  switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_CUBIC_SPLINE: {
+      double rh = 2. * r / h;
+      double result = 0.;
+      if(rh < 2.0) {
+        if(rh < 1.0)
+          result = 1.0 - 1.5 * rh * rh + .75 * rh * rh * rh;
+        else
+          result = 0.25 * (2 - rh) * (2 - rh) * (2 - rh);
+        result *= cubic_sigma[D - 1] / pow(h, D);
+      }
+      return result;
+    }
+    case FSPH_KERNEL_WENDLAND_C2: {
+      double rh = r / h;
+      double hd = (D == 3) ? h * h * h : h * h;
+      double rh2 = (1 - rh) * (1 - rh);
+      double sigma = wc2_sigma[D - 1] / hd;
+      double result = sigma * rh2 * rh2 * (4 * rh + 1);
+      return result * (rh < 1.0);
+    }
+    case FSPH_KERNEL_WENDLAND_C4: {
+      double rh = r / h;
+      double hd = (D == 3) ? h * h * h : h * h;
+      double rh1 = 1 - rh;
+      double rh2 = rh1 * rh1;
+      double rh6 = rh2 * rh2 * rh2;
+      double sigma = wc4_sigma[D - 1] / hd;
+      double result = sigma * rh6 * (1 + rh * (6 + rh * 35 / 3));
+      return result * (rh < 1.0);
+    }
+    case FSPH_KERNEL_WENDLAND_C6:
+    default: {
+      double rh = r / h;
+      double hd = (D == 3) ? h * h * h : h * h;
+      double rh2 = (1 - rh) * (1 - rh);
+      double rh4 = rh2 * rh2;
+      double sigma = wc6_sigma[D - 1] / hd;
+      double result = sigma * rh4 * rh4 * (1 + rh * (8 + rh * (25 + rh * 32)));
+      return result * (rh < 1.0);
+    }
+  }
+}
+
+/* kernel_gradient<K,D>(vecP, h): kernels.h:132-153 (cubic), :322-361 (C2),
+ * :435-463 (C4), :536-566 (C6). */
+static void kgrad(const orc_ctx * c, const double * p, double h, double * out) {
+  const int D = c->D;
+  double r = 0;
+  for(int d = 0; d < D; ++d)
+    r += p[d] * p[d];
+  r = sqrt(r); /* flecsi::magnitude */
+  switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_CUBIC_SPLINE: {
+      double rh = 2. * r / h;
+      for(int d = 0; d < D; ++d)
+        out[d] = 0.0;
+      if(rh < 2.0) {
+        double dWdr;
+        double sigma = 2. * cubic_sigma[D - 1] / pow(h, D + 1);
+        if(rh < 1.0)
+          dWdr = -3.0 * rh + 9. / 4. * rh * rh;
+        else
+          dWdr = -.75 * (2 - rh) * (2 - rh);
+        for(int d = 0; d < D; ++d)
+          out[d] = p[d] * sigma * dWdr / (r + TINY);
+      }
+      return;
+    }
+    case FSPH_KERNEL_WENDLAND_C2: {
+      double rh = r / h;
+      double hd1 = (D == 3) ? h * h * h * h : h * h * h;
+      double rh2 = (1 - rh) * (1 - rh);
+      double sigma = 2. * wc2_sigma[D - 1] / hd1;
+      double dWdr = -10. * rh * rh2 * (1 - rh);
+      double f = (rh < 1.0) * (sigma * dWdr / (r + TINY));
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * f;
+      return;
+    }
+    case FSPH_KERNEL_WENDLAND_C4: {
+      double rh = r / h;
+      double hd1 = (D == 3) ? h * h * h * h : h * h * h;
+      double rh2 = (1 - rh) * (1 - rh);
+      double rh3 = rh2 * (1 - rh);
+      double sigma = 14. * wc4_sigma[D - 1] / hd1;
+      double dWdr = -4. / 3. * rh * rh3 * rh2 * (1 + 5. * rh);
+      double f = (rh < 1.0) * (sigma * dWdr / (r + TINY));
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * f;
+      return;
+    }
+    case FSPH_KERNEL_WENDLAND_C6:
+    default: {
+      double rh = r / h;
+      double hd1 = (D == 3) ? h * h * h * h : h * h * h;
+      double rh2 = (1 - rh) * (1 - rh);
+      double rh3 = rh2 * (1 - rh);
+      double rh4 = rh2 * rh2;
+      double sigma = wc6_sigma[D - 1] / hd1;
+      double dWdr = -22. * rh * rh4 * rh3 * (1 + rh * (7 + rh * 16));
+      double f = (rh < 1.0) * (sigma * dWdr / (r + TINY));
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * f;
+      return;
+    }
+  }
+}
+
+/* viscosity::mu (viscosity.h:81-93) */
+static double visc_mu(const orc_ctx * c, double h_ab, const double * vel_ab,
+  const double * pos_ab) {
+  double dotp = 0, dist2 = 0;
+  for(int d = 0; d < c->D; ++d)
+    dotp += vel_ab[d] * pos_ab[d];
+  for(int d = 0; d < c->D; ++d)
+    dist2 += pos_ab[d] * pos_ab[d];
+  double result = h_ab * dotp /
+                  (dist2 + c->p.sph_viscosity_epsilon * h_ab * h_ab + TINY);
+  return result * (dotp < 0.0);
+}
+
+/* viscosity_function<visc_constant> (viscosity.h:128-137) */
+static double visc_pi(const orc_ctx * c, double rho_ab, double c_ab, double mu_ab) {
+  return (-c->p.sph_viscosity_alpha * c_ab + c->p.sph_viscosity_beta * mu_ab) *
+         mu_ab / rho_ab;
+}
+
+/* ---------------------------------------------------------------- EOS -- */
+/* eos_t<ideal/polytropic> (eos/eos.h:57-209) */
+static void eos_pressure(orc_ctx * c, int64_t i, double uval, double * P,
+  double * cs) {
+  const double g = c->p.poly_gamma;
+  if(c->p.eos_type == FSPH_EOS_POLYTROPIC) {
+    *P = c->K[i] * pow(c->rho[i], g);
+    *cs = sqrt(c->K[i] * g * pow(c->rho[i], g - 1.));
+  }
+  else {
+    *P = (g - 1.) * c->rho[i] * uval;
+    *cs = sqrt(g * (g - 1.) * uval);
+  }
+}
+
+/* ------------------------------------------------------------ context -- */
+static void * xalloc(size_t n) {
+  void * p = calloc(n ? n : 1, 1);
+  return p;
+}
+
+orc_ctx * orc_create(const fsph_params * p) {
+  if(!p || (p->dimension != 2 && p->dimension != 3))
+    return NULL;
+  orc_ctx * c = (orc_ctx *)xalloc(sizeof(orc_ctx));
+  c->p = *p;
+  c->D = p->dimension;
+  c->nthreads = 1;
+  /* kernels::select (kernels.h:753-767) */
+  c->kernel_width = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE) ? 3.0 : 2.0;
+  return c;
+}
+
+static void free_tree(orc_ctx * c) {
+  free(c->nodes);
+  free(c->edepth);
+  free(c->groups);
+  c->nodes = NULL;
+  c->edepth = NULL;
+  c->groups = NULL;
+  c->nnodes = c->node_cap = c->ngroups = 0;
+  c->tree_ok = 0;
+}
+
+static void free_state(orc_ctx * c) {
+  for(int d = 0; d < 3; ++d) {
+    free(c->x[d]); free(c->v[d]); free(c->vh[d]); free(c->a[d]); free(c->ga[d]);
+  }
+  free(c->gpot); free(c->m); free(c->h); free(c->rho); free(c->P); free(c->cs);
+  free(c->u); free(c->e); free(c->dudt); free(c->dedt); free(c->K);
+  free(c->alpha); free(c->vsig); free(c->dtp); free(c->id); free(c->key);
+  free(c->csnew);
+}
+
+void orc_destroy(orc_ctx * c) {
+  if(!c)
+    return;
+  free_state(c);
+  free_tree(c);
+  free(c);
+}
+
+int orc_set_threads(orc_ctx * c, int nthreads) {
+  c->nthreads = nthreads > 0 ? nthreads : 1;
+  return FSPH_OK;
+}
+
+/* analysis::set_initial_time_iteration (analysis.h:221-249) */
+static void init_time(orc_ctx * c) {
+  const fsph_params * p = &c->p;
+  c->iteration = p->initial_iteration;
+  c->totaltime = p->initial_time;
+  c->dt = p->initial_dt;
+  c->dt_saved = 0.0;
+  c->totaltime_next = 0.0;
+  c->t_screen = c->t_scalar = c->t_h5 = 0.0;
+  if(p->out_screen_dt > 0.0) {
+    c->t_screen = p->out_screen_dt * ((int64_t)(c->totaltime / p->out_screen_dt));
+    if(c->t_screen < c->totaltime) c->t_screen = c->totaltime;
+  }
+  if(p->out_scalar_dt > 0.0) {
+    c->t_scalar = p->out_scalar_dt * ((int64_t)(c->totaltime / p->out_scalar_dt));
+    if(c->t_scalar < c->totaltime) c->t_scalar = c->totaltime;
+  }
+  if(p->out_h5data_dt > 0.0) {
+    c->t_h5 = p->out_h5data_dt * ((int64_t)(c->totaltime / p->out_h5data_dt));
+    if(c->t_h5 < c->totaltime) c->t_h5 = c->totaltime;
+  }
+}
+
+#define CPY_IN(dst, src)                                                       \
+  do {                                                                         \
+    if(src) memcpy(dst, src, sizeof(double) * n);                              \
+    else memset(dst, 0, sizeof(double) * n);                                   \
+  } while(0)
+
+int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
+  if(!v || v->n < 2 || !v->x || !v->y || (c->D == 3 && !v->z) || !v->m ||
+     !v->h || !v->id)
+    return FSPH_ERR_ARG;
+  const int64_t n = v->n;
+  free_state(c);
+  free_tree(c);
+  c->n = c->cap = n;
+  for(int d = 0; d < 3; ++d) {
+    c->x[d] = xalloc(8 * n); c->v[d] = xalloc(8 * n); c->vh[d] = xalloc(8 * n);
+    c->a[d] = xalloc(8 * n); c->ga[d] = xalloc(8 * n);
+  }
+  c->gpot = xalloc(8 * n); c->m = xalloc(8 * n); c->h = xalloc(8 * n);
+  c->rho = xalloc(8 * n); c->P = xalloc(8 * n); c->cs = xalloc(8 * n);
+  c->u = xalloc(8 * n); c->e = xalloc(8 * n); c->dudt = xalloc(8 * n);
+  c->dedt = xalloc(8 * n); c->K = xalloc(8 * n); c->alpha = xalloc(8 * n);
+  c->vsig = xalloc(8 * n); c->dtp = xalloc(8 * n); c->id = xalloc(8 * n);
+  c->key = xalloc(8 * n); c->csnew = xalloc(8 * n);
+  double * const xs[3] = {v->x, v->y, v->z};
+  double * const vs[3] = {v->vx, v->vy, v->vz};
+  double * const vhs[3] = {v->vhx, v->vhy, v->vhz};
+  double * const as[3] = {v->ax, v->ay, v->az};
+  double * const gas[3] = {v->gax, v->gay, v->gaz};
+  for(int d = 0; d < c->D; ++d) {
+    CPY_IN(c->x[d], xs[d]); CPY_IN(c->v[d], vs[d]); CPY_IN(c->vh[d], vhs[d]);
+    CPY_IN(c->a[d], as[d]); CPY_IN(c->ga[d], gas[d]);
+  }
+  CPY_IN(c->gpot, v->gpot); CPY_IN(c->m, v->m); CPY_IN(c->h, v->h);
+  CPY_IN(c->rho, v->rho); CPY_IN(c->P, v->P); CPY_IN(c->cs, v->cs);
+  CPY_IN(c->u, v->u); CPY_IN(c->e, v->e); CPY_IN(c->dudt, v->dudt);
+  CPY_IN(c->dedt, v->dedt); CPY_IN(c->K, v->K); CPY_IN(c->alpha, v->alpha);
+  CPY_IN(c->vsig, v->vsig); CPY_IN(c->dtp, v->dt);
+  memcpy(c->id, v->id, 8 * n);
+  init_time(c);
+  return FSPH_OK;
+}
+
+#define CPY_OUT(dst, src)                                                      \
+  do {                                                                         \
+    if(dst) memcpy(dst, src, sizeof(double) * n);                             \
+  } while(0)
+
+int orc_download(orc_ctx * c, fsph_soa_view * v) {
+  if(!v || v->n != c->n)
+    return FSPH_ERR_ARG;
+  const int64_t n = c->n;
+  double * const xs[3] = {v->x, v->y, v->z};
+  double * const vs[3] = {v->vx, v->vy, v->vz};
+  double * const vhs[3] = {v->vhx, v->vhy, v->vhz};
+  double * const as[3] = {v->ax, v->ay, v->az};
+  double * const gas[3] = {v->gax, v->gay, v->gaz};
+  for(int d = 0; d < c->D; ++d) {
+    CPY_OUT(xs[d], c->x[d]); CPY_OUT(vs[d], c->v[d]); CPY_OUT(vhs[d], c->vh[d]);
+    CPY_OUT(as[d], c->a[d]); CPY_OUT(gas[d], c->ga[d]);
+  }
+  CPY_OUT(v->gpot, c->gpot); CPY_OUT(v->m, c->m); CPY_OUT(v->h, c->h);
+  CPY_OUT(v->rho, c->rho); CPY_OUT(v->P, c->P); CPY_OUT(v->cs, c->cs);
+  CPY_OUT(v->u, c->u); CPY_OUT(v->e, c->e); CPY_OUT(v->dudt, c->dudt);
+  CPY_OUT(v->dedt, c->dedt); CPY_OUT(v->K, c->K); CPY_OUT(v->alpha, c->alpha);
+  CPY_OUT(v->vsig, c->vsig); CPY_OUT(v->dt, c->dtp);
+  if(v->id) memcpy(v->id, c->id, 8 * n);
+  if(v->key) memcpy(v->key, c->key, 8 * n);
+  return FSPH_OK;
+}
+
+int orc_get_time(orc_ctx * c, double * dt, double * t, int64_t * it) {
+  if(dt) *dt = c->dt;
+  if(t) *t = c->totaltime;
+  if(it) *it = c->iteration;
+  return FSPH_OK;
+}
+
+int orc_set_time(orc_ctx * c, double dt, double t, int64_t it) {
+  c->dt = dt;
+  c->totaltime = t;
+  c->iteration = it;
+  return FSPH_OK;
+}
+
+int orc_get_range(orc_ctx * c, double * r) {
+  for(int d = 0; d < c->D; ++d) {
+    r[d] = c->range[0][d];
+    r[c->D + d] = c->range[1][d];
+  }
+  return FSPH_OK;
+}
+
+/* ------------------------------------------------- update_iteration -- */
+typedef struct {
+  uint64_t key;
+  int64_t id;
+  int64_t idx;
+} sortrec;
+
+static int cmp_sortrec(const void * a, const void * b) {
+  const sortrec * l = (const sortrec *)a;
+  const sortrec * r = (const sortrec *)b;
+  /* comparator of bodies_system.h:197-205 */
+  if(l->key < r->key) return -1;
+  if(l->key > r->key) return 1;
+  if(l->id < r->id) return -1;
+  if(l->id > r->id) return 1;
+  return 0;
+}
+
+static void permute_d(double ** f, const sortrec * rec, int64_t n, double * tmp) {
+  for(int64_t i = 0; i < n; ++i)
+    tmp[i] = (*f)[rec[i].idx];
+  memcpy(*f, tmp, 8 * n);
+}
+
+/* compute_cofm for a chain (one child node, no entities), as
+ * default_physics.h:59-119 evaluates it. */
+static void chain_up(int D, double * com, double * mass, double * radius,
+  double * lap) {
+  double nc[3];
+  double cm = *mass;
+  for(int d = 0; d < D; ++d)
+    nc[d] = 0.0 + cm * com[d];
+  double nm = 0.0 + cm;
+  for(int d = 0; d < D; ++d)
+    nc[d] /= nm;
+  double dist = dist_pts(D, nc, com);
+  double nr = dmax_(0.0, dist + *radius);
+  double nl = dmax_(0.0, dist + *radius + *lap);
+  for(int d = 0; d < D; ++d)
+    com[d] = nc[d];
+  *mass = nm;
+  *radius = nr;
+  *lap = nl;
+}
+
+static int64_t build_node(orc_ctx * c, int64_t s, int64_t e, int ltop) {
+  const int D = c->D;
+  const int md = max_depth_of(D);
+  int lbot = lcp_levels(c, c->key[s], c->key[e - 1]);
+  if(lbot >= md) {
+    c->err = FSPH_ERR_DUPLICATE_KEY;
+    return -1;
+  }
+  if(c->nnodes == c->node_cap) {
+    c->node_cap = c->node_cap ? 2 * c->node_cap : 1024;
+    c->nodes = (onode *)realloc(c->nodes, sizeof(onode) * c->node_cap);
+  }
+  int64_t me = c->nnodes++;
+  onode nd;
+  memset(&nd, 0, sizeof(nd));
+  nd.s = s;
+  nd.e = e;
+  nd.ltop = ltop;
+  nd.lbot = lbot;
+  /* children: split [s,e) by the digit at level lbot+1 */
+  int64_t i = s;
+  while(i < e) {
+    int dg = digit_of(c, c->key[i], lbot + 1);
+    int64_t j = i + 1;
+    while(j < e && digit_of(c, c->key[j], lbot + 1) == dg)
+      ++j;
+    if(j - i == 1) {
+      nd.child[nd.nchild++] = ~i;
+      c->edepth[i] = lbot + 1;
+    }
+    else {
+      int64_t ci = build_node(c, i, j, lbot + 1);
+      if(ci < 0)
+        return -1;
+      nd.child[nd.nchild++] = ci;
+    }
+    i = j;
+  }
+  /* compute_cofm (default_physics.h:59-119): entities first, then nodes,
+   * each in child order */
+  double coord[3] = {0, 0, 0};
+  double mass = 0, radius = 0, lap = 0;
+  int64_t sub = 0;
+  for(int d = 0; d < D; ++d) {
+    nd.bmax[d] = -DBL_MAX;
+    nd.bmin[d] = DBL_MAX;
+  }
+  for(int k = 0; k < nd.nchild; ++k) {
+    if(nd.child[k] >= 0)
+      continue;
+    int64_t p = ~nd.child[k];
+    for(int d = 0; d < D; ++d)
+      coord[d] += c->m[p] * c->x[d][p];
+    mass += c->m[p];
+    ++sub;
+    for(int d = 0; d < D; ++d) {
+      nd.bmin[d] = dmin_(nd.bmin[d], c->x[d][p] - c->h[p] / 2.);
+      nd.bmax[d] = dmax_(nd.bmax[d], c->x[d][p] + c->h[p] / 2.);
+    }
+  }
+  for(int k = 0; k < nd.nchild; ++k) {
+    if(nd.child[k] < 0)
+      continue;
+    const onode * ch = &c->nodes[nd.child[k]];
+    for(int d = 0; d < D; ++d)
+      coord[d] += ch->tmass * ch->tcom[d];
+    mass += ch->tmass;
+    sub += ch->sub;
+    for(int d = 0; d < D; ++d) {
+      nd.bmin[d] = dmin_(nd.bmin[d], ch->bmin[d]);
+      nd.bmax[d] = dmax_(nd.bmax[d], ch->bmax[d]);
+    }
+  }
+  for(int d = 0; d < D; ++d)
+    coord[d] /= mass;
+  for(int k = 0; k < nd.nchild; ++k) {
+    if(nd.child[k] >= 0)
+      continue;
+    int64_t p = ~nd.child[k];
+    double xp[3];
+    getx(c, p, xp);
+    double dist = dist_pts(D, coord, xp);
+    radius = dmax_(radius, dist);
+    lap = dmax_(lap, dist + c->h[p]);
+  }
+  for(int k = 0; k < nd.nchild; ++k) {
+    if(nd.child[k] < 0)
+      continue;
+    const onode * ch = &c->nodes[nd.child[k]];
+    double dist = dist_pts(D, coord, ch->tcom);
+    radius = dmax_(radius, dist + ch->tradius);
+    lap = dmax_(lap, dist + ch->tradius + ch->tlap);
+  }
+  for(int d = 0; d < D; ++d)
+    nd.com[d] = nd.tcom[d] = coord[d];
+  nd.mass = nd.tmass = mass;
+  nd.radius = nd.tradius = radius;
+  nd.lap = nd.tlap = lap;
+  nd.sub = sub;
+  for(int l = lbot; l > ltop; --l)
+    chain_up(D, nd.tcom, &nd.tmass, &nd.tradius, &nd.tlap);
+  c->nodes[me] = nd;
+  return me;
+}
+
+/* groups in the order traversal_sph visits them (tree_topology.h:220-235):
+ * depth-first, highest child first. */
+static void collect_groups(orc_ctx * c, int64_t node) {
+  const onode * nd = &c->nodes[node];
+  if(nd->sub <= GROUP_MAX) {
+    c->groups[c->ngroups++] = node;
+    return;
+  }
+  for(int k = nd->nchild - 1; k >= 0; --k) {
+    int64_t ch = c->nodes[node].child[k];
+    if(ch < 0)
+      c->groups[c->ngroups++] = ch;
+    else
+      collect_groups(c, ch);
+  }
+}
+
+int orc_update_iteration(orc_ctx * c) {
+  const int D = c->D;
+  const int64_t n = c->n;
+  if(n < 2)
+    return FSPH_ERR_STATE;
+  free_tree(c);
+  /* mpi_compute_range (bodies_system.h:231-268) */
+  double lo[3], hi[3];
+  for(int d = 0; d < D; ++d)
+    lo[d] = hi[d] = c->x[d][n - 1];
+  for(int64_t i = 0; i < n; ++i)
+    for(int d = 0; d < D; ++d) {
+      if(c->x[d][i] + c->h[i] > hi[d]) hi[d] = c->x[d][i] + c->h[i];
+      if(c->x[d][i] - c->h[i] < lo[d]) lo[d] = c->x[d][i] - c->h[i];
+    }
+  int same = 1;
+  for(int d = 0; d < D; ++d) {
+    c->range[0][d] = lo[d];
+    c->range[1][d] = hi[d];
+    if(lo[d] != hi[d]) same = 0;
+  }
+  if(same)
+    return FSPH_ERR_ARG;
+  /* keys: morton_curve_u(range, p) (filling_curve.h:503-525) */
+  const int md = max_depth_of(D);
+  const uint64_t one = 1;
+  const uint64_t max_val = (one << (63 / D)) - 1;
+  for(int64_t i = 0; i < n; ++i) {
+    uint64_t coords[3];
+    for(int d = 0; d < D; ++d) {
+      double mn = c->range[0][d];
+      double scale = c->range[1][d] - mn;
+      uint64_t q = (uint64_t)((c->x[d][i] - mn) / scale *
+                              (double)(one << (63 / D)));
+      coords[d] = q < max_val ? q : max_val;
+    }
+    uint64_t value = one << (md * D);
+    for(int l = 0; l < md; ++l)
+      for(int d = 0; d < D; ++d)
+        value |= ((coords[d] >> l) & one) << (l * D + d);
+    c->key[i] = value;
+  }
+  /* sort by (key, id) and permute every field */
+  sortrec * rec = (sortrec *)malloc(sizeof(sortrec) * n);
+  for(int64_t i = 0; i < n; ++i) {
+    rec[i].key = c->key[i];
+    rec[i].id = c->id[i];
+    rec[i].idx = i;
+  }
+  qsort(rec, n, sizeof(sortrec), cmp_sortrec);
+  double * tmp = (double *)malloc(8 * n);
+  for(int d = 0; d < 3; ++d) {
+    permute_d(&c->x[d], rec, n, tmp); permute_d(&c->v[d], rec, n, tmp);
+    permute_d(&c->vh[d], rec, n, tmp); permute_d(&c->a[d], rec, n, tmp);
+    permute_d(&c->ga[d], rec, n, tmp);
+  }
+  double ** fs[] = {&c->gpot, &c->m, &c->h, &c->rho, &c->P, &c->cs, &c->u,
+    &c->e, &c->dudt, &c->dedt, &c->K, &c->alpha, &c->vsig, &c->dtp};
+  for(size_t k = 0; k < sizeof(fs) / sizeof(fs[0]); ++k)
+    permute_d(fs[k], rec, n, tmp);
+  for(int64_t i = 0; i < n; ++i) {
+    c->id[i] = rec[i].id;
+    c->key[i] = rec[i].key;
+  }
+  free(tmp);
+  free(rec);
+  /* tree (tree_topology.h:878-997) */
+  c->edepth = (int *)xalloc(sizeof(int) * n);
+  c->err = FSPH_OK;
+  int64_t root = build_node(c, 0, n, 0);
+  if(root != 0 || c->err)
+    return c->err ? c->err : FSPH_ERR_STATE;
+  c->groups = (int64_t *)xalloc(sizeof(int64_t) * n);
+  c->ngroups = 0;
+  collect_groups(c, 0);
+  c->tree_ok = 1;
+  return FSPH_OK;
+}
+
+int orc_reset_ghosts(orc_ctx * c) {
+  /* bodies_system.h:273-275: clean + build_tree over unchanged keys.  The
+   * reference re-runs the build; repeat it so the CPU baseline pays the same
+   * cost (results are identical). */
+  if(!c->tree_ok)
+    return FSPH_ERR_STATE;
+  free(c->nodes);
+  c->nodes = NULL;
+  c->nnodes = c->node_cap = 0;
+  c->err = FSPH_OK;
+  build_node(c, 0, c->n, 0);
+  c->ngroups = 0;
+  collect_groups(c, 0);
+  return c->err;
+}
+
+/* -------------------------------------------------------- the walk -- */
+static int within_distance2(int D, const double * p1, const double * p2,
+  double r) {
+  double s = 0;
+  for(int d = 0; d < D; ++d)
+    s += (p1[d] - p2[d]) * (p1[d] - p2[d]);
+  return s <= r * r;
+}
+
+static int intersects_box_box(int D, const double * min1, const double * max1,
+  const double * min2, const double * max2) {
+  int sep = 0;
+  for(int d = 0; d < D; ++d)
+    sep |= (max1[d] < min2[d]);
+  for(int d = 0; d < D; ++d)
+    sep |= (max2[d] < min1[d]);
+  return !sep;
+}
+
+static int intersects_sphere_box(int D, const double * mn, const double * mx,
+  const double * ctr, double r) {
+  if(D == 3) { /* tree_geometry.h:329-341 */
+    double x[3];
+    for(int d = 0; d < 3; ++d)
+      x[d] = ctr[d] < mx[d] ? ctr[d] : mx[d];
+    for(int d = 0; d < 3; ++d)
+      x[d] = x[d] < mn[d] ? mn[d] : x[d];
+    double dist = (x[0] - ctr[0]) * (x[0] - ctr[0]) +
+                  (x[1] - ctr[1]) * (x[1] - ctr[1]) +
+                  (x[2] - ctr[2]) * (x[2] - ctr[2]);
+    return dist <= r * r;
+  }
+  /* 2D: tree_geometry.h:219-227, tol = 10 eps */
+  double x[2];
+  for(int d = 0; d < 2; ++d)
+    x[d] = dmax_(mn[d], dmin_(ctr[d], mx[d]));
+  double dist = dist_pts(2, x, ctr);
+  return dist - r <= DBL_EPSILON * 10.;
+}
+
+static void scratch_init(scratch * s) { memset(s, 0, sizeof(*s)); }
+
+static void scratch_free(scratch * s) {
+  free(s->q);
+  free(s->nq);
+  for(int k = 0; k < GROUP_MAX; ++k)
+    if(s->nb) free(s->nb[k]);
+  free(s->nb);
+  free(s->nbn);
+  free(s->nbcap);
+}
+
+static void push_nb(scratch * s, int k, int64_t v) {
+  if(s->nbn[k] == s->nbcap[k]) {
+    s->nbcap[k] = s->nbcap[k] ? 2 * s->nbcap[k] : 256;
+    s->nb[k] = (int64_t *)realloc(s->nb[k], sizeof(int64_t) * s->nbcap[k]);
+  }
+  s->nb[k][s->nbn[k]++] = v;
+}
+
+static void push_q(scratch * s, int64_t ** q, int64_t * qn, int64_t v) {
+  if(*qn == s->qcap) {
+    int64_t nc = s->qcap ? 2 * s->qcap : 4096;
+    s->q = (int64_t *)realloc(s->q, sizeof(int64_t) * nc);
+    s->nq = (int64_t *)realloc(s->nq, sizeof(int64_t) * nc);
+    s->qcap = nc;
+    *q = s->nq; /* caller always pushes into nq */
+  }
+  (*q)[(*qn)++] = v;
+}
+
+static const int * g_edepth_sort; /* for the (depth, index) sort */
+static int cmp_depth_idx(const void * a, const void * b) {
+  int64_t l = *(const int64_t *)a, r = *(const int64_t *)b;
+  int dl = g_edepth_sort[l], dr = g_edepth_sort[r];
+  if(dl != dr) return dl < dr ? -1 : 1;
+  return l < r ? -1 : (l > r ? 1 : 0);
+}
+
+static void sort_by_depth(const orc_ctx * c, int64_t * v, int64_t n) {
+  /* insertion sort on (edepth, index): lists are short and mostly ordered */
+  for(int64_t i = 1; i < n; ++i) {
+    int64_t x = v[i];
+    int dx = c->edepth[x];
+    int64_t j = i - 1;
+    while(j >= 0 &&
+          (c->edepth[v[j]] > dx || (c->edepth[v[j]] == dx && v[j] > x))) {
+      v[j + 1] = v[j];
+      --j;
+    }
+    v[j + 1] = x;
+  }
+  (void)cmp_depth_idx;
+}
+
+/* Neighbour search of one group (tree_topology.h:292-400).  Fills
+ * s->nb[k] for members k in cur_entities order (descending index); returns
+ * the member count and writes the members to `mem`. */
+static int walk_group(const orc_ctx * c, int64_t g, scratch * s, int64_t * mem) {
+  const int D = c->D;
+  int nm = 0;
+  const onode * G = NULL;
+  if(g >= 0) {
+    G = &c->nodes[g];
+    for(int64_t i = G->e - 1; i >= G->s; --i)
+      mem[nm++] = i;
+  }
+  else
+    mem[nm++] = ~g;
+  if(!s->nb) {
+    s->nb = (int64_t **)xalloc(sizeof(int64_t *) * GROUP_MAX);
+    s->nbn = (int64_t *)xalloc(sizeof(int64_t) * GROUP_MAX);
+    s->nbcap = (int64_t *)xalloc(sizeof(int64_t) * GROUP_MAX);
+  }
+  for(int k = 0; k < nm; ++k)
+    s->nbn[k] = 0;
+  double xm[GROUP_MAX][3];
+  for(int k = 0; k < nm; ++k)
+    getx(c, mem[k], xm[k]);
+  int64_t * q;
+  int64_t qn = 0, nqn;
+  if(s->qcap == 0) {
+    s->qcap = 4096;
+    s->q = (int64_t *)malloc(sizeof(int64_t) * s->qcap);
+    s->nq = (int64_t *)malloc(sizeof(int64_t) * s->qcap);
+  }
+  s->q[qn++] = 0; /* root */
+  while(qn > 0) {
+    nqn = 0;
+    q = s->nq;
+    for(int64_t j = 0; j < qn; ++j) {
+      int64_t cell = s->q[j];
+      if(cell >= 0) {
+        const onode * nd = &c->nodes[cell];
+        if(G && !intersects_box_box(D, nd->bmin, nd->bmax, G->bmin, G->bmax))
+          continue;
+        for(int k = 0; k < nm; ++k) {
+          if(intersects_sphere_box(D, nd->bmin, nd->bmax, xm[k], c->h[mem[k]])) {
+            for(int l = 0; l < nd->nchild; ++l)
+              push_q(s, &q, &nqn, nd->child[l]);
+            break;
+          }
+        }
+      }
+      else {
+        int64_t e = ~cell;
+        double xe[3];
+        getx(c, e, xe);
+        if(G) {
+          double extent = dmax_(c->h[e], G->tlap) + G->tradius;
+          if(!within_distance2(D, xe, G->tcom, extent))
+            continue;
+        }
+        for(int k = 0; k < nm; ++k) {
+          double extent = dmax_(c->h[mem[k]], c->h[e]);
+          if(within_distance2(D, xm[k], xe, extent))
+            push_nb(s, k, e);
+        }
+      }
+    }
+    /* swap queues */
+    int64_t * t = s->q;
+    s->q = s->nq;
+    s->nq = t;
+    qn = nqn;
+  }
+  for(int k = 0; k < nm; ++k)
+    sort_by_depth(c, s->nb[k], s->nbn[k]);
+  return nm;
+}
+
+/* ----------------------------------------------------- pair physics -- */
+/* compute_density + recover_internal_energy + EOS (default_physics.h:193-228,
+ * 126-145, 309-316); writes rho, u, P and the NEW sound speed into csnew. */
+static int density_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double h_a = c->h[a];
+  double pa[3];
+  getx(c, a, pa);
+  double rho_a = 0.0;
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double r = 0;
+    for(int d = 0; d < D; ++d) {
+      double dd = pa[d] - c->x[d][b];
+      r += dd * dd;
+    }
+    r = sqrt(r);
+    double Wab = kfun(c, r, .5 * (h_a + c->h[b]));
+    rho_a += c->m[b] * Wab;
+  }
+  if(!(rho_a > 0))
+    return FSPH_ERR_NEG_DENSITY;
+  c->rho[a] = rho_a;
+  if(c->p.evolve_internal_energy && c->p.thermokinetic_formulation) {
+    double vv = 0;
+    for(int d = 0; d < D; ++d)
+      vv += c->v[d][a] * c->v[d][a];
+    double ekin = .5 * vv;
+    double eint = c->e[a] - ekin - 0.0;
+    if(!(eint > 0))
+      return FSPH_ERR_NEG_ENERGY;
+    c->u[a] = eint;
+  }
+  double P, cs;
+  eos_pressure(c, a, c->u[a], &P, &cs);
+  c->P[a] = P;
+  c->csnew[a] = cs;
+  return FSPH_OK;
+}
+
+/* compute_signalspeed (default_physics.h:236-265) with the visiting-order
+ * rule for the neighbours' sound speed. */
+static void vsig_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double c_a = c->csnew[a];
+  double pa[3];
+  getx(c, a, pa);
+  double vsig = 0.0;
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pb[3];
+    getx(c, b, pb);
+    double dist = dist_pts(D, pa, pb);
+    double dotv = 0;
+    for(int d = 0; d < D; ++d) {
+      double n_d = (pa[d] - pb[d]) / dist;
+      double v_d = c->v[d][a] - c->v[d][b];
+      dotv += v_d * n_d;
+    }
+    double c_b = (b > a || b == a) ? c->csnew[b] : c->cs[b];
+    double cab = dmax_(c_a, c_b);
+    vsig = dmax_(vsig, cab - dmin_(dotv, 0.0));
+  }
+  c->vsig[a] = vsig;
+}
+
+/* compute_acceleration (default_physics.h:348-408) */
+static void accel_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double h_a = c->h[a], rho_a = c->rho[a], P_a = c->P[a], c_a = c->cs[a];
+  double pa[3], v12a[3];
+  getx(c, a, pa);
+  for(int d = 0; d < D; ++d)
+    v12a[d] = c->vh[d][a];
+  const double Prho2_a = P_a / (rho_a * rho_a);
+  double acc[3] = {0, 0, 0};
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pos_ab[3], v12_ab[3], DiWa[3];
+    int same = 1;
+    for(int d = 0; d < D; ++d) {
+      if(c->x[d][b] != pa[d]) same = 0;
+      pos_ab[d] = pa[d] - c->x[d][b];
+      v12_ab[d] = v12a[d] - c->vh[d][b];
+    }
+    double m_b = c->m[b] * (!same);
+    double h_ab = .5 * (h_a + c->h[b]);
+    double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
+    double rho_ab = .5 * (rho_a + c->rho[b]);
+    double c_ab = .5 * (c_a + c->cs[b]);
+    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    kgrad(c, pos_ab, h_ab, DiWa);
+    double Prho2_b = c->P[b] / (c->rho[b] * c->rho[b]);
+    double s = -m_b * (Prho2_a + Prho2_b + Pi);
+    for(int d = 0; d < D; ++d)
+      acc[d] += DiWa[d] * s;
+  }
+  for(int d = 0; d < D; ++d) {
+    c->a[d][a] = acc[d] + 0.0; /* + external_force::acceleration ("none") */
+    c->ga[d][a] = 0;
+  }
+  c->gpot[a] = 0;
+}
+
+/* compute_dudt (default_physics.h:421-487) */
+static void dudt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  if(c->iteration < c->p.relaxation_steps) {
+    c->dudt[a] = 0.0;
+    return;
+  }
+  const double h_a = c->h[a], rho_a = c->rho[a], P_a = c->P[a], c_a = c->cs[a];
+  double pa[3], va[3], v12a[3];
+  getx(c, a, pa);
+  for(int d = 0; d < D; ++d) {
+    va[d] = c->v[d][a];
+    v12a[d] = c->vh[d][a];
+  }
+  double dp = 0.0, dv = 0.0;
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pos_ab[3], v12_ab[3], vel_ab[3], DiWab[3];
+    int same = 1;
+    for(int d = 0; d < D; ++d) {
+      if(c->x[d][b] != pa[d]) same = 0;
+      pos_ab[d] = pa[d] - c->x[d][b];
+      v12_ab[d] = v12a[d] - c->vh[d][b];
+      vel_ab[d] = va[d] - c->v[d][b];
+    }
+    double m_b = c->m[b] * (!same);
+    double h_ab = .5 * (h_a + c->h[b]);
+    double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
+    double rho_ab = .5 * (rho_a + c->rho[b]);
+    double c_ab = .5 * (c_a + c->cs[b]);
+    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    kgrad(c, pos_ab, h_ab, DiWab);
+    double vdw = 0;
+    for(int d = 0; d < D; ++d)
+      vdw += vel_ab[d] * DiWab[d];
+    dp += m_b * vdw;
+    dv += m_b * vdw * Pi;
+  }
+  c->dudt[a] = P_a / (rho_a * rho_a) * dp + .5 * dv;
+}
+
+/* compute_dedt (default_physics.h:502-566) */
+static void dedt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double h_a = c->h[a], rho_a = c->rho[a], P_a = c->P[a], c_a = c->cs[a];
+  double pa[3], va[3], v12a[3];
+  getx(c, a, pa);
+  double gv = 0;
+  for(int d = 0; d < D; ++d) {
+    va[d] = c->v[d][a];
+    v12a[d] = c->vh[d][a];
+    gv += c->ga[d][a] * va[d];
+  }
+  const double Prho2_a = P_a / (rho_a * rho_a);
+  double dedt = 0;
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pos_ab[3], v12_ab[3], DiWab[3];
+    int same = 1;
+    for(int d = 0; d < D; ++d) {
+      if(c->x[d][b] != pa[d]) same = 0;
+      pos_ab[d] = pa[d] - c->x[d][b];
+      v12_ab[d] = v12a[d] - c->vh[d][b];
+    }
+    double m_b = c->m[b] * (!same);
+    double h_ab = .5 * (h_a + c->h[b]);
+    double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
+    double rho_ab = .5 * (rho_a + c->rho[b]);
+    double c_ab = .5 * (c_a + c->cs[b]);
+    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    kgrad(c, pos_ab, h_ab, DiWab);
+    double vad = 0, vbd = 0;
+    for(int d = 0; d < D; ++d)
+      vad += va[d] * DiWab[d];
+    for(int d = 0; d < D; ++d)
+      vbd += c->v[d][b] * DiWab[d];
+    double Prho2_b = c->P[b] / (c->rho[b] * c->rho[b]);
+    dedt -= m_b * (Prho2_a * vbd + vad * Prho2_b + .5 * Pi * (vbd + vad));
+  }
+  dedt += gv;
+  c->dedt[a] = dedt;
+}
+
+enum { PASS_DENSITY, PASS_VSIG, PASS_ACCEL, PASS_DUDT, PASS_DEDT };
+
+/* apply_in_smoothinglength: walk every group and apply the pass to its
+ * members (tree_topology.h:253-409). */
+static int run_pass(orc_ctx * c, int pass) {
+  if(!c->tree_ok)
+    return FSPH_ERR_STATE;
+  int status = FSPH_OK;
+  const int64_t ng = c->ngroups;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(c->nthreads)
+#endif
+  {
+    scratch s;
+    scratch_init(&s);
+    int64_t mem[GROUP_MAX];
+    int local = FSPH_OK;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for(int64_t g = 0; g < ng; ++g) {
+      int nm = walk_group(c, c->groups[g], &s, mem);
+      for(int k = 0; k < nm; ++k) {
+        int64_t a = mem[k];
+        switch(pass) {
+          case PASS_DENSITY: {
+            int st = density_one(c, a, s.nb[k], s.nbn[k]);
+            if(st && !local) local = st;
+            break;
+          }
+          case PASS_VSIG: vsig_one(c, a, s.nb[k], s.nbn[k]); break;
+          case PASS_ACCEL: accel_one(c, a, s.nb[k], s.nbn[k]); break;
+          case PASS_DUDT: dudt_one(c, a, s.nb[k], s.nbn[k]); break;
+          case PASS_DEDT: dedt_one(c, a, s.nb[k], s.nbn[k]); break;
+        }
+      }
+    }
+    scratch_free(&s);
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    {
+      if(local && !status) status = local;
+    }
+  }
+  return status;
+}
+
+int orc_density_pressure_soundspeed(orc_ctx * c) {
+  /* compute_density_pressure_soundspeed (default_physics.h:309-320).  The
+   * signal speed needs every new sound speed of the pass first; the visiting
+   * order rule inside vsig_one reproduces the reference's in-place update. */
+  int st = run_pass(c, PASS_DENSITY);
+  if(st)
+    return st;
+  run_pass(c, PASS_VSIG);
+  memcpy(c->cs, c->csnew, 8 * c->n);
+  return FSPH_OK;
+}
+
+int orc_acceleration(orc_ctx * c) { return run_pass(c, PASS_ACCEL); }
+int orc_dudt(orc_ctx * c) { return run_pass(c, PASS_DUDT); }
+int orc_dedt(orc_ctx * c) { return run_pass(c, PASS_DEDT); }
+
+/* ------------------------------------------------------- apply_all -- */
+int orc_eos_init(orc_ctx * c) {
+  /* eos_t<>::init -> compute_adiabatic (eos.h:67-92,157-159) */
+  for(int64_t i = 0; i < c->n; ++i)
+    c->K[i] = c->P[i] / pow(c->rho[i], c->p.poly_gamma);
+  return FSPH_OK;
+}
+
+int orc_set_total_energy(orc_ctx * c) {
+  /* default_physics.h:327-335 */
+  for(int64_t i = 0; i < c->n; ++i) {
+    double vv = 0;
+    for(int d = 0; d < c->D; ++d)
+      vv += c->v[d][i] * c->v[d][i];
+    double ekin = .5 * vv;
+    c->e[i] = ekin + c->u[i] + 0.0;
+  }
+  return FSPH_OK;
+}
+
+int orc_save_velocityhalf(orc_ctx * c) {
+  /* integration.h:52-55 */
+  for(int d = 0; d < c->D; ++d)
+    memcpy(c->vh[d], c->v[d], 8 * c->n);
+  return FSPH_OK;
+}
+
+int orc_leapfrog_kick_v(orc_ctx * c) {
+  /* integration.h:65-70 */
+  const double s = 0.5 * c->dt;
+  for(int64_t i = 0; i < c->n; ++i)
+    for(int d = 0; d < c->D; ++d)
+      c->v[d][i] = c->v[d][i] + (c->a[d][i] + c->ga[d][i]) * s;
+  return FSPH_OK;
+}
+
+int orc_leapfrog_kick_u(orc_ctx * c) {
+  /* integration.h:80-84 */
+  for(int64_t i = 0; i < c->n; ++i)
+    c->u[i] = c->u[i] + 0.5 * c->dt * c->dudt[i];
+  return FSPH_OK;
+}
+
+int orc_leapfrog_kick_e(orc_ctx * c) {
+  /* integration.h:94-98 */
+  for(int64_t i = 0; i < c->n; ++i)
+    c->e[i] = c->e[i] + 0.5 * c->dt * c->dedt[i];
+  return FSPH_OK;
+}
+
+int orc_leapfrog_drift(orc_ctx * c) {
+  /* integration.h:106-110 */
+  for(int64_t i = 0; i < c->n; ++i)
+    for(int d = 0; d < c->D; ++d)
+      c->x[d][i] = c->x[d][i] + c->v[d][i] * c->dt;
+  return FSPH_OK;
+}
+
+int orc_recompute_pressure_soundspeed(orc_ctx * c) {
+  /* default_physics.h:153-161 */
+  for(int64_t i = 0; i < c->n; ++i) {
+    double uint = c->u[i];
+    double P, cs;
+    eos_pressure(c, i, uint + 0.5 * c->dt * c->dudt[i], &P, &cs);
+    c->P[i] = P;
+    c->cs[i] = cs;
+  }
+  return FSPH_OK;
+}
+
+int orc_recompute_pressure_soundspeed_thermokinetic(orc_ctx * c) {
+  /* default_physics.h:169-182 */
+  for(int64_t i = 0; i < c->n; ++i) {
+    double vv = 0;
+    for(int d = 0; d < c->D; ++d)
+      vv += c->v[d][i] * c->v[d][i];
+    double ekin = .5 * vv;
+    double eint = c->e[i] - ekin - 0.0;
+    if(!(eint > 0))
+      return FSPH_ERR_NEG_ENERGY;
+    c->u[i] = eint;
+    double vda = 0;
+    for(int d = 0; d < c->D; ++d)
+      vda += c->v[d][i] * c->a[d][i];
+    double P, cs;
+    eos_pressure(c, i, eint + 0.5 * c->dt * (c->dedt[i] - vda), &P, &cs);
+    c->P[i] = P;
+    c->cs[i] = cs;
+  }
+  return FSPH_OK;
+}
+
+int orc_compute_dt(orc_ctx * c) {
+  /* default_physics.h:602-695 */
+  const double tiny = 1e-24, mc = 0.6;
+  const fsph_params * p = &c->p;
+  for(int64_t i = 0; i < c->n; ++i) {
+    const double dx = c->h[i] / (p->sph_eta * c->kernel_width);
+    double vn = 0;
+    for(int d = 0; d < c->D; ++d)
+      vn += c->v[d][i] * c->v[d][i];
+    vn = sqrt(vn);
+    const double dt_v = dx / (vn + tiny);
+    double acc = 0;
+    for(int d = 0; d < c->D; ++d) {
+      double ad = c->a[d][i] + c->ga[d][i];
+      acc += ad * ad;
+    }
+    acc = sqrt(acc);
+    const double dt_a = sqrt(dx / (acc + tiny));
+    const double dt_c =
+      dx / (tiny + c->vsig[i] * (1 + mc * p->sph_viscosity_alpha));
+    double dtmin = p->timestep_cfl_factor * dmin_(dmin_(dt_v, dt_a), dt_c);
+    if(p->evolve_internal_energy && p->thermokinetic_formulation) {
+      const double eint = c->u[i];
+      if(!(eint > 0))
+        return FSPH_ERR_NEG_ENERGY;
+      int it;
+      for(it = 0; it < 20; ++it) {
+        double gdv = 0;
+        for(int d = 0; d < c->D; ++d)
+          gdv += c->v[d][i] * c->ga[d][i];
+        double delta_epot = 0.0 - 0.0;
+        double delta_egrv = -dtmin * gdv;
+        if(delta_epot + delta_egrv < eint * 0.5)
+          break;
+        dtmin *= 0.25;
+      }
+      if(it >= 20)
+        return FSPH_ERR_DT;
+    }
+    c->dtp[i] = dtmin;
+  }
+  return FSPH_OK;
+}
+
+int orc_set_adaptive_timestep(orc_ctx * c) {
+  /* default_physics.h:761-823 */
+  const fsph_params * p = &c->p;
+  double dtmin = 1e24;
+  for(int64_t i = 0; i < c->n; ++i)
+    dtmin = dmin_(dtmin, c->dtp[i]);
+  if(dtmin < c->dt)
+    c->dt = dmin_(dtmin, c->dt / 2.0);
+  if(dtmin > 2.0 * c->dt)
+    c->dt = c->dt * 2.0;
+  c->totaltime_next = c->totaltime + c->dt;
+  if(p->out_screen_dt > 0) {
+    if(c->totaltime == c->t_screen) {
+      if(c->dt_saved > 0) c->dt = c->dt_saved;
+      c->t_screen += p->out_screen_dt;
+    }
+    if(c->totaltime + c->dt > c->t_screen - 0.1 * p->out_screen_dt) {
+      c->dt_saved = c->dt;
+      c->totaltime_next = c->t_screen;
+    }
+  }
+  if(p->out_scalar_dt > 0) {
+    if(c->totaltime == c->t_scalar) {
+      if(c->dt_saved > 0) c->dt = c->dt_saved;
+      c->t_scalar += p->out_scalar_dt;
+    }
+    if(c->totaltime + c->dt > c->t_scalar - 0.1 * p->out_scalar_dt) {
+      c->dt_saved = c->dt;
+      c->totaltime_next = dmin_(c->totaltime_next, c->t_scalar);
+    }
+  }
+  if(p->out_h5data_dt > 0) {
+    if(c->totaltime == c->t_h5) {
+      if(c->dt_saved > 0) c->dt = c->dt_saved;
+      c->t_h5 += p->out_h5data_dt;
+    }
+    if(c->totaltime + c->dt > c->t_h5 - 0.1 * p->out_h5data_dt) {
+      c->dt_saved = c->dt;
+      c->totaltime_next = dmin_(c->totaltime_next, c->t_h5);
+    }
+  }
+  c->dt = c->totaltime_next - c->totaltime;
+  return FSPH_OK;
+}
+
+int orc_compute_smoothinglength(orc_ctx * c) {
+  /* default_physics.h:825-848 */
+  for(int64_t i = 0; i < c->n; ++i) {
+    double q = c->m[i] / c->rho[i];
+    double r = (c->D == 3) ? cbrt(q) : sqrt(q);
+    c->h[i] = r * c->p.sph_eta * c->kernel_width;
+  }
+  return FSPH_OK;
+}
+
+int orc_compute_average_smoothinglength(orc_ctx * c) {
+  /* default_physics.h:879-898 */
+  orc_compute_smoothinglength(c);
+  double total = 0.;
+  for(int64_t i = 0; i < c->n; ++i)
+    total += c->h[i];
+  double new_h = 1. / (double)c->n * total;
+  for(int64_t i = 0; i < c->n; ++i)
+    c->h[i] = new_h;
+  return FSPH_OK;
+}
+
+int orc_check_nans(orc_ctx * c) {
+  /* default_physics.h:918-945 */
+  for(int64_t i = 0; i < c->n; ++i) {
+    for(int d = 0; d < c->D; ++d)
+      if(c->x[d][i] != c->x[d][i] || c->v[d][i] != c->v[d][i] ||
+         c->vh[d][i] != c->vh[d][i] || c->a[d][i] != c->a[d][i] ||
+         c->ga[d][i] != c->ga[d][i])
+        return FSPH_ERR_NAN;
+    double f[] = {c->m[i], c->gpot[i], c->rho[i], c->P[i], c->e[i], c->dedt[i],
+      c->dudt[i], c->K[i], c->vsig[i]};
+    for(size_t k = 0; k < sizeof(f) / sizeof(f[0]); ++k)
+      if(f[k] != f[k])
+        return FSPH_ERR_NAN;
+    if(c->p.evolve_internal_energy && c->u[i] != c->u[i])
+      return FSPH_ERR_NAN;
+  }
+  return FSPH_OK;
+}
+
+int orc_check_negativity(orc_ctx * c) {
+  /* default_physics.h:953-979 */
+  for(int64_t i = 0; i < c->n; ++i)
+    if(c->rho[i] < 0 || c->P[i] < 0 ||
+       (c->p.evolve_internal_energy && c->u[i] < 0))
+      return FSPH_ERR_NEGATIVITY;
+  return FSPH_OK;
+}
+
+int orc_advance_time(orc_ctx * c) {
+  /* default_physics.h:853-860 */
+  c->iteration++;
+  if(c->p.adaptive_timestep)
+    c->totaltime = c->totaltime_next;
+  else
+    c->totaltime = c->totaltime + c->dt;
+  return FSPH_OK;
+}
+
+int orc_gravity_direct(orc_ctx * c, int64_t s0, int64_t s1) {
+  /* fmm::gravitation_p2p (fmm.h:37-46) summed over every source, skipping
+   * the sink's own id (fmm.h:136-137). */
+  const int D = c->D;
+  const double G = c->p.gravitational_constant;
+  if(s0 < 0 || s1 > c->n || s0 > s1)
+    return FSPH_ERR_ARG;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(c->nthreads)
+#endif
+  for(int64_t i = s0; i < s1; ++i) {
+    double pi[3], acc[3] = {0, 0, 0}, pot = 0;
+    getx(c, i, pi);
+    for(int64_t j = 0; j < c->n; ++j) {
+      if(c->id[j] == c->id[i])
+        continue;
+      double pj[3];
+      getx(c, j, pj);
+      double dist = dist_pts(D, pi, pj);
+      pot += -G * c->m[j] / dist;
+      double f = -G * c->m[j] / (dist * dist * dist);
+      for(int d = 0; d < D; ++d)
+        acc[d] += f * (pi[d] - pj[d]);
+    }
+    for(int d = 0; d < D; ++d)
+      c->ga[d][i] = acc[d];
+    c->gpot[i] = pot;
+  }
+  return FSPH_OK;
+}
+
+#define TRY(x)                                                                 \
+  do {                                                                         \
+    int st_ = (x);                                                             \
+    if(st_) return st_;                                                        \
+  } while(0)
+
+/* One iteration of mpi_init_task's loop (hydro/main_driver.cc:98-279;
+ * newtonian/main_driver.cc:98-298 when enable_fmm, with direct-summation
+ * gravity standing in for the FMM). */
+int orc_step(orc_ctx * c) {
+  const fsph_params * p = &c->p;
+  if(p->relaxation_steps != 0 || p->sph_viscosity != FSPH_VISC_CONSTANT)
+    return FSPH_ERR_ARG;
+  if(c->iteration == p->initial_iteration) {
+    TRY(orc_update_iteration(c));
+    TRY(orc_eos_init(c));
+    if(p->thermokinetic_formulation)
+      TRY(orc_set_total_energy(c));
+    TRY(orc_density_pressure_soundspeed(c));
+    TRY(orc_save_velocityhalf(c));
+    TRY(orc_reset_ghosts(c));
+    TRY(orc_acceleration(c));
+    if(p->enable_fmm)
+      TRY(orc_gravity_direct(c, 0, c->n));
+    if(p->thermokinetic_formulation && p->enable_fmm)
+      TRY(orc_set_total_energy(c));
+    if(p->adaptive_timestep) {
+      TRY(orc_compute_dt(c));
+      TRY(orc_set_adaptive_timestep(c));
+    }
+    if(p->evolve_internal_energy) {
+      for(int m = 1; m <= p->pressure_updates_number; ++m) {
+        if(p->thermokinetic_formulation) {
+          TRY(orc_dedt(c));
+          TRY(orc_recompute_pressure_soundspeed_thermokinetic(c));
+        }
+        else {
+          TRY(orc_dudt(c));
+          TRY(orc_recompute_pressure_soundspeed(c));
+        }
+        if(m < p->pressure_updates_number)
+          TRY(orc_reset_ghosts(c));
+      }
+    }
+  }
+  else {
+    if(p->evolve_internal_energy) {
+      if(p->thermokinetic_formulation)
+        TRY(orc_leapfrog_kick_e(c));
+      else
+        TRY(orc_leapfrog_kick_u(c));
+    }
+    TRY(orc_leapfrog_kick_v(c));
+    TRY(orc_save_velocityhalf(c));
+    TRY(orc_leapfrog_drift(c));
+    TRY(orc_update_iteration(c));
+    TRY(orc_density_pressure_soundspeed(c));
+    TRY(orc_reset_ghosts(c));
+    TRY(orc_acceleration(c));
+    if(p->enable_fmm)
+      TRY(orc_gravity_direct(c, 0, c->n));
+    TRY(orc_leapfrog_kick_v(c));
+    TRY(orc_reset_ghosts(c));
+    if(p->evolve_internal_energy) {
+      for(int m = 1; m <= p->pressure_updates_number; ++m) {
+        if(p->thermokinetic_formulation) {
+          TRY(orc_dedt(c));
+          TRY(orc_recompute_pressure_soundspeed_thermokinetic(c));
+        }
+        else {
+          TRY(orc_dudt(c));
+          TRY(orc_recompute_pressure_soundspeed(c));
+        }
+        if(m < p->pressure_updates_number)
+          TRY(orc_reset_ghosts(c));
+      }
+      if(p->thermokinetic_formulation)
+        TRY(orc_leapfrog_kick_e(c));
+      else
+        TRY(orc_leapfrog_kick_u(c));
+    }
+  }
+  if(p->sph_variable_h)
+    TRY(orc_compute_smoothinglength(c));
+  else if(p->sph_update_uniform_h)
+    TRY(orc_compute_average_smoothinglength(c));
+  TRY(orc_check_nans(c));
+  TRY(orc_check_negativity(c));
+  if(p->adaptive_timestep) {
+    TRY(orc_compute_dt(c));
+    TRY(orc_set_adaptive_timestep(c));
+  }
+  return orc_advance_time(c);
+}
+
+int orc_get_neighbors(orc_ctx * c, int64_t * offsets, int64_t * indices,
+  int64_t capacity) {
+  if(!c->tree_ok)
+    return FSPH_ERR_STATE;
+  scratch s;
+  scratch_init(&s);
+  int64_t mem[GROUP_MAX];
+  /* counts first */
+  int64_t * cnt = (int64_t *)xalloc(sizeof(int64_t) * c->n);
+  for(int64_t g = 0; g < c->ngroups; ++g) {
+    int nm = walk_group(c, c->groups[g], &s, mem);
+    for(int k = 0; k < nm; ++k)
+      cnt[mem[k]] = s.nbn[k];
+  }
+  offsets[0] = 0;
+  for(int64_t i = 0; i < c->n; ++i)
+    offsets[i + 1] = offsets[i] + cnt[i];
+  free(cnt);
+  if(indices) {
+    if(offsets[c->n] > capacity) {
+      scratch_free(&s);
+      return FSPH_ERR_ARG;
+    }
+    for(int64_t g = 0; g < c->ngroups; ++g) {
+      int nm = walk_group(c, c->groups[g], &s, mem);
+      for(int k = 0; k < nm; ++k)
+        memcpy(indices + offsets[mem[k]], s.nb[k], 8 * s.nbn[k]);
+    }
+  }
+  scratch_free(&s);
+  return FSPH_OK;
+}
+
+int orc_get_order(orc_ctx * c, int64_t * order) {
+  if(!c->tree_ok)
+    return FSPH_ERR_STATE;
+  int64_t k = 0;
+  for(int64_t g = 0; g < c->ngroups; ++g) {
+    int64_t gg = c->groups[g];
+    if(gg < 0)
+      order[k++] = ~gg;
+    else
+      for(int64_t i = c->nodes[gg].e - 1; i >= c->nodes[gg].s; --i)
+        order[k++] = i;
+  }
+  return FSPH_OK;
+}

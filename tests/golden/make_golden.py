@@ -1,0 +1,91 @@
+"""Generate the golden fixtures from the reference itself.
+
+Runs the laristra/flecsph hot path compiled here (oracle/_ref, built from the
+reference sources by oracle/Makefile) on small seeded inputs and stores
+inputs and outputs as compressed .npz files next to this script:
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+Each fixture holds: the input state (in a shuffled order), the parameter
+block, and after update_iteration the Morton keys, sorted ids, range and
+neighbour lists (CSR, in the reference's own order) plus the processing
+order of apply_in_smoothinglength; then the full state and (dt, time,
+iteration) after each of `steps` driver iterations.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from flecsph_gb300 import setups  # noqa: E402
+from flecsph_gb300.abi import DOUBLE_FIELDS, KERNEL_WENDLAND_C4  # noqa: E402
+import pyoracle  # noqa: E402
+
+
+def cases():
+    s, p, m = setups.sod3d(40, 10, 10)
+    yield "sod3d_4000", setups.shuffled(s, 1), p, 3
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.thermokinetic_formulation = 0
+    yield "sod3d_dudt_4000", setups.shuffled(s, 2), p, 2
+    s, p, m = setups.sedov3d(16)
+    yield "sedov3d_4096", setups.shuffled(s, 3), p, 2
+    s, p, m = setups.polytrope3d(3000)
+    p.enable_fmm = 0
+    p.sph_variable_h = 1
+    yield "polytrope3d_varh_3000", s, p, 2
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.sph_kernel = KERNEL_WENDLAND_C4
+    yield "sod3d_c4_4000", setups.shuffled(s, 4), p, 2
+    s, p, m = setups.sod2d(100, 10)
+    yield "sod2d_1000", setups.shuffled(s, 5), p, 2
+    s, p, m = setups.noh2d(40)
+    yield "noh2d_1264", setups.shuffled(s, 6), p, 2
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not pyoracle.build_ref(ref_root):
+        sys.exit(f"reference sources not found at {ref_root}")
+    for name, state, params, steps in cases():
+        o = pyoracle.Oracle("reference", params)
+        o.upload(state)
+        out = {}
+        for f in DOUBLE_FIELDS + ["id"]:
+            out["in_" + f] = state[f]
+        o.update_iteration()
+        upd = o.download()
+        out["upd_key"] = upd["key"]
+        out["upd_id"] = upd["id"]
+        out["upd_range"] = o.range()
+        off, idx = o.neighbors()
+        out["nb_offsets"] = off.astype(np.int64)
+        out["nb_indices"] = idx.astype(np.int32)
+        out["order"] = o.order().astype(np.int32)
+        # restart from the input so the steps start at the initial iteration
+        o.close()
+        o = pyoracle.Oracle("reference", params)
+        o.upload(state)
+        for k in range(steps):
+            o.step()
+            st = o.download()
+            for f in DOUBLE_FIELDS + ["id"]:
+                out[f"s{k}_{f}"] = st[f]
+            out[f"s{k}_time"] = np.array(o.time()[:2])
+            out[f"s{k}_iteration"] = np.array(o.time()[2])
+        out["params_json"] = np.array(json.dumps(params.as_dict()))
+        out["steps"] = np.array(steps)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **out)
+        o.close()
+        print(f"{name}: n={len(state['x'])} steps={steps} -> {os.path.getsize(path)} bytes")
+
+
+if __name__ == "__main__":
+    main()
