@@ -1,0 +1,861 @@
+// fsph_api.cu -- the C ABI (include/fsph.h): context, data movement and the
+// body_system / physics call surface, sequenced on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fsph_internal.cuh"
+
+using namespace fsph;
+
+namespace {
+
+const int GROUP_MAX = 32;
+
+struct TimerRec {
+  int phase;
+  int e0, e1;
+};
+
+}  // namespace
+
+struct fsph_ctx {
+  fsph_params p;
+  PhysParams pp;
+  int device = 0;
+  int nsm = 152;
+  cudaStream_t stream = nullptr;
+  int64_t cap = 0;
+  int n = 0;
+  Particles P{}, Palt{};
+  double * cs_new = nullptr;
+  unsigned long long * skeys = nullptr;
+  unsigned long long * skeys_tmp = nullptr;
+  int * svals = nullptr;
+  int * svals_tmp = nullptr;
+  unsigned * hist = nullptr;
+  unsigned long long * d_range = nullptr;
+  Tree T{};
+  Lists Ls{};
+  DevTime * d_time = nullptr;
+  DevStatus * d_status = nullptr;
+  double * d_cons = nullptr;
+  int64_t iteration = 0;
+  bool tree_ok = false;
+  bool uploaded = false;
+  long long launches = 0;
+  // timers
+  bool timing = false;
+  std::vector<cudaEvent_t> events;
+  int ev_used = 0;
+  std::vector<TimerRec> pending;
+  double timer_ms[FSPH_TIMER_COUNT] = {0};
+  long long timer_calls[FSPH_TIMER_COUNT] = {0};
+  std::string last_error;
+  std::vector<void *> allocs;
+
+  Launch L() { return Launch{stream, &launches}; }
+};
+
+namespace {
+
+fsph_status cuda_fail(fsph_ctx * c, cudaError_t e, const char * where) {
+  if(c) {
+    c->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  }
+  return e == cudaErrorMemoryAllocation ? FSPH_ERR_OOM : FSPH_ERR_CUDA;
+}
+
+#define CK(expr)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if(e_ != cudaSuccess)                                                      \
+      return cuda_fail(c, e_, #expr);                                          \
+  } while(0)
+
+template<class T>
+cudaError_t dalloc(fsph_ctx * c, T ** p, size_t count) {
+  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+  if(e == cudaSuccess)
+    c->allocs.push_back(*p);
+  return e;
+}
+
+void phase_begin(fsph_ctx * c, int phase, int * tok) {
+  *tok = -1;
+  if(!c->timing)
+    return;
+  if(c->ev_used + 2 > (int)c->events.size()) {
+    // flush: everything recorded so far is accumulated
+    cudaStreamSynchronize(c->stream);
+    for(auto & r : c->pending) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->events[r.e0], c->events[r.e1]);
+      c->timer_ms[r.phase] += ms;
+      c->timer_calls[r.phase] += 1;
+    }
+    c->pending.clear();
+    c->ev_used = 0;
+  }
+  *tok = c->ev_used;
+  cudaEventRecord(c->events[c->ev_used++], c->stream);
+  (void)phase;
+}
+
+void phase_end(fsph_ctx * c, int phase, int tok) {
+  if(!c->timing || tok < 0)
+    return;
+  int e1 = c->ev_used++;
+  cudaEventRecord(c->events[e1], c->stream);
+  c->pending.push_back(TimerRec{phase, tok, e1});
+}
+
+struct Phase {
+  fsph_ctx * c;
+  int phase, tok;
+  Phase(fsph_ctx * c_, int ph) : c(c_), phase(ph) { phase_begin(c, ph, &tok); }
+  ~Phase() { phase_end(c, phase, tok); }
+};
+
+void make_phys(const fsph_params * p, PhysParams * pp) {
+  pp->dim = p->dimension;
+  pp->kernel = p->sph_kernel;
+  pp->eos = p->eos_type;
+  pp->thermokinetic = p->thermokinetic_formulation;
+  pp->evolve_u = p->evolve_internal_energy;
+  pp->adaptive = p->adaptive_timestep;
+  pp->gamma = p->poly_gamma;
+  pp->eta = p->sph_eta;
+  pp->kw = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE) ? 3.0 : 2.0;
+  pp->alpha = p->sph_viscosity_alpha;
+  pp->beta = p->sph_viscosity_beta;
+  pp->eps = p->sph_viscosity_epsilon;
+  pp->cfl = p->timestep_cfl_factor;
+  pp->out_screen_dt = p->out_screen_dt;
+  pp->out_scalar_dt = p->out_scalar_dt;
+  pp->out_h5data_dt = p->out_h5data_dt;
+  pp->G = p->gravitational_constant;
+}
+
+// analysis::set_initial_time_iteration (analysis.h:221-249)
+void init_time(const fsph_params * p, DevTime * t) {
+  memset(t, 0, sizeof(*t));
+  t->iteration = p->initial_iteration;
+  t->totaltime = p->initial_time;
+  t->dt = p->initial_dt;
+  auto snap = [&](double every, double * slot) {
+    if(every > 0.0) {
+      *slot = every * (double)((int64_t)(t->totaltime / every));
+      if(*slot < t->totaltime)
+        *slot = t->totaltime;
+    }
+  };
+  snap(p->out_screen_dt, &t->t_screen);
+  snap(p->out_scalar_dt, &t->t_scalar);
+  snap(p->out_h5data_dt, &t->t_h5);
+}
+
+bool params_supported(const fsph_params * p, std::string * why) {
+  if(p->dimension != 2 && p->dimension != 3) {
+    *why = "dimension must be 2 or 3";
+    return false;
+  }
+  if(p->sph_kernel != FSPH_KERNEL_CUBIC_SPLINE &&
+     p->sph_kernel != FSPH_KERNEL_WENDLAND_C2 &&
+     p->sph_kernel != FSPH_KERNEL_WENDLAND_C4 &&
+     p->sph_kernel != FSPH_KERNEL_WENDLAND_C6) {
+    *why = "sph_kernel not implemented";
+    return false;
+  }
+  if(p->eos_type != FSPH_EOS_IDEAL && p->eos_type != FSPH_EOS_POLYTROPIC) {
+    *why = "eos_type not implemented";
+    return false;
+  }
+  if(p->sph_viscosity != FSPH_VISC_CONSTANT) {
+    *why = "only visc_constant";
+    return false;
+  }
+  if(p->relaxation_steps != 0) {
+    *why = "relaxation_steps must be 0";
+    return false;
+  }
+  if(p->periodic_boundary_x || p->periodic_boundary_y || p->periodic_boundary_z) {
+    *why = "periodic boundaries not implemented";
+    return false;
+  }
+  if(p->max_neighbors < 8 || p->max_neighbors > 4096) {
+    *why = "max_neighbors out of [8, 4096]";
+    return false;
+  }
+  if(p->precision_mode != FSPH_PRECISION_FP64 &&
+     p->precision_mode != FSPH_PRECISION_MIXED) {
+    *why = "precision_mode";
+    return false;
+  }
+  return true;
+}
+
+fsph_status set_device(fsph_ctx * c) {
+  CK(cudaSetDevice(c->device));
+  return FSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fsph_params_default(fsph_params * p) {
+  memset(p, 0, sizeof(*p));
+  p->dimension = 3;
+  p->sph_kernel = FSPH_KERNEL_WENDLAND_C4;
+  p->eos_type = FSPH_EOS_IDEAL;
+  p->sph_viscosity = FSPH_VISC_CONSTANT;
+  p->poly_gamma = 1.4;
+  p->sph_eta = 1.5;
+  p->sph_viscosity_alpha = 1.0;
+  p->sph_viscosity_beta = 2.0;
+  p->sph_viscosity_epsilon = 0.01;
+  p->timestep_cfl_factor = 0.25;
+  p->initial_dt = 0.001;
+  p->gravitational_constant = 1.0;
+  p->box_length = 3.0;
+  p->box_width = 1.0;
+  p->box_height = 1.0;
+  p->thermokinetic_formulation = 1;
+  p->evolve_internal_energy = 1;
+  p->pressure_updates_number = 1;
+  p->precision_mode = FSPH_PRECISION_FP64;
+  p->max_neighbors = 256;
+  p->gravity_order = 2;
+}
+
+int32_t fsph_abi_version(void) { return FSPH_ABI_VERSION; }
+
+const char * fsph_status_string(int32_t s) {
+  switch(s) {
+    case FSPH_OK: return "FSPH_OK";
+    case FSPH_ERR_ARG: return "FSPH_ERR_ARG";
+    case FSPH_ERR_CUDA: return "FSPH_ERR_CUDA";
+    case FSPH_ERR_NAN: return "FSPH_ERR_NAN";
+    case FSPH_ERR_NEG_DENSITY: return "FSPH_ERR_NEG_DENSITY";
+    case FSPH_ERR_NEG_ENERGY: return "FSPH_ERR_NEG_ENERGY";
+    case FSPH_ERR_NEGATIVITY: return "FSPH_ERR_NEGATIVITY";
+    case FSPH_ERR_LIST_OVERFLOW: return "FSPH_ERR_LIST_OVERFLOW";
+    case FSPH_ERR_STACK_OVERFLOW: return "FSPH_ERR_STACK_OVERFLOW";
+    case FSPH_ERR_TIMEOUT: return "FSPH_ERR_TIMEOUT";
+    case FSPH_ERR_DUPLICATE_KEY: return "FSPH_ERR_DUPLICATE_KEY";
+    case FSPH_ERR_DT: return "FSPH_ERR_DT";
+    case FSPH_ERR_STATE: return "FSPH_ERR_STATE";
+    case FSPH_ERR_NO_DEVICE: return "FSPH_ERR_NO_DEVICE";
+    case FSPH_ERR_OOM: return "FSPH_ERR_OOM";
+  }
+  return "unknown";
+}
+
+const char * fsph_last_error(const fsph_ctx * c) {
+  return c ? c->last_error.c_str() : "";
+}
+
+fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
+  fsph_status * status) {
+  fsph_status dummy;
+  if(!status)
+    status = &dummy;
+  std::string why;
+  if(!p || capacity < 2 || capacity > (int64_t)1 << 30 || !params_supported(p, &why)) {
+    *status = FSPH_ERR_ARG;
+    return nullptr;
+  }
+  int ndev = 0;
+  if(cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    *status = FSPH_ERR_NO_DEVICE;
+    return nullptr;
+  }
+  fsph_ctx * c = new fsph_ctx();
+  c->p = *p;
+  make_phys(p, &c->pp);
+  c->device = device;
+  c->cap = capacity;
+  auto fail = [&](fsph_status s) {
+    fsph_destroy(c);
+    *status = s;
+    return (fsph_ctx *)nullptr;
+  };
+  if(cudaSetDevice(device) != cudaSuccess)
+    return fail(FSPH_ERR_CUDA);
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FSPH_ERR_CUDA);
+  const size_t N = (size_t)capacity;
+  const size_t Npad = (N + 31) / 32 * 32;
+  bool ok = true;
+  for(int k = 0; k < NF; ++k) {
+    ok &= dalloc(c, &c->P.f[k], N) == cudaSuccess;
+    ok &= dalloc(c, &c->Palt.f[k], N) == cudaSuccess;
+  }
+  ok &= dalloc(c, &c->P.id, N) == cudaSuccess;
+  ok &= dalloc(c, &c->Palt.id, N) == cudaSuccess;
+  ok &= dalloc(c, &c->P.key, N) == cudaSuccess;
+  ok &= dalloc(c, &c->Palt.key, N) == cudaSuccess;
+  ok &= dalloc(c, &c->cs_new, N) == cudaSuccess;
+  ok &= dalloc(c, &c->skeys, N) == cudaSuccess;
+  ok &= dalloc(c, &c->skeys_tmp, N) == cudaSuccess;
+  ok &= dalloc(c, &c->svals, N) == cudaSuccess;
+  ok &= dalloc(c, &c->svals_tmp, N) == cudaSuccess;
+  ok &= dalloc(c, &c->hist, radix_hist_entries((int)N)) == cudaSuccess;
+  ok &= dalloc(c, &c->d_range, 8) == cudaSuccess;
+  ok &= dalloc(c, &c->T.left, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.right, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.parent, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.leaf_parent, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.first, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.last, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.box, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.box2, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.opar, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.gref, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.counter, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.edepth, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.group_first, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.group_last, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.ngroups, 1) == cudaSuccess;
+  c->Ls.maxnb = p->max_neighbors;
+  ok &= dalloc(c, &c->Ls.idx, Npad * (size_t)p->max_neighbors) == cudaSuccess;
+  ok &= dalloc(c, &c->Ls.cnt, N) == cudaSuccess;
+  ok &= dalloc(c, &c->d_time, 1) == cudaSuccess;
+  ok &= dalloc(c, &c->d_status, 1) == cudaSuccess;
+  ok &= dalloc(c, &c->d_cons, 8) == cudaSuccess;
+  if(!ok) {
+    cudaGetLastError();
+    return fail(FSPH_ERR_OOM);
+  }
+  if(cudaMemset(c->d_status, 0, sizeof(DevStatus)) != cudaSuccess)
+    return fail(FSPH_ERR_CUDA);
+  c->events.resize(4096);
+  for(auto & e : c->events)
+    if(cudaEventCreate(&e) != cudaSuccess)
+      return fail(FSPH_ERR_CUDA);
+  *status = FSPH_OK;
+  return c;
+}
+
+void fsph_destroy(fsph_ctx * c) {
+  if(!c)
+    return;
+  cudaSetDevice(c->device);
+  if(c->stream)
+    cudaStreamSynchronize(c->stream);
+  for(void * p : c->allocs)
+    cudaFree(p);
+  for(auto & e : c->events)
+    if(e)
+      cudaEventDestroy(e);
+  if(c->stream)
+    cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
+  if(!c || !v || v->n < 2 || v->n > c->cap || !v->x || !v->y ||
+     (c->p.dimension == 3 && !v->z) || !v->m || !v->h || !v->id)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  const int n = (int)v->n;
+  c->n = n;
+  c->P.n = c->Palt.n = n;
+  const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
+    v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
+    v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
+    v->vsig, v->dt};
+  for(int k = 0; k < NF; ++k) {
+    if(src[k])
+      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
+        cudaMemcpyHostToDevice, c->stream));
+    else
+      CK(cudaMemsetAsync(c->P.f[k], 0, sizeof(double) * n, c->stream));
+  }
+  CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n,
+    cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->P.key, 0, sizeof(unsigned long long) * n, c->stream));
+  DevTime t;
+  init_time(&c->p, &t);
+  CK(cudaMemcpyAsync(c->d_time, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(DevStatus), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->iteration = c->p.initial_iteration;
+  c->tree_ok = false;
+  c->uploaded = true;
+  return FSPH_OK;
+}
+
+fsph_status fsph_sync(fsph_ctx * c) {
+  if(!c)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaGetLastError());
+  DevStatus st;
+  CK(cudaMemcpy(&st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+  if(st.code) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "%s at particle %lld",
+      fsph_status_string(st.code), st.index);
+    c->last_error = buf;
+    CK(cudaMemset(c->d_status, 0, sizeof(DevStatus)));
+    return (fsph_status)st.code;
+  }
+  return FSPH_OK;
+}
+
+fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
+  if(!c || !v || v->n != c->n || !c->uploaded)
+    return FSPH_ERR_ARG;
+  fsph_status s = fsph_sync(c);
+  if(s)
+    return s;
+  const int n = c->n;
+  double * dst[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx, v->vhy,
+    v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m, v->h,
+    v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha, v->vsig,
+    v->dt};
+  for(int k = 0; k < NF; ++k) {
+    if(k == F_Z || k == F_VZ || k == F_VHZ || k == F_AZ || k == F_GAZ)
+      if(c->p.dimension == 2)
+        continue;
+    if(dst[k])
+      CK(cudaMemcpyAsync(dst[k], c->P.f[k], sizeof(double) * n,
+        cudaMemcpyDeviceToHost, c->stream));
+  }
+  if(v->id)
+    CK(cudaMemcpyAsync(v->id, c->P.id, sizeof(long long) * n,
+      cudaMemcpyDeviceToHost, c->stream));
+  if(v->key)
+    CK(cudaMemcpyAsync(v->key, c->P.key, sizeof(unsigned long long) * n,
+      cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return FSPH_OK;
+}
+
+fsph_status fsph_get_time(fsph_ctx * c, double * dt, double * tt,
+  int64_t * it) {
+  fsph_status s = fsph_sync(c);
+  if(s)
+    return s;
+  DevTime t;
+  CK(cudaMemcpy(&t, c->d_time, sizeof(t), cudaMemcpyDeviceToHost));
+  if(dt) *dt = t.dt;
+  if(tt) *tt = t.totaltime;
+  if(it) *it = t.iteration;
+  return FSPH_OK;
+}
+
+fsph_status fsph_set_time(fsph_ctx * c, double dt, double tt, int64_t it) {
+  fsph_status s = fsph_sync(c);
+  if(s)
+    return s;
+  DevTime t;
+  CK(cudaMemcpy(&t, c->d_time, sizeof(t), cudaMemcpyDeviceToHost));
+  t.dt = dt;
+  t.totaltime = tt;
+  t.iteration = it;
+  CK(cudaMemcpy(c->d_time, &t, sizeof(t), cudaMemcpyHostToDevice));
+  c->iteration = it;
+  return FSPH_OK;
+}
+
+fsph_status fsph_get_range(fsph_ctx * c, double * range) {
+  if(!c || !range || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = fsph_sync(c);
+  if(s)
+    return s;
+  unsigned long long bits[6];
+  CK(cudaMemcpy(bits, c->d_range, sizeof(bits), cudaMemcpyDeviceToHost));
+  const int D = c->p.dimension;
+  for(int k = 0; k < 2; ++k)
+    for(int d = 0; d < D; ++d) {
+      unsigned long long u = bits[3 * k + d];
+      long long b = (u & 0x8000000000000000ull)
+                      ? (long long)(u & 0x7fffffffffffffffull)
+                      : (long long)~u;
+      double x;
+      memcpy(&x, &b, 8);
+      range[k * D + d] = x;
+    }
+  return FSPH_OK;
+}
+
+// ------------------------------------------------------------ body_system
+fsph_status fsph_update_iteration(fsph_ctx * c) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  const int n = c->n;
+  {
+    Phase ph(c, FSPH_TIMER_RANGE_KEYS);
+    CK(launch_range_keys(L, c->P, c->pp, (double *)c->d_range, c->skeys, c->svals));
+  }
+  {
+    Phase ph(c, FSPH_TIMER_SORT);
+    CK(radix_sort_pairs(L, c->skeys, c->svals, c->skeys_tmp, c->svals_tmp, n,
+      c->hist, 0));
+    CK(launch_check_duplicates(L, c->skeys, n, c->d_status));
+    CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys));
+    Particles t = c->P;
+    c->P = c->Palt;
+    c->Palt = t;
+  }
+  {
+    Phase ph(c, FSPH_TIMER_TREE);
+    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX));
+  }
+  {
+    Phase ph(c, FSPH_TIMER_NEIGHBORS);
+    CK(launch_neighbors(L, c->P, c->pp, c->T, c->Ls, c->d_status, c->nsm,
+      c->d_range));
+  }
+  c->tree_ok = true;
+  return FSPH_OK;
+}
+
+fsph_status fsph_reset_ghosts(fsph_ctx * c) {
+  // bodies_system::reset_ghosts rebuilds the tree over unchanged keys to
+  // refresh MPI ghosts (mpisph/bodies_system.h:273-275); on one device the
+  // tree and the neighbour lists it would produce are the ones held already.
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  return FSPH_OK;
+}
+
+fsph_status fsph_density_pressure_soundspeed(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  {
+    Phase ph(c, FSPH_TIMER_DENSITY);
+    CK(launch_density_fp64(L, c->P, c->pp, c->Ls, c->cs_new, c->d_status));
+  }
+  {
+    Phase ph(c, FSPH_TIMER_VSIG);
+    CK(launch_vsig_fp64(L, c->P, c->pp, c->Ls, c->cs_new));
+  }
+  // the new sound speed becomes the particle's sound speed
+  double * t = c->P.f[F_CS];
+  c->P.f[F_CS] = c->cs_new;
+  c->cs_new = t;
+  // keep the alternate set's pointer table consistent for the next permute
+  return FSPH_OK;
+}
+
+static fsph_status accel_impl(fsph_ctx * c, int kick) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_ACCEL);
+  CK(launch_accel_fp64(L, c->P, c->pp, c->Ls, kick, c->d_time));
+  return FSPH_OK;
+}
+
+fsph_status fsph_acceleration(fsph_ctx * c) { return accel_impl(c, 0); }
+
+fsph_status fsph_dudt(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_ENERGY);
+  CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
+  return FSPH_OK;
+}
+
+fsph_status fsph_dedt(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_ENERGY);
+  CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
+  return FSPH_OK;
+}
+
+static fsph_status elem(fsph_ctx * c, int op, int phase) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, phase);
+  CK(launch_elementwise(L, c->P, c->pp, op, c->d_time, c->d_status));
+  return FSPH_OK;
+}
+
+fsph_status fsph_eos_init(fsph_ctx * c) { return elem(c, OP_EOS_INIT, FSPH_TIMER_INTEGRATE); }
+fsph_status fsph_set_total_energy(fsph_ctx * c) {
+  return elem(c, OP_SET_TOTAL_ENERGY, FSPH_TIMER_INTEGRATE);
+}
+fsph_status fsph_save_velocityhalf(fsph_ctx * c) {
+  return elem(c, OP_SAVE_VHALF, FSPH_TIMER_INTEGRATE);
+}
+fsph_status fsph_leapfrog_kick_v(fsph_ctx * c) { return elem(c, OP_KICK_V, FSPH_TIMER_INTEGRATE); }
+fsph_status fsph_leapfrog_kick_u(fsph_ctx * c) { return elem(c, OP_KICK_U, FSPH_TIMER_INTEGRATE); }
+fsph_status fsph_leapfrog_kick_e(fsph_ctx * c) { return elem(c, OP_KICK_E, FSPH_TIMER_INTEGRATE); }
+fsph_status fsph_leapfrog_drift(fsph_ctx * c) { return elem(c, OP_DRIFT, FSPH_TIMER_INTEGRATE); }
+fsph_status fsph_recompute_pressure_soundspeed(fsph_ctx * c) {
+  return elem(c, OP_RECOMPUTE, FSPH_TIMER_INTEGRATE);
+}
+fsph_status fsph_recompute_pressure_soundspeed_thermokinetic(fsph_ctx * c) {
+  return elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE);
+}
+fsph_status fsph_check_nans(fsph_ctx * c) { return elem(c, OP_CHECK_NANS, FSPH_TIMER_DT); }
+fsph_status fsph_check_negativity(fsph_ctx * c) {
+  return elem(c, OP_CHECK_NEGATIVITY, FSPH_TIMER_DT);
+}
+fsph_status fsph_compute_smoothinglength(fsph_ctx * c) {
+  return elem(c, OP_SMOOTHING_LENGTH, FSPH_TIMER_INTEGRATE);
+}
+
+fsph_status fsph_compute_average_smoothinglength(fsph_ctx * c) {
+  fsph_status s = elem(c, OP_SMOOTHING_LENGTH, FSPH_TIMER_INTEGRATE);
+  if(s)
+    return s;
+  Launch L = c->L();
+  CK(launch_hsum(L, c->P, c->d_time));
+  return elem(c, OP_SET_H, FSPH_TIMER_INTEGRATE);
+}
+
+fsph_status fsph_compute_dt(fsph_ctx * c) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_DT);
+  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status));
+  return FSPH_OK;
+}
+
+fsph_status fsph_set_adaptive_timestep(fsph_ctx * c) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  CK(launch_set_adaptive_timestep(L, c->pp, c->d_time));
+  return FSPH_OK;
+}
+
+fsph_status fsph_advance_time(fsph_ctx * c) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  CK(launch_advance_time(L, c->pp, c->d_time));
+  c->iteration++;
+  return FSPH_OK;
+}
+
+fsph_status fsph_gravitation(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  c->last_error = "gravity is not available in this build";
+  return FSPH_ERR_ARG;
+}
+
+#define TRY(x)                                                                 \
+  do {                                                                         \
+    fsph_status s_ = (x);                                                      \
+    if(s_) return s_;                                                          \
+  } while(0)
+
+// One iteration of the driver loop (app/drivers/hydro/main_driver.cc:98-279;
+// newtonian/main_driver.cc:103-298 when enable_fmm).  Elementwise steps that
+// the reference runs back to back are fused; every fusion only combines
+// per-particle updates whose inputs the fused pass does not read from
+// neighbours.
+fsph_status fsph_step(fsph_ctx * c) {
+  if(!c || !c->uploaded)
+    return FSPH_ERR_STATE;
+  const fsph_params & p = c->p;
+  const bool thermo = p.thermokinetic_formulation;
+  const bool evolve = p.evolve_internal_energy;
+  if(p.enable_fmm)
+    return FSPH_ERR_ARG;
+  if(c->iteration == p.initial_iteration) {
+    TRY(fsph_update_iteration(c));
+    TRY(fsph_eos_init(c));
+    if(thermo)
+      TRY(fsph_set_total_energy(c));
+    TRY(fsph_density_pressure_soundspeed(c));
+    TRY(fsph_save_velocityhalf(c));
+    TRY(accel_impl(c, 0));
+    if(p.adaptive_timestep) {
+      TRY(fsph_compute_dt(c));
+      TRY(fsph_set_adaptive_timestep(c));
+    }
+    if(evolve) {
+      for(int m = 1; m <= p.pressure_updates_number; ++m) {
+        if(thermo) {
+          TRY(fsph_dedt(c));
+          TRY(elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE));
+        }
+        else {
+          TRY(fsph_dudt(c));
+          TRY(elem(c, OP_RECOMPUTE, FSPH_TIMER_INTEGRATE));
+        }
+      }
+    }
+  }
+  else {
+    TRY(elem(c, !evolve ? OP_KICK_DRIFT_NONE : (thermo ? OP_KICK_DRIFT_E : OP_KICK_DRIFT_U),
+      FSPH_TIMER_INTEGRATE));
+    TRY(fsph_update_iteration(c));
+    TRY(fsph_density_pressure_soundspeed(c));
+    TRY(accel_impl(c, 1));
+    if(evolve) {
+      for(int m = 1; m <= p.pressure_updates_number; ++m) {
+        const bool lastp = m == p.pressure_updates_number;
+        if(thermo) {
+          TRY(fsph_dedt(c));
+          TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_E : OP_RECOMPUTE_THERMO,
+            FSPH_TIMER_INTEGRATE));
+        }
+        else {
+          TRY(fsph_dudt(c));
+          TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_U : OP_RECOMPUTE,
+            FSPH_TIMER_INTEGRATE));
+        }
+      }
+    }
+  }
+  if(p.sph_variable_h)
+    TRY(fsph_compute_smoothinglength(c));
+  else if(p.sph_update_uniform_h)
+    TRY(fsph_compute_average_smoothinglength(c));
+  TRY(fsph_check_nans(c));
+  TRY(fsph_check_negativity(c));
+  if(p.adaptive_timestep) {
+    TRY(fsph_compute_dt(c));
+    TRY(fsph_set_adaptive_timestep(c));
+  }
+  return fsph_advance_time(c);
+}
+
+fsph_status fsph_get_neighbors(fsph_ctx * c, int64_t * offsets,
+  int64_t * indices, int64_t capacity) {
+  if(!c || !offsets || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = fsph_sync(c);
+  if(s)
+    return s;
+  const int n = c->n;
+  std::vector<int> cnt(n);
+  CK(cudaMemcpy(cnt.data(), c->Ls.cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  offsets[0] = 0;
+  for(int i = 0; i < n; ++i)
+    offsets[i + 1] = offsets[i] + cnt[i];
+  if(!indices)
+    return FSPH_OK;
+  if(offsets[n] > capacity)
+    return FSPH_ERR_ARG;
+  const size_t npad = ((size_t)n + 31) / 32 * 32;
+  std::vector<int> raw(npad * (size_t)c->Ls.maxnb);
+  CK(cudaMemcpy(raw.data(), c->Ls.idx, sizeof(int) * raw.size(),
+    cudaMemcpyDeviceToHost));
+  for(int i = 0; i < n; ++i)
+    for(int j = 0; j < cnt[i]; ++j)
+      indices[offsets[i] + j] = raw[list_slot(i, j, c->Ls.maxnb)];
+  return FSPH_OK;
+}
+
+fsph_status fsph_conserved_sums(fsph_ctx * c, fsph_conserved * out) {
+  if(!c || !out || !c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  CK(launch_conserved(L, c->P, c->pp, c->d_cons));
+  s = fsph_sync(c);
+  if(s)
+    return s;
+  double v[8];
+  CK(cudaMemcpy(v, c->d_cons, sizeof(v), cudaMemcpyDeviceToHost));
+  out->mass = v[0];
+  out->energy = v[1];
+  for(int d = 0; d < 3; ++d) {
+    out->momentum[d] = v[2 + d];
+    out->angular_momentum[d] = v[5 + d];
+  }
+  return FSPH_OK;
+}
+
+fsph_status fsph_timers(fsph_ctx * c, double * ms, int32_t count,
+  int64_t * launches) {
+  if(!c)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  CK(cudaStreamSynchronize(c->stream));
+  for(auto & r : c->pending) {
+    float e = 0;
+    CK(cudaEventElapsedTime(&e, c->events[r.e0], c->events[r.e1]));
+    c->timer_ms[r.phase] += e;
+    c->timer_calls[r.phase] += 1;
+  }
+  c->pending.clear();
+  c->ev_used = 0;
+  for(int k = 0; k < count && k < FSPH_TIMER_COUNT; ++k) {
+    if(ms)
+      ms[k] = c->timer_ms[k];
+    if(launches)
+      launches[k] = c->timer_calls[k];
+  }
+  return FSPH_OK;
+}
+
+fsph_status fsph_timers_reset(fsph_ctx * c) {
+  if(!c)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  CK(cudaStreamSynchronize(c->stream));
+  c->pending.clear();
+  c->ev_used = 0;
+  for(int k = 0; k < FSPH_TIMER_COUNT; ++k) {
+    c->timer_ms[k] = 0;
+    c->timer_calls[k] = 0;
+  }
+  c->timing = true;
+  return FSPH_OK;
+}
+
+int64_t fsph_launch_count(const fsph_ctx * c) { return c ? c->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,364 @@
+// fsph_elementwise.cu -- per-particle (apply_all / get_all) kernels, the
+// timestep reduction and the scalar time bookkeeping, all FP64 and
+// compiled with -fmad=false so they round like the reference.
+#include <cuda_runtime.h>
+
+#include "fsph_sphmath.cuh"
+
+namespace fsph {
+
+#define ELEM_THREADS 256
+
+__device__ __forceinline__ unsigned long long ord_enc_e(double x) {
+  long long b = __double_as_longlong(x);
+  return b < 0 ? ~(unsigned long long)b
+               : ((unsigned long long)b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_dec_e(unsigned long long u) {
+  return (u & 0x8000000000000000ull)
+           ? __longlong_as_double((long long)(u & 0x7fffffffffffffffull))
+           : __longlong_as_double((long long)~u);
+}
+__device__ __forceinline__ double dmin_(double a, double b) { return b < a ? b : a; }
+
+// recover_internal_energy (default_physics.h:126-145)
+template<int D>
+__device__ __forceinline__ double recover_u(const Particles & P, int i,
+  DevStatus * st) {
+  double vv = 0;
+  for(int d = 0; d < D; ++d)
+    vv += P.f[F_VX + d][i] * P.f[F_VX + d][i];
+  double ekin = .5 * vv;
+  double eint = P.f[F_E][i] - ekin - 0.0;
+  if(!(eint > 0))
+    raise_status(st, FSPH_ERR_NEG_ENERGY, i);
+  return eint;
+}
+
+template<int D>
+__global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
+  PhysParams pp, int op, const DevTime * tm, DevStatus * st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= P.n)
+    return;
+  double ** f = P.f;
+  const double dt = tm->dt;
+  switch(op) {
+    case OP_EOS_INIT:  // eos.h:67-92,157-159
+      f[F_K][i] = f[F_P][i] / pow(f[F_RHO][i], pp.gamma);
+      break;
+    case OP_SET_TOTAL_ENERGY: {  // default_physics.h:327-335
+      double vv = 0;
+      for(int d = 0; d < D; ++d)
+        vv += f[F_VX + d][i] * f[F_VX + d][i];
+      double ekin = .5 * vv;
+      f[F_E][i] = ekin + f[F_U][i] + 0.0;
+      break;
+    }
+    case OP_SAVE_VHALF:  // integration.h:52-55
+      for(int d = 0; d < D; ++d)
+        f[F_VHX + d][i] = f[F_VX + d][i];
+      break;
+    case OP_KICK_V: {  // integration.h:65-70
+      const double s = 0.5 * dt;
+      for(int d = 0; d < D; ++d)
+        f[F_VX + d][i] = f[F_VX + d][i] + (f[F_AX + d][i] + f[F_GAX + d][i]) * s;
+      break;
+    }
+    case OP_KICK_U:  // integration.h:80-84
+      f[F_U][i] = f[F_U][i] + 0.5 * dt * f[F_DUDT][i];
+      break;
+    case OP_KICK_E:  // integration.h:94-98
+      f[F_E][i] = f[F_E][i] + 0.5 * dt * f[F_DEDT][i];
+      break;
+    case OP_DRIFT:  // integration.h:106-110
+      for(int d = 0; d < D; ++d)
+        f[F_X + d][i] = f[F_X + d][i] + f[F_VX + d][i] * dt;
+      break;
+    case OP_KICK_DRIFT_E:
+    case OP_KICK_DRIFT_U:
+    case OP_KICK_DRIFT_NONE: {
+      // the start of a leapfrog step, hydro/main_driver.cc:176-188:
+      // kick e (or u), kick v, save v_half, drift
+      if(op == OP_KICK_DRIFT_E)
+        f[F_E][i] = f[F_E][i] + 0.5 * dt * f[F_DEDT][i];
+      else if(op == OP_KICK_DRIFT_U)
+        f[F_U][i] = f[F_U][i] + 0.5 * dt * f[F_DUDT][i];
+      const double s = 0.5 * dt;
+      for(int d = 0; d < D; ++d) {
+        double v = f[F_VX + d][i] + (f[F_AX + d][i] + f[F_GAX + d][i]) * s;
+        f[F_VX + d][i] = v;
+        f[F_VHX + d][i] = v;
+        f[F_X + d][i] = f[F_X + d][i] + v * dt;
+      }
+      break;
+    }
+    case OP_RECOMPUTE:
+    case OP_RECOMPUTE_KICK_U: {  // default_physics.h:153-161 (+ kick_u)
+      double uint = f[F_U][i];
+      double P_, cs;
+      eos_p_cs(pp, f[F_RHO][i], uint + 0.5 * dt * f[F_DUDT][i], f[F_K][i], P_, cs);
+      f[F_P][i] = P_;
+      f[F_CS][i] = cs;
+      if(op == OP_RECOMPUTE_KICK_U)
+        f[F_U][i] = uint + 0.5 * dt * f[F_DUDT][i];
+      break;
+    }
+    case OP_RECOMPUTE_THERMO:
+    case OP_RECOMPUTE_KICK_E: {  // default_physics.h:169-182 (+ kick_e)
+      double eint = recover_u<D>(P, i, st);
+      f[F_U][i] = eint;
+      double vda = 0;
+      for(int d = 0; d < D; ++d)
+        vda += f[F_VX + d][i] * f[F_AX + d][i];
+      double P_, cs;
+      eos_p_cs(pp, f[F_RHO][i], eint + 0.5 * dt * (f[F_DEDT][i] - vda),
+        f[F_K][i], P_, cs);
+      f[F_P][i] = P_;
+      f[F_CS][i] = cs;
+      if(op == OP_RECOMPUTE_KICK_E)
+        f[F_E][i] = f[F_E][i] + 0.5 * dt * f[F_DEDT][i];
+      break;
+    }
+    case OP_SMOOTHING_LENGTH: {  // default_physics.h:825-848
+      double q = f[F_M][i] / f[F_RHO][i];
+      double r = D == 3 ? cbrt(q) : sqrt(q);
+      f[F_H][i] = r * pp.eta * pp.kw;
+      break;
+    }
+    case OP_SET_H:  // second half of compute_average_smoothinglength
+      f[F_H][i] = 1. / (double)P.n * tm->hsum;
+      break;
+    case OP_CHECK_NANS: {  // default_physics.h:918-945
+      bool bad = false;
+      for(int d = 0; d < D; ++d) {
+        double q[5] = {f[F_X + d][i], f[F_VX + d][i], f[F_VHX + d][i],
+          f[F_AX + d][i], f[F_GAX + d][i]};
+        for(int k = 0; k < 5; ++k)
+          bad |= q[k] != q[k];
+      }
+      const int sc[] = {F_M, F_GPOT, F_RHO, F_P, F_E, F_DEDT, F_DUDT, F_K, F_VSIG};
+      for(int k = 0; k < 9; ++k)
+        bad |= f[sc[k]][i] != f[sc[k]][i];
+      if(pp.evolve_u)
+        bad |= f[F_U][i] != f[F_U][i];
+      if(bad)
+        raise_status(st, FSPH_ERR_NAN, i);
+      break;
+    }
+    case OP_CHECK_NEGATIVITY:  // default_physics.h:953-979
+      if(f[F_RHO][i] < 0 || f[F_P][i] < 0 || (pp.evolve_u && f[F_U][i] < 0))
+        raise_status(st, FSPH_ERR_NEGATIVITY, i);
+      break;
+  }
+}
+
+cudaError_t launch_elementwise(const Launch & L, const Particles & P,
+  const PhysParams & pp, int op, DevTime * t, DevStatus * st) {
+  const int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
+  if(pp.dim == 3)
+    k_elem<3><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, op, t, st);
+  else
+    k_elem<2><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, op, t, st);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+// compute_dt (default_physics.h:602-695) per particle, then the minimum.
+__global__ void k_dt_init(DevTime * t) { t->dtmin_bits = ord_enc_e(1e24); }
+
+template<int D>
+__global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
+  PhysParams pp, DevTime * tm, DevStatus * st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtmin = 1e24;
+  if(i < P.n) {
+    double ** f = P.f;
+    const double tiny = 1e-24, mc = 0.6;
+    const double dx = f[F_H][i] / (pp.eta * pp.kw);
+    double vn = 0;
+    for(int d = 0; d < D; ++d)
+      vn += f[F_VX + d][i] * f[F_VX + d][i];
+    vn = sqrt(vn);
+    const double dt_v = dx / (vn + tiny);
+    double acc = 0;
+    for(int d = 0; d < D; ++d) {
+      double ad = f[F_AX + d][i] + f[F_GAX + d][i];
+      acc += ad * ad;
+    }
+    acc = sqrt(acc);
+    const double dt_a = sqrt(dx / (acc + tiny));
+    const double dt_c = dx / (tiny + f[F_VSIG][i] * (1 + mc * pp.alpha));
+    dtmin = pp.cfl * dmin_(dmin_(dt_v, dt_a), dt_c);
+    if(pp.evolve_u && pp.thermokinetic) {
+      const double eint = f[F_U][i];
+      if(!(eint > 0))
+        raise_status(st, FSPH_ERR_NEG_ENERGY, i);
+      double gdv = 0;
+      for(int d = 0; d < D; ++d)
+        gdv += f[F_VX + d][i] * f[F_GAX + d][i];
+      int it;
+      for(it = 0; it < 20; ++it) {
+        double delta_epot = 0.0 - 0.0;
+        double delta_egrv = -dtmin * gdv;
+        if(delta_epot + delta_egrv < eint * 0.5)
+          break;
+        dtmin *= 0.25;
+      }
+      if(it >= 20)
+        raise_status(st, FSPH_ERR_DT, i);
+    }
+    f[F_DT][i] = dtmin;
+  }
+  for(int o = 16; o; o >>= 1)
+    dtmin = dmin_(dtmin, __shfl_xor_sync(0xffffffffu, dtmin, o));
+  if((threadIdx.x & 31) == 0)
+    atomicMin(&tm->dtmin_bits, ord_enc_e(dtmin));
+}
+
+cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
+  const PhysParams & pp, DevTime * t, DevStatus * st) {
+  k_dt_init<<<1, 1, 0, L.stream>>>(t);
+  const int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
+  if(pp.dim == 3)
+    k_compute_dt<3><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+  else
+    k_compute_dt<2><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+  *L.counter += 2;
+  return cudaGetLastError();
+}
+
+// set_adaptive_timestep (default_physics.h:761-823), one thread.
+__global__ void k_set_adaptive(PhysParams pp, DevTime * t) {
+  double dtmin = ord_dec_e(t->dtmin_bits);
+  double dt = t->dt;
+  if(dtmin < dt)
+    dt = dmin_(dtmin, dt / 2.0);
+  if(dtmin > 2.0 * dt)
+    dt = dt * 2.0;
+  double tt = t->totaltime;
+  double next = tt + dt;
+  if(pp.out_screen_dt > 0) {
+    if(tt == t->t_screen) {
+      if(t->dt_saved > 0) dt = t->dt_saved;
+      t->t_screen += pp.out_screen_dt;
+    }
+    if(tt + dt > t->t_screen - 0.1 * pp.out_screen_dt) {
+      t->dt_saved = dt;
+      next = t->t_screen;
+    }
+  }
+  if(pp.out_scalar_dt > 0) {
+    if(tt == t->t_scalar) {
+      if(t->dt_saved > 0) dt = t->dt_saved;
+      t->t_scalar += pp.out_scalar_dt;
+    }
+    if(tt + dt > t->t_scalar - 0.1 * pp.out_scalar_dt) {
+      t->dt_saved = dt;
+      next = dmin_(next, t->t_scalar);
+    }
+  }
+  if(pp.out_h5data_dt > 0) {
+    if(tt == t->t_h5) {
+      if(t->dt_saved > 0) dt = t->dt_saved;
+      t->t_h5 += pp.out_h5data_dt;
+    }
+    if(tt + dt > t->t_h5 - 0.1 * pp.out_h5data_dt) {
+      t->dt_saved = dt;
+      next = dmin_(next, t->t_h5);
+    }
+  }
+  t->totaltime_next = next;
+  t->dt = next - tt;
+}
+
+cudaError_t launch_set_adaptive_timestep(const Launch & L,
+  const PhysParams & pp, DevTime * t) {
+  k_set_adaptive<<<1, 1, 0, L.stream>>>(pp, t);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+// advance_time (default_physics.h:853-860)
+__global__ void k_advance(PhysParams pp, DevTime * t) {
+  t->iteration++;
+  if(pp.adaptive)
+    t->totaltime = t->totaltime_next;
+  else
+    t->totaltime = t->totaltime + t->dt;
+}
+
+cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,
+  DevTime * t) {
+  k_advance<<<1, 1, 0, L.stream>>>(pp, t);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+// Deterministic sum of h (fixed two-level order) for the averaged h.
+__global__ void __launch_bounds__(1024) k_hsum(Particles P, DevTime * t) {
+  __shared__ double part[1024];
+  double s = 0;
+  for(int i = threadIdx.x; i < P.n; i += 1024)
+    s += P.f[F_H][i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 512; o; o >>= 1) {
+    if(threadIdx.x < o)
+      part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0)
+    t->hsum = part[0];
+}
+
+cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t) {
+  k_hsum<<<1, 1024, 0, L.stream>>>(P, t);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+// Conserved totals (analysis.h:56-214): mass, energy, momentum (3),
+// angular momentum (3); one block, fixed order (deterministic).
+__global__ void __launch_bounds__(512) k_conserved(Particles P, PhysParams pp,
+  double * out) {
+  __shared__ double part[8][512];
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int D = pp.dim;
+  for(int i = threadIdx.x; i < P.n; i += 512) {
+    double m = P.f[F_M][i];
+    double x[3] = {P.f[F_X][i], P.f[F_Y][i], D == 3 ? P.f[F_Z][i] : 0.0};
+    double v[3] = {P.f[F_VX][i], P.f[F_VY][i], D == 3 ? P.f[F_VZ][i] : 0.0};
+    s[0] += m;
+    if(pp.thermokinetic)
+      s[1] += m * P.f[F_E][i];
+    else
+      s[1] += m * (P.f[F_U][i] + .5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+    s[1] += .5 * m * P.f[F_GPOT][i];
+    for(int d = 0; d < 3; ++d)
+      s[2 + d] += m * v[d];
+    s[5] += m * (x[1] * v[2] - x[2] * v[1]);
+    s[6] += m * (x[2] * v[0] - x[0] * v[2]);
+    s[7] += m * (x[0] * v[1] - x[1] * v[0]);
+  }
+  for(int k = 0; k < 8; ++k)
+    part[k][threadIdx.x] = s[k];
+  __syncthreads();
+  for(int o = 256; o; o >>= 1) {
+    if(threadIdx.x < o)
+      for(int k = 0; k < 8; ++k)
+        part[k][threadIdx.x] += part[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x < 8)
+    out[threadIdx.x] = part[threadIdx.x][0];
+}
+
+cudaError_t launch_conserved(const Launch & L, const Particles & P,
+  const PhysParams & pp, double * out8) {
+  k_conserved<<<1, 512, 0, L.stream>>>(P, pp, out8);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace fsph

@@ -1,0 +1,146 @@
+// fsph_internal.cuh -- device-side types shared by the translation units of
+// libfsph_gb300.so.  Not part of the public ABI (that is include/fsph.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fsph.h"
+
+namespace fsph {
+
+// Particle fields held on the device, one FP64 array each (SoA).  Order is
+// free; the names follow body_u (include/physics/body.h:221-251).
+enum Field {
+  F_X, F_Y, F_Z, F_VX, F_VY, F_VZ, F_VHX, F_VHY, F_VHZ, F_AX, F_AY, F_AZ,
+  F_GAX, F_GAY, F_GAZ, F_GPOT, F_M, F_H, F_RHO, F_P, F_CS, F_U, F_E, F_DUDT,
+  F_DEDT, F_K, F_ALPHA, F_VSIG, F_DT, NF
+};
+
+// physics:: time globals of the reference (default_physics.h:32-39), kept in
+// device memory so a whole step runs without a host round trip.
+struct DevTime {
+  double dt, dt_saved, totaltime, totaltime_next;
+  double t_screen, t_scalar, t_h5;
+  long long iteration;
+  // global reductions written by kernels
+  unsigned long long dtmin_bits;  // ordered encoding of min particle dt
+  double hsum;                    // sum of h (average smoothing length)
+};
+
+// First device-side error: code (fsph_status) and the particle it concerns.
+struct DevStatus {
+  int code;
+  int flags;  // informational bits (FLAG_*)
+  long long index;
+};
+enum { FLAG_LIST_ORDER_CHUNKED = 1 };
+
+struct Particles {
+  double * f[NF];
+  long long * id;
+  unsigned long long * key;
+  int n;
+};
+
+struct PhysParams {
+  int dim, kernel, eos, thermokinetic, evolve_u, adaptive;
+  double gamma, eta, kw, alpha, beta, eps, cfl;
+  double out_screen_dt, out_scalar_dt, out_h5data_dt;
+  double G;
+};
+
+// Binary radix tree over the sorted keys (n-1 internal nodes, node 0 is the
+// root).  Child encoding: >= 0 internal node, < 0 leaf ~index.
+struct NodeBox {   // 64 bytes: two aligned double4 loads
+  double lo[3];
+  double hmax;
+  double hi[3];
+  double pad;
+};
+
+struct Tree {
+  int * left;
+  int * right;
+  int * parent;       // internal node -> parent (-1 for the root)
+  int * leaf_parent;  // particle -> parent internal node
+  int * first;
+  int * last;
+  NodeBox * box;
+  NodeBox * box2;          // reference node box: union of [x - h/2, x + h/2]
+  int * opar;              // particle -> binary node standing for its octree parent
+  int * gref;              // particle -> its reference traversal group
+  unsigned * counter;
+  unsigned char * edepth;  // reference octree depth of each particle
+  int * group_first;
+  int * group_last;
+  int * ngroups;           // device scalar
+};
+
+struct Lists {
+  int * idx;   // interleaved: [(i>>5)][slot][i&31]
+  int * cnt;
+  int maxnb;
+};
+
+__host__ __device__ inline size_t list_slot(int i, int j, int maxnb) {
+  return ((size_t)(i >> 5) * (size_t)maxnb + (size_t)j) * 32u + (size_t)(i & 31);
+}
+
+// Kernel launch helpers (host).  Each translation unit exports plain host
+// functions; the API layer strings them together on the context stream.
+struct Launch {
+  cudaStream_t stream;
+  long long * counter;  // launches issued
+};
+
+// ---- fsph_tree.cu ----
+cudaError_t launch_range_keys(const Launch & L, const Particles & P,
+  const PhysParams & pp, double * d_range, unsigned long long * keys_out,
+  int * idx_out);
+cudaError_t radix_sort_pairs(const Launch & L, unsigned long long * keys,
+  int * vals, unsigned long long * keys_tmp, int * vals_tmp, int n,
+  unsigned * hist, int nblocks_cap);
+size_t radix_hist_entries(int n);
+cudaError_t launch_check_duplicates(const Launch & L,
+  const unsigned long long * keys, int n, DevStatus * st);
+cudaError_t launch_permute(const Launch & L, const Particles & src,
+  const Particles & dst, const int * perm, const unsigned long long * keys);
+cudaError_t launch_build_tree(const Launch & L, const Particles & P,
+  const PhysParams & pp, Tree & T, int group_max);
+cudaError_t launch_neighbors(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Tree & T, Lists & Ls, DevStatus * st, int nsm,
+  const unsigned long long * rbits);
+
+// ---- fsph_fp64.cu ----
+cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st);
+cudaError_t launch_vsig_fp64(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const double * cs_new);
+cudaError_t launch_accel_fp64(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, int kick, const DevTime * t);
+cudaError_t launch_dudt_fp64(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const DevTime * t);
+cudaError_t launch_dedt_fp64(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls);
+
+// ---- fsph_elementwise.cu ----
+enum ElemOp {
+  OP_EOS_INIT, OP_SET_TOTAL_ENERGY, OP_SAVE_VHALF, OP_KICK_V, OP_KICK_U,
+  OP_KICK_E, OP_DRIFT, OP_RECOMPUTE, OP_RECOMPUTE_THERMO, OP_SMOOTHING_LENGTH,
+  OP_CHECK_NANS, OP_CHECK_NEGATIVITY, OP_KICK_DRIFT_E, OP_KICK_DRIFT_U,
+  OP_KICK_DRIFT_NONE, OP_SET_H, OP_RECOMPUTE_KICK_E, OP_RECOMPUTE_KICK_U
+};
+cudaError_t launch_elementwise(const Launch & L, const Particles & P,
+  const PhysParams & pp, int op, DevTime * t, DevStatus * st);
+cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
+  const PhysParams & pp, DevTime * t, DevStatus * st);
+cudaError_t launch_set_adaptive_timestep(const Launch & L,
+  const PhysParams & pp, DevTime * t);
+cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,
+  DevTime * t);
+cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t);
+cudaError_t launch_conserved(const Launch & L, const Particles & P,
+  const PhysParams & pp, double * out8);
+
+}  // namespace fsph

@@ -1,0 +1,170 @@
+// fsph_sphmath.cuh -- FP64 device restatement of the reference's SPH
+// kernels, viscosity and EOS.  Every expression keeps the reference's
+// operand order; the including translation units are compiled with
+// -fmad=false, so each operation rounds exactly as the reference's does.
+#pragma once
+
+#include "fsph_internal.cuh"
+
+namespace fsph {
+
+// kernels::TINY (include/physics/kernels.h:64) and viscosity::TINY
+// (include/physics/viscosity.h:36): 1e10 * DBL_MIN.
+#define FSPH_TINY (1e10 * 2.2250738585072014e-308)
+#define FSPH_PI 3.14159265358979323846
+
+// Normalisations sigma[D-1] (kernels.h:40-46)
+__device__ __forceinline__ double cubic_sigma(int D) {
+  return D == 1 ? 4. / 3. : (D == 2 ? 40. / (7. * FSPH_PI) : 8. / FSPH_PI);
+}
+__device__ __forceinline__ double wc2_sigma(int D) {
+  return D == 1 ? 1.25 : (D == 2 ? 7. / FSPH_PI : 21. / (2. * FSPH_PI));
+}
+__device__ __forceinline__ double wc4_sigma(int D) {
+  return D == 1 ? 1.5 : (D == 2 ? 9. / FSPH_PI : 495. / (32. * FSPH_PI));
+}
+__device__ __forceinline__ double wc6_sigma(int D) {
+  return D == 1 ? 55. / 32.
+                : (D == 2 ? 78. / (7. * FSPH_PI) : 1365. / (64. * FSPH_PI));
+}
+
+// kernel<K,D>(r, h) -- kernels.h:106-121, 282-312, 375-410, 477-512
+template<int D, int K>
+__device__ __forceinline__ double kfun(double r, double h) {
+  if(K == FSPH_KERNEL_CUBIC_SPLINE) {
+    double rh = 2. * r / h;
+    double result = 0.;
+    if(rh < 2.0) {
+      if(rh < 1.0)
+        result = 1.0 - 1.5 * rh * rh + .75 * rh * rh * rh;
+      else
+        result = 0.25 * (2 - rh) * (2 - rh) * (2 - rh);
+      result *= cubic_sigma(D) / pow(h, (double)D);
+    }
+    return result;
+  }
+  else if(K == FSPH_KERNEL_WENDLAND_C2) {
+    double rh = r / h;
+    double hd = D == 3 ? h * h * h : h * h;
+    double rh2 = (1 - rh) * (1 - rh);
+    double sigma = wc2_sigma(D) / hd;
+    double result = sigma * rh2 * rh2 * (4 * rh + 1);
+    return result * (rh < 1.0);
+  }
+  else if(K == FSPH_KERNEL_WENDLAND_C4) {
+    double rh = r / h;
+    double hd = D == 3 ? h * h * h : h * h;
+    double rh1 = 1 - rh;
+    double rh2 = rh1 * rh1;
+    double rh6 = rh2 * rh2 * rh2;
+    double sigma = wc4_sigma(D) / hd;
+    double result = sigma * rh6 * (1 + rh * (6 + rh * 35 / 3));
+    return result * (rh < 1.0);
+  }
+  else {
+    double rh = r / h;
+    double hd = D == 3 ? h * h * h : h * h;
+    double rh2 = (1 - rh) * (1 - rh);
+    double rh4 = rh2 * rh2;
+    double sigma = wc6_sigma(D) / hd;
+    double result = sigma * rh4 * rh4 * (1 + rh * (8 + rh * (25 + rh * 32)));
+    return result * (rh < 1.0);
+  }
+}
+
+// kernel_gradient<K,D>(vecP, h) -- kernels.h:132-153, 322-361, 435-463, 536-566
+template<int D, int K>
+__device__ __forceinline__ void kgrad(const double * p, double h, double * out) {
+  double r = 0;
+  for(int d = 0; d < D; ++d)
+    r += p[d] * p[d];
+  r = sqrt(r);
+  if(K == FSPH_KERNEL_CUBIC_SPLINE) {
+    double rh = 2. * r / h;
+    for(int d = 0; d < D; ++d)
+      out[d] = 0.0;
+    if(rh < 2.0) {
+      double dWdr;
+      double sigma = 2. * cubic_sigma(D) / pow(h, (double)(D + 1));
+      if(rh < 1.0)
+        dWdr = -3.0 * rh + 9. / 4. * rh * rh;
+      else
+        dWdr = -.75 * (2 - rh) * (2 - rh);
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * sigma * dWdr / (r + FSPH_TINY);
+    }
+    return;
+  }
+  double f;
+  if(K == FSPH_KERNEL_WENDLAND_C2) {
+    double rh = r / h;
+    double hd1 = D == 3 ? h * h * h * h : h * h * h;
+    double rh2 = (1 - rh) * (1 - rh);
+    double sigma = 2. * wc2_sigma(D) / hd1;
+    double dWdr = -10. * rh * rh2 * (1 - rh);
+    f = (rh < 1.0) * (sigma * dWdr / (r + FSPH_TINY));
+  }
+  else if(K == FSPH_KERNEL_WENDLAND_C4) {
+    double rh = r / h;
+    double hd1 = D == 3 ? h * h * h * h : h * h * h;
+    double rh2 = (1 - rh) * (1 - rh);
+    double rh3 = rh2 * (1 - rh);
+    double sigma = 14. * wc4_sigma(D) / hd1;
+    double dWdr = -4. / 3. * rh * rh3 * rh2 * (1 + 5. * rh);
+    f = (rh < 1.0) * (sigma * dWdr / (r + FSPH_TINY));
+  }
+  else {
+    double rh = r / h;
+    double hd1 = D == 3 ? h * h * h * h : h * h * h;
+    double rh2 = (1 - rh) * (1 - rh);
+    double rh3 = rh2 * (1 - rh);
+    double rh4 = rh2 * rh2;
+    double sigma = wc6_sigma(D) / hd1;
+    double dWdr = -22. * rh * rh4 * rh3 * (1 + rh * (7 + rh * 16));
+    f = (rh < 1.0) * (sigma * dWdr / (r + FSPH_TINY));
+  }
+  for(int d = 0; d < D; ++d)
+    out[d] = p[d] * f;
+}
+
+// viscosity::mu (viscosity.h:81-93)
+template<int D>
+__device__ __forceinline__ double visc_mu(double eps, double h_ab,
+  const double * vel_ab, const double * pos_ab) {
+  double dotp = 0, dist2 = 0;
+  for(int d = 0; d < D; ++d)
+    dotp += vel_ab[d] * pos_ab[d];
+  for(int d = 0; d < D; ++d)
+    dist2 += pos_ab[d] * pos_ab[d];
+  double result = h_ab * dotp / (dist2 + eps * h_ab * h_ab + FSPH_TINY);
+  return result * (dotp < 0.0);
+}
+
+// viscosity_function<visc_constant> (viscosity.h:128-137)
+__device__ __forceinline__ double visc_pi(double alpha, double beta,
+  double rho_ab, double c_ab, double mu_ab) {
+  return (-alpha * c_ab + beta * mu_ab) * mu_ab / rho_ab;
+}
+
+// eos_t<ideal>/<polytropic> compute_pressure + compute_soundspeed
+// (eos/eos.h:102-119, 166-183)
+__device__ __forceinline__ void eos_p_cs(const PhysParams & pp, double rho,
+  double u, double K, double & P, double & cs) {
+  const double g = pp.gamma;
+  if(pp.eos == FSPH_EOS_POLYTROPIC) {
+    P = K * pow(rho, g);
+    cs = sqrt(K * g * pow(rho, g - 1.));
+  }
+  else {
+    P = (g - 1.) * rho * u;
+    cs = sqrt(g * (g - 1.) * u);
+  }
+}
+
+__device__ __forceinline__ void raise_status(DevStatus * st, int code,
+  long long index) {
+  if(atomicCAS(&st->code, 0, code) == 0)
+    st->index = index;
+}
+
+}  // namespace fsph

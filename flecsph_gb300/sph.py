@@ -1,0 +1,197 @@
+"""Python host mirror of FleCSPH's body_system over libfsph_gb300.so.
+
+``BodySystem`` exposes the calls the reference drivers make on
+``body_system<double, D>`` (mpisph/bodies_system.h) and the physics modules
+they pass to it, each forwarding to one C-ABI entry point of
+include/fsph.h.  The reference's template-callback style
+(``bs.apply_in_smoothinglength(physics::compute_acceleration)``) becomes an
+explicit method per physics module, because the GPU library fuses the
+traversal with the physics.
+
+There is no CPU fallback: if the shared library or a CUDA device is missing
+every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (Conserved, FsphError, Params, SoAView, TIMER_COUNT, TIMER_NAMES,
+                  make_view, new_state)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfsph_gb300.so")
+
+_lib = None
+
+_STEP_FUNCS = [
+    "update_iteration", "reset_ghosts", "density_pressure_soundspeed",
+    "acceleration", "dudt", "dedt", "eos_init", "set_total_energy",
+    "save_velocityhalf", "leapfrog_kick_v", "leapfrog_kick_u", "leapfrog_kick_e",
+    "leapfrog_drift", "recompute_pressure_soundspeed",
+    "recompute_pressure_soundspeed_thermokinetic", "compute_dt", "check_nans",
+    "check_negativity", "set_adaptive_timestep", "compute_smoothinglength",
+    "compute_average_smoothinglength", "gravitation", "advance_time", "step", "sync",
+    "timers_reset",
+]
+
+
+def library():
+    """Load libfsph_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run flecsph_gb300.build.build() first")
+    lib = C.CDLL(LIB_PATH)
+    lib.fsph_create.restype = C.c_void_p
+    lib.fsph_create.argtypes = [C.POINTER(Params), C.c_int32, C.c_int64,
+                                C.POINTER(C.c_int)]
+    lib.fsph_destroy.argtypes = [C.c_void_p]
+    lib.fsph_destroy.restype = None
+    lib.fsph_params_default.argtypes = [C.POINTER(Params)]
+    lib.fsph_params_default.restype = None
+    lib.fsph_abi_version.restype = C.c_int32
+    lib.fsph_status_string.restype = C.c_char_p
+    lib.fsph_status_string.argtypes = [C.c_int32]
+    lib.fsph_last_error.restype = C.c_char_p
+    lib.fsph_last_error.argtypes = [C.c_void_p]
+    for f in _STEP_FUNCS:
+        fn = getattr(lib, "fsph_" + f)
+        fn.argtypes = [C.c_void_p]
+        fn.restype = C.c_int
+    lib.fsph_upload.argtypes = [C.c_void_p, C.POINTER(SoAView)]
+    lib.fsph_download.argtypes = [C.c_void_p, C.POINTER(SoAView)]
+    lib.fsph_get_time.argtypes = [C.c_void_p, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.fsph_set_time.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64]
+    lib.fsph_get_range.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fsph_get_neighbors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+    lib.fsph_conserved_sums.argtypes = [C.c_void_p, C.POINTER(Conserved)]
+    lib.fsph_timers.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.fsph_launch_count.argtypes = [C.c_void_p]
+    lib.fsph_launch_count.restype = C.c_int64
+    _lib = lib
+    return lib
+
+
+class BodySystem:
+    """One particle system on one GPU (mirror of body_system<double, D>)."""
+
+    def __init__(self, params, capacity, device=0):
+        lib = library()
+        self.params = params
+        st = C.c_int(0)
+        self.ctx = lib.fsph_create(C.byref(params), device, int(capacity), C.byref(st))
+        if not self.ctx:
+            raise FsphError(st.value, "fsph_create")
+        self.lib = lib
+        self.n = 0
+        self.capacity = capacity
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.fsph_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, where):
+        if st:
+            detail = self.lib.fsph_last_error(self.ctx).decode()
+            raise FsphError(st, where, detail)
+
+    def __getattr__(self, name):
+        if name in _STEP_FUNCS:
+            fn = getattr(self.lib, "fsph_" + name)
+
+            def call():
+                self._check(fn(self.ctx), name)
+            call.__name__ = name
+            return call
+        raise AttributeError(name)
+
+    # -- data movement ---------------------------------------------------
+    def read_bodies(self, state):
+        """Upload a particle state (dict of numpy arrays, FP64 SoA)."""
+        keep = {k: np.ascontiguousarray(v) for k, v in state.items()}
+        self._keep = keep
+        self.n = len(keep["x"])
+        v = make_view(keep)
+        self._check(self.lib.fsph_upload(self.ctx, C.byref(v)), "upload")
+
+    upload = read_bodies
+
+    def download(self, fields=None):
+        out = new_state(self.n)
+        v = make_view(out, fields=fields)
+        self._check(self.lib.fsph_download(self.ctx, C.byref(v)), "download")
+        if fields is not None:
+            out = {k: out[k] for k in fields}
+        return out
+
+    def time(self):
+        dt, t, it = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.lib.fsph_get_time(self.ctx, C.byref(dt), C.byref(t), C.byref(it)),
+                    "get_time")
+        return dt.value, t.value, it.value
+
+    def set_time(self, dt, t, it):
+        self._check(self.lib.fsph_set_time(self.ctx, dt, t, it), "set_time")
+
+    def range(self):
+        r = np.zeros(2 * self.params.dimension)
+        self._check(self.lib.fsph_get_range(self.ctx, r.ctypes.data), "get_range")
+        return r
+
+    def neighbors(self):
+        off = np.zeros(self.n + 1, np.int64)
+        self._check(self.lib.fsph_get_neighbors(self.ctx, off.ctypes.data, None, 0),
+                    "get_neighbors")
+        idx = np.zeros(int(off[-1]), np.int64)
+        self._check(self.lib.fsph_get_neighbors(self.ctx, off.ctypes.data,
+                                                idx.ctypes.data, len(idx)),
+                    "get_neighbors")
+        return off, idx
+
+    def conserved(self):
+        c = Conserved()
+        self._check(self.lib.fsph_conserved_sums(self.ctx, C.byref(c)), "conserved")
+        return dict(mass=c.mass, energy=c.energy, momentum=list(c.momentum),
+                    angular_momentum=list(c.angular_momentum))
+
+    def timers(self):
+        ms = np.zeros(TIMER_COUNT)
+        calls = np.zeros(TIMER_COUNT, np.int64)
+        self._check(self.lib.fsph_timers(self.ctx, ms.ctypes.data, TIMER_COUNT,
+                                         calls.ctypes.data), "timers")
+        return {TIMER_NAMES[k]: (ms[k], int(calls[k])) for k in range(len(TIMER_NAMES))}
+
+    def launch_count(self):
+        return int(self.lib.fsph_launch_count(self.ctx))
+
+    # -- reference-style aliases ------------------------------------------
+    def apply_in_smoothinglength(self, name):
+        """apply_in_smoothinglength(f) for f in the physics modules the
+        library implements ('compute_density_pressure_soundspeed',
+        'compute_acceleration', 'compute_dudt', 'compute_dedt')."""
+        table = {
+            "compute_density_pressure_soundspeed": self.density_pressure_soundspeed,
+            "compute_acceleration": self.acceleration,
+            "compute_dudt": self.dudt,
+            "compute_dedt": self.dedt,
+        }
+        table[name]()
+
+    def gravitation_fmm(self):
+        self.gravitation()
