@@ -1,0 +1,357 @@
+"""Benchmark: particle-steps/s of the SPH step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+                    [--n1d 128] [--precision mixed|fp64]
+
+Workload: the 3D Sedov blast, 128^3 = 2,097,152 particles on a 1%-jittered
+lattice (seeded), Wendland C6, ideal gas gamma 5/3, thermokinetic energy,
+adaptive dt -- one "step" is one full leapfrog iteration of the hydro
+driver loop (kick/drift, keys, sort, tree, neighbour lists, density/EOS,
+signal speed, acceleration, de/dt with the pressure predictor, dt
+reduction).  Inputs are resident in HBM when the timed region starts; the
+particle state (~0.5 GB) and neighbour lists (~0.8 GB) exceed the 129 MB L2,
+so no explicit flush is needed between steps.
+
+`value` is measured with CUDA events on the library's stream around K
+steps; `e2e` repeats the measurement through the C ABI with host buffers,
+copying each step's inputs from pinned host memory and its results back.
+`--impl reference` times the reference algorithm on the host cores instead
+(the CPU oracle: the reference compiled from its sources where those exist
+on this machine, otherwise the plain-C restatement), on a 64^3 sample of
+the same problem.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--n1d", type=int, default=128)
+    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines()]
+        except OSError:
+            return out
+        rows = [[x.strip() for x in r] for r in rows if len(r) >= 8]
+        if not rows:
+            return out
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[4 + k].lower() == "active":
+                    reasons.add(nm)
+        out.update(sm_mhz=statistics.median(sm) if sm else None,
+                   sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        os.unlink(self.f.name)
+        return out
+
+
+def run_cpu_oracle(n1d, steps, threads, min_seconds=10.0, max_steps=None):
+    """Time the reference algorithm on the host cores on a Sedov sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from flecsph_gb300 import setups
+    kind = "reference" if pyoracle.have_ref(3) else "port"
+    if kind == "port":
+        pyoracle.build_port()
+    s, p, meta = setups.sedov3d(n1d)
+    o = pyoracle.Oracle(kind, p, threads=threads)
+    o.upload(s)
+    o.step()  # initial iteration (not timed)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        o.step()
+        done += 1
+        el = time.perf_counter() - t0
+        if max_steps is not None and done >= max_steps:
+            break
+        if max_steps is None and el >= min_seconds:
+            break
+    el = time.perf_counter() - t0
+    return dict(value=meta["n"] * done / el, unit="particle-steps/s",
+                cores=threads if kind == "port" else 1, kind=kind,
+                sample=f"Sedov 3D {n1d}^3 = {meta['n']} particles, {done} leapfrog "
+                       f"iterations after the initial one, {el:.1f} s",
+                seconds=el, steps=done)
+
+
+def reference_arm(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n1d = 64
+    steps, warm = args.steps, args.warmup
+    r0 = run_cpu_oracle(n1d, max(1, warm), threads, max_steps=max(1, warm))
+    r = run_cpu_oracle(n1d, steps, threads, max_steps=steps)
+    line = {
+        "metric": "particle-steps/s", "value": r["value"], "unit": "particle-steps/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"sedov3d_{n1d}^3 sample of sedov3d_128^3",
+                   "n_particles": (n1d ** 3), "kernel": "wendland_c6",
+                   "threads": r["cores"]},
+        "cpu_baseline": {"value": r["value"], "unit": "particle-steps/s",
+                         "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
+        "e2e": {"value": r["value"], "unit": "particle-steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del r0
+    print(json.dumps(line), flush=True)
+
+
+# fields a host driver hands over per step (what the leapfrog step reads) and
+# takes back (what it writes)
+IN_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "gax", "gay", "gaz",
+             "m", "h", "cs", "u", "e", "dedt", "K"]
+OUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "vhx", "vhy", "vhz", "ax", "ay", "az",
+              "gax", "gay", "gaz", "gpot", "rho", "P", "cs", "u", "e", "dedt", "vsig",
+              "dt", "h"]
+
+
+def gpu_arm(args):
+    rank, world, local = dist_info()
+    dist = init_dist(world)
+    from flecsph_gb300 import build, setups
+    from flecsph_gb300.abi import PRECISION_FP64, PRECISION_MIXED, make_view
+    if rank == 0:
+        build.build()
+    barrier(dist)
+    from flecsph_gb300 import sph
+
+    s, p, meta = setups.sedov3d(args.n1d)
+    n = meta["n"]
+    mixed_ok = sph.mixed_available() if hasattr(sph, "mixed_available") else False
+    prec = args.precision
+    if prec == "auto":
+        prec = "mixed" if mixed_ok else "fp64"
+    results = {}
+    modes = ["fp64"] + (["mixed"] if mixed_ok else [])
+    if prec == "fp64":
+        modes = ["fp64"]
+    for mode in modes:
+        p.precision_mode = PRECISION_MIXED if mode == "mixed" else PRECISION_FP64
+        bs = sph.BodySystem(p, n, device=local)
+        bs.read_bodies(s)
+        bs.step()  # initial iteration
+        for _ in range(args.warmup):
+            bs.step()
+        bs.sync()
+        off = np.zeros(n + 1, np.int64)
+        bs.lib.fsph_get_neighbors(bs.ctx, off.ctypes.data, None, 0)
+        nb_mean = float(off[-1]) / n
+        bs.timers_reset()
+        launches0 = bs.launch_count()
+        barrier(dist)
+        with Clocks(local) as clk:
+            bs.mark(0)
+            for _ in range(args.steps):
+                bs.step()
+            bs.mark(1)
+            ms = bs.elapsed_ms(0, 1)
+        bs.sync()
+        launches = bs.launch_count() - launches0
+        ms = max_over_ranks(dist, ms)
+        timers = bs.timers()
+        state = bs.download(fields=["ax", "ay", "az", "id"])
+        results[mode] = dict(ms=ms, timers=timers, launches=launches, nb_mean=nb_mean,
+                             clocks=clk.summary(), accel=state)
+        # end to end through the C ABI with pinned host buffers
+        if not args.no_e2e:
+            host = bs.download()
+            for f in set(IN_FIELDS + OUT_FIELDS):
+                if f in host:
+                    host[f] = np.ascontiguousarray(host[f])
+            regs = []
+            for f in set(IN_FIELDS + OUT_FIELDS):
+                sph.host_register(host[f])
+                regs.append(host[f])
+            for f in ("id", "key"):
+                sph.host_register(host[f])
+                regs.append(host[f])
+            vin = make_view(host, fields=set(IN_FIELDS) | {"id"})
+            vout = make_view(host, fields=set(OUT_FIELDS) | {"id", "key"})
+            h2d = 8 * n * (len(IN_FIELDS) + 1)
+            d2h = 8 * n * (len(OUT_FIELDS) + 2)
+            barrier(dist)
+            t0 = time.perf_counter()
+            bs.mark(2)
+            for _ in range(args.steps):
+                bs.upload_fields(vin)
+                bs.step()
+                bs.download_into(vout)
+            bs.mark(3)
+            e2e_ms = bs.elapsed_ms(2, 3)
+            wall = time.perf_counter() - t0
+            e2e_ms = max_over_ranks(dist, e2e_ms)
+            for a in regs:
+                sph.host_unregister(a)
+            results[mode]["e2e"] = dict(ms=e2e_ms, wall_s=wall, h2d=h2d, d2h=d2h)
+        bs.close()
+
+    if rank != 0:
+        return
+    head = results["mixed" if "mixed" in results else "fp64"]
+    K = args.steps
+    value = world * n * K / (head["ms"] * 1e-3)
+    # dominant kernel and its roofline
+    t = head["timers"]
+    top = max((k for k in t if t[k][1] > 0), key=lambda k: t[k][0])
+    fp64_peak = sph.measure_peak(0, local)
+    fp32_peak = sph.measure_peak(1, local)
+    pk = fp32_peak if "mixed" in results else fp64_peak
+    if top in FLOPS:
+        per_launch_ms = t[top][0] / t[top][1]
+        flops = n * head["nb_mean"] * FLOPS[top]
+        achieved = flops / (per_launch_ms * 1e-3) / 1e12
+        roof = {"bound": "fp32" if "mixed" in results else "fp64", "kernel": top,
+                "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
+                "frac": achieved / pk,
+                "peak_source": "in-repo FMA-chain probe (fsph_measure_peak), measured this run",
+                "traffic": None}
+    else:
+        roof = {"bound": "hbm", "kernel": top, "achieved": None, "peak": 6815.2,
+                "unit": "GB/s", "frac": None, "traffic": None}
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": head["ms"] / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if "mixed" in results else "f64",
+        "data": "synthetic",
+        "config": {"workload": f"sedov3d_{args.n1d}^3", "n_particles": n,
+                   "kernel": "wendland_c6", "gamma": 5.0 / 3.0, "eta": meta["eta"],
+                   "mean_neighbors": head["nb_mean"], "parallelism": f"replicas{world}",
+                   "l2": "inputs exceed L2 (state ~0.5 GB, lists ~0.8 GB); no flush",
+                   "precision": "mixed" if "mixed" in results else "fp64"},
+        "gpu_launches": head["launches"],
+        "clocks": head["clocks"],
+        "roofline": roof,
+        "per_kernel_ms_per_step": {k: v[0] / K for k, v in t.items() if v[1]},
+        "fp64": {"value": world * n * K / (results["fp64"]["ms"] * 1e-3),
+                 "ms_per_step": results["fp64"]["ms"] / K},
+    }
+    if "mixed" in results:
+        a64 = results["fp64"]["accel"]
+        am = results["mixed"]["accel"]
+        o64 = np.argsort(a64["id"])
+        om = np.argsort(am["id"])
+        A64 = np.stack([a64[k][o64] for k in ("ax", "ay", "az")], 1)
+        AM = np.stack([am[k][om] for k in ("ax", "ay", "az")], 1)
+        mag = np.linalg.norm(A64, axis=1)
+        rms = np.sqrt((mag ** 2).mean())
+        err = np.linalg.norm(AM - A64, axis=1) / np.maximum(mag, 1e-3 * rms)
+        line["mixed_vs_fp64"] = {"speedup": results["fp64"]["ms"] / results["mixed"]["ms"],
+                                 "accel_rel_err_max": float(err.max()),
+                                 "accel_rel_err_median": float(np.median(err))}
+    if "e2e" in head:
+        e = head["e2e"]
+        line["e2e"] = {"value": world * n * K / (e["ms"] * 1e-3), "unit": "particle-steps/s",
+                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"]}
+    if not args.no_cpu:
+        cpu = run_cpu_oracle(64, None, os.cpu_count() or 1, min_seconds=10.0)
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line["peaks_measured"] = {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -24,6 +24,7 @@ SOURCES = {
     "fsph_elementwise.cu": ["-fmad=false"],
     "fsph_mixed.cu": [],
     "fsph_gravity.cu": [],
+    "fsph_peak.cu": [],
     "fsph_api.cu": [],
 }
 

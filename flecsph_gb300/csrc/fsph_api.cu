@@ -56,6 +56,7 @@ struct fsph_ctx {
   long long timer_calls[FSPH_TIMER_COUNT] = {0};
   std::string last_error;
   std::vector<void *> allocs;
+  cudaEvent_t marks[64] = {};
 
   Launch L() { return Launch{stream, &launches}; }
 };
@@ -338,6 +339,9 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   for(auto & e : c->events)
     if(cudaEventCreate(&e) != cudaSuccess)
       return fail(FSPH_ERR_CUDA);
+  for(auto & e : c->marks)
+    if(cudaEventCreate(&e) != cudaSuccess)
+      return fail(FSPH_ERR_CUDA);
   *status = FSPH_OK;
   return c;
 }
@@ -351,6 +355,9 @@ void fsph_destroy(fsph_ctx * c) {
   for(void * p : c->allocs)
     cudaFree(p);
   for(auto & e : c->events)
+    if(e)
+      cudaEventDestroy(e);
+  for(auto & e : c->marks)
     if(e)
       cudaEventDestroy(e);
   if(c->stream)
@@ -390,6 +397,63 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   c->iteration = c->p.initial_iteration;
   c->tree_ok = false;
   c->uploaded = true;
+  return FSPH_OK;
+}
+
+fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
+  if(!c || !v || !c->uploaded || v->n != c->n)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  const int n = c->n;
+  const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
+    v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
+    v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
+    v->vsig, v->dt};
+  for(int k = 0; k < NF; ++k)
+    if(src[k])
+      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
+        cudaMemcpyHostToDevice, c->stream));
+  if(v->id)
+    CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n,
+      cudaMemcpyHostToDevice, c->stream));
+  return FSPH_OK;
+}
+
+fsph_status fsph_host_register(void * ptr, int64_t bytes) {
+  if(!ptr || bytes <= 0)
+    return FSPH_ERR_ARG;
+  cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+  return e == cudaSuccess ? FSPH_OK : FSPH_ERR_CUDA;
+}
+
+fsph_status fsph_host_unregister(void * ptr) {
+  if(!ptr)
+    return FSPH_ERR_ARG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? FSPH_OK : FSPH_ERR_CUDA;
+}
+
+fsph_status fsph_mark(fsph_ctx * c, int32_t slot) {
+  if(!c || slot < 0 || slot >= 64)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  CK(cudaEventRecord(c->marks[slot], c->stream));
+  return FSPH_OK;
+}
+
+fsph_status fsph_mark_elapsed(fsph_ctx * c, int32_t a, int32_t b, double * ms) {
+  if(!c || !ms || a < 0 || a >= 64 || b < 0 || b >= 64)
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  CK(cudaEventSynchronize(c->marks[b]));
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, c->marks[a], c->marks[b]));
+  *ms = f;
   return FSPH_OK;
 }
 

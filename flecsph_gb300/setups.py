@@ -64,14 +64,16 @@ def sod3d(nx=80, ny=20, nz=20, gamma=1.4, eta=1.5, seed=None):
     return s, params, meta
 
 
-def sedov3d(n1d=128, gamma=5.0 / 3.0, eta=1.44, jitter=0.01, seed=12345,
+def sedov3d(n1d=128, gamma=5.0 / 3.0, eta=1.495, jitter=0.01, seed=12345,
             energy=1.0, u0=1.0e-5):
     """3D Sedov blast on a jittered cubic lattice in [-0.5, 0.5]^3.
 
     rho = 1 (m = dx^3), u = u0, per-axis N(0, jitter*dx) jitter from
     numpy's PCG64(seed); energy E deposited as u_b += E w_b / sum(m w) with
     w_b = W_C6(r_b, 2h), i.e. kernel-weighted over particles within 2h of
-    the origin.  eta = 1.44 gives h = 2.88 dx, about 100 neighbours.
+    the origin.  eta = 1.495 gives h = 2.99 dx: with the 1% jitter the mean
+    neighbour count (self included) is 100 (93 lattice points lie within
+    2.83 dx, the next shell of 30 sits at 3 dx).
     """
     dx = 1.0 / n1d
     pos = _lattice(n1d, n1d, n1d, (-0.5, -0.5, -0.5), dx)

@@ -71,6 +71,13 @@ def library():
     lib.fsph_timers.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
     lib.fsph_launch_count.argtypes = [C.c_void_p]
     lib.fsph_launch_count.restype = C.c_int64
+    lib.fsph_upload_fields.argtypes = [C.c_void_p, C.POINTER(SoAView)]
+    lib.fsph_host_register.argtypes = [C.c_void_p, C.c_int64]
+    lib.fsph_host_unregister.argtypes = [C.c_void_p]
+    lib.fsph_mark.argtypes = [C.c_void_p, C.c_int32]
+    lib.fsph_mark_elapsed.argtypes = [C.c_void_p, C.c_int32, C.c_int32,
+                                      C.POINTER(C.c_double)]
+    lib.fsph_measure_peak.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_double)]
     _lib = lib
     return lib
 
@@ -140,6 +147,22 @@ class BodySystem:
             out = {k: out[k] for k in fields}
         return out
 
+    def upload_fields(self, view):
+        """Copy the non-NULL fields of an fsph_soa_view (host pointers) into
+        the current particle order without touching time or iteration."""
+        self._check(self.lib.fsph_upload_fields(self.ctx, C.byref(view)), "upload_fields")
+
+    def download_into(self, view):
+        self._check(self.lib.fsph_download(self.ctx, C.byref(view)), "download")
+
+    def mark(self, slot):
+        self._check(self.lib.fsph_mark(self.ctx, slot), "mark")
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_double()
+        self._check(self.lib.fsph_mark_elapsed(self.ctx, a, b, C.byref(ms)), "mark_elapsed")
+        return ms.value
+
     def time(self):
         dt, t, it = C.c_double(), C.c_double(), C.c_int64()
         self._check(self.lib.fsph_get_time(self.ctx, C.byref(dt), C.byref(t), C.byref(it)),
@@ -195,3 +218,23 @@ class BodySystem:
 
     def gravitation_fmm(self):
         self.gravitation()
+
+
+def host_register(arr):
+    """Pin a numpy array's memory for full-speed host<->device copies."""
+    st = library().fsph_host_register(arr.ctypes.data, arr.nbytes)
+    if st:
+        raise FsphError(st, "host_register")
+
+
+def host_unregister(arr):
+    library().fsph_host_unregister(arr.ctypes.data)
+
+
+def measure_peak(kind, device=0):
+    """Measured FMA throughput of the device in TFLOP/s: kind 0 FP64, 1 FP32."""
+    v = C.c_double()
+    st = library().fsph_measure_peak(device, kind, C.byref(v))
+    if st:
+        raise FsphError(st, "measure_peak")
+    return v.value

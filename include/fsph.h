@@ -204,6 +204,14 @@ const char * fsph_last_error(const fsph_ctx * ctx);
 fsph_status fsph_upload(fsph_ctx * ctx, const fsph_soa_view * host);
 /* Device -> host copy, current (sorted) order.  Synchronous. */
 fsph_status fsph_download(fsph_ctx * ctx, fsph_soa_view * host);
+/* Host -> device copy of the non-NULL fields of `host` (host->n must equal
+ * the uploaded count) into the current particle order, keeping time,
+ * iteration and tree state: the per-step input path of a host-side driver. */
+fsph_status fsph_upload_fields(fsph_ctx * ctx, const fsph_soa_view * host);
+/* Page-lock (pin) / release a host buffer so the copies above run at full
+ * link speed.  Thin wrappers over cudaHostRegister/cudaHostUnregister. */
+fsph_status fsph_host_register(void * ptr, int64_t bytes);
+fsph_status fsph_host_unregister(void * ptr);
 fsph_status fsph_get_time(fsph_ctx * ctx, double * dt, double * totaltime,
   int64_t * iteration);
 fsph_status fsph_set_time(fsph_ctx * ctx, double dt, double totaltime,
@@ -261,6 +269,14 @@ fsph_status fsph_timers(fsph_ctx * ctx, double * ms, int32_t count,
 fsph_status fsph_timers_reset(fsph_ctx * ctx);
 /* Number of kernel launches this context has issued (all kinds). */
 int64_t fsph_launch_count(const fsph_ctx * ctx);
+/* Record CUDA event `slot` (0..63) on the context's stream; elapsed device
+ * time between two recorded slots (synchronises on the later one). */
+fsph_status fsph_mark(fsph_ctx * ctx, int32_t slot);
+fsph_status fsph_mark_elapsed(fsph_ctx * ctx, int32_t from, int32_t to,
+  double * ms);
+/* Measured arithmetic peak of `device`: kind 0 = FP64 FMA, 1 = FP32 FMA,
+ * in TFLOP/s (2 flops per FMA), from a register-resident FMA chain kernel. */
+fsph_status fsph_measure_peak(int32_t device, int32_t kind, double * tflops);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ def cases():
     s, p, m = setups.sod3d(40, 10, 10)
     p.thermokinetic_formulation = 0
     yield "sod3d_dudt_4000", setups.shuffled(s, 2), p, 2
-    s, p, m = setups.sedov3d(16)
+    s, p, m = setups.sedov3d(16, eta=1.44)
     yield "sedov3d_4096", setups.shuffled(s, 3), p, 2
     s, p, m = setups.polytrope3d(3000)
     p.enable_fmm = 0
