@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfsph_gb300.so")
+DRIVER = os.path.join(HERE, "hydro_driver")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = {
@@ -76,7 +77,19 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+def build_driver():
+    """The C++ hydro driver (csrc/hydro_driver.cpp) over the C ABI."""
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", os.path.join(CSRC, "hydro_driver.cpp"),
+           "-L" + HERE, "-lfsph_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
