@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "fsph_internal.cuh"
 
 namespace fsph {
@@ -781,3 +783,82 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
 }
 
 }  // namespace fsph
+
+// ------------------------------------------- allocation-free key sort --
+// Range, Morton keys and the radix sort of fsph_update_iteration for
+// callers that must not allocate device memory themselves -- for example a
+// host application whose device memory is owned by its own pool allocator,
+// or a time-critical loop in which cudaMalloc/cudaFree (which may
+// synchronise the device) are not acceptable.  Its scratch (range words,
+// ping-pong keys and indices, digit histogram) is this file-scope array,
+// sized for FSPH_NOALLOC_SORT_MAX particles: 12,845,312 bytes that every
+// GPU loading the library holds until the process exits.
+#define FSPH_NOALLOC_SORT_MAX (1 << 20)
+#define NOALLOC_RANGE_BYTES 256
+#define NOALLOC_KEYS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 8)
+#define NOALLOC_VALS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 4)
+#define NOALLOC_HIST_BYTES ((size_t)256 * (FSPH_NOALLOC_SORT_MAX / RS_TILE) * 4)
+#define NOALLOC_TOTAL \
+  (NOALLOC_RANGE_BYTES + NOALLOC_KEYS_BYTES + NOALLOC_VALS_BYTES + NOALLOC_HIST_BYTES)
+
+namespace fsph {
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_TOTAL];
+}  // namespace fsph
+
+namespace {
+// Device address of g_noalloc_scratch per device.  In host code the symbol
+// names a host-side shadow, not device memory, so the address must come
+// from cudaGetSymbolAddress, taken once per device with that device current.
+std::mutex g_noalloc_mu;
+void * g_noalloc_addr[64] = {};
+}  // namespace
+
+extern "C" fsph_status fsph_sort_keys_noalloc(const double * x,
+  const double * y, const double * z, const double * h, int64_t n,
+  int32_t dimension, uint64_t * keys_out, int32_t * perm_out, void * stream) {
+  using namespace fsph;
+  if(n < 2 || n > FSPH_NOALLOC_SORT_MAX || (dimension != 2 && dimension != 3) ||
+     !x || !y || (dimension == 3 && !z) || !h || !keys_out || !perm_out)
+    return FSPH_ERR_ARG;
+  int dev = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return FSPH_ERR_NO_DEVICE;
+  void * base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if(!g_noalloc_addr[dev]) {
+      void * ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if(e != cudaSuccess || !ptr)
+        return FSPH_ERR_CUDA;
+      g_noalloc_addr[dev] = ptr;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  unsigned char * b = (unsigned char *)base;
+  double * range = (double *)b;
+  unsigned long long * ktmp = (unsigned long long *)(b + NOALLOC_RANGE_BYTES);
+  int * vtmp = (int *)(b + NOALLOC_RANGE_BYTES + NOALLOC_KEYS_BYTES);
+  unsigned * hist =
+    (unsigned *)(b + NOALLOC_RANGE_BYTES + NOALLOC_KEYS_BYTES + NOALLOC_VALS_BYTES);
+  Particles P{};
+  P.f[F_X] = const_cast<double *>(x);
+  P.f[F_Y] = const_cast<double *>(y);
+  P.f[F_Z] = const_cast<double *>(z ? z : y);
+  P.f[F_H] = const_cast<double *>(h);
+  P.n = (int)n;
+  PhysParams pp{};
+  pp.dim = dimension;
+  long long launches = 0;
+  Launch L{(cudaStream_t)stream, &launches};
+  // every scratch word that is read is first written by these launches: the
+  // range words by k_range_init, the histogram by k_radix_hist per pass
+  if(launch_range_keys(L, P, pp, range, (unsigned long long *)keys_out,
+       perm_out) != cudaSuccess)
+    return FSPH_ERR_CUDA;
+  if(radix_sort_pairs(L, (unsigned long long *)keys_out, perm_out, ktmp, vtmp,
+       (int)n, hist, 0) != cudaSuccess)
+    return FSPH_ERR_CUDA;
+  return FSPH_OK;
+}
+

@@ -274,6 +274,23 @@ int64_t fsph_launch_count(const fsph_ctx * ctx);
 fsph_status fsph_mark(fsph_ctx * ctx, int32_t slot);
 fsph_status fsph_mark_elapsed(fsph_ctx * ctx, int32_t from, int32_t to,
   double * ms);
+/* Allocation-free variant of the range + Morton-key + radix-sort part of
+ * fsph_update_iteration, with no counterpart in the reference.  For callers
+ * that must not allocate device memory (an application whose device memory
+ * belongs to its own pool allocator, or a time-critical loop where
+ * cudaMalloc/cudaFree could synchronise the device).  Inputs x, y, z (NULL
+ * in 2D) and h and outputs keys_out[n] (sorted Morton keys) and
+ * perm_out[n] (input index of each sorted position) are DEVICE pointers of
+ * the caller; work is enqueued on `stream` (a cudaStream_t, NULL = default)
+ * of the current device.  Scratch is a fixed 12.25 MiB static device array
+ * in the library, so n must be in [2, 1048576] (FSPH_ERR_ARG otherwise),
+ * and every call shares it: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  Nothing is allocated. */
+fsph_status fsph_sort_keys_noalloc(const double * x, const double * y,
+  const double * z, const double * h, int64_t n, int32_t dimension,
+  uint64_t * keys_out, int32_t * perm_out, void * stream);
 /* Measured arithmetic peak of `device`: kind 0 = FP64 FMA, 1 = FP32 FMA,
  * in TFLOP/s (2 flops per FMA), from a register-resident FMA chain kernel. */
 fsph_status fsph_measure_peak(int32_t device, int32_t kind, double * tflops);
