@@ -218,8 +218,10 @@ def gpu_arm(args):
         prec = "mixed" if mixed_ok else "fp64"
     results = {}
     modes = ["fp64"] + (["mixed"] if mixed_ok else [])
-    if prec == "fp64":
+    if args.precision == "fp64":
         modes = ["fp64"]
+    elif args.precision == "mixed":
+        modes = ["mixed"]
     for mode in modes:
         p.precision_mode = PRECISION_MIXED if mode == "mixed" else PRECISION_FP64
         bs = sph.BodySystem(p, n, device=local)
@@ -318,10 +320,11 @@ def gpu_arm(args):
         "clocks": head["clocks"],
         "roofline": roof,
         "per_kernel_ms_per_step": {k: v[0] / K for k, v in t.items() if v[1]},
-        "fp64": {"value": world * n * K / (results["fp64"]["ms"] * 1e-3),
-                 "ms_per_step": results["fp64"]["ms"] / K},
     }
-    if "mixed" in results:
+    if "fp64" in results:
+        line["fp64"] = {"value": world * n * K / (results["fp64"]["ms"] * 1e-3),
+                        "ms_per_step": results["fp64"]["ms"] / K}
+    if "mixed" in results and "fp64" in results:
         a64 = results["fp64"]["accel"]
         am = results["mixed"]["accel"]
         o64 = np.argsort(a64["id"])

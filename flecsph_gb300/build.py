@@ -23,7 +23,7 @@ SOURCES = {
     "fsph_tree.cu": ["-fmad=false"],
     "fsph_fp64.cu": ["-fmad=false"],
     "fsph_elementwise.cu": ["-fmad=false"],
-    "fsph_mixed.cu": [],
+    "fsph_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "fsph_gravity.cu": [],
     "fsph_peak.cu": [],
     "fsph_api.cu": [],

@@ -40,6 +40,8 @@ struct fsph_ctx {
   unsigned long long * d_range = nullptr;
   Tree T{};
   Lists Ls{};
+  Packed K{};
+  bool mixed = false;
   DevTime * d_time = nullptr;
   DevStatus * d_status = nullptr;
   double * d_cons = nullptr;
@@ -314,7 +316,7 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->T.leaf_parent, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.first, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.last, N) == cudaSuccess;
-  ok &= dalloc(c, &c->T.box, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.qbox, 2 * N) == cudaSuccess;
   ok &= dalloc(c, &c->T.box2, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.opar, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.gref, N) == cudaSuccess;
@@ -323,6 +325,12 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->T.group_first, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.group_last, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.ngroups, 1) == cudaSuccess;
+  ok &= dalloc(c, &c->K.qpos, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.vhm, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.vel, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.thermo, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
+  c->mixed = p->precision_mode == FSPH_PRECISION_MIXED;
   c->Ls.maxnb = p->max_neighbors;
   ok &= dalloc(c, &c->Ls.idx, Npad * (size_t)p->max_neighbors) == cudaSuccess;
   ok &= dalloc(c, &c->Ls.cnt, N) == cudaSuccess;
@@ -581,12 +589,15 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   }
   {
     Phase ph(c, FSPH_TIMER_TREE);
-    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX));
+    CK(launch_pack_positions(L, c->P, c->pp, c->d_range, c->K));
+    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX, c->d_range, c->K.qpos));
   }
   {
+    // FP64 mode keeps each list in the reference's order so its sums round
+    // like the reference's; the mixed path only needs the set
     Phase ph(c, FSPH_TIMER_NEIGHBORS);
     CK(launch_neighbors(L, c->P, c->pp, c->T, c->Ls, c->d_status, c->nsm,
-      c->d_range));
+      c->d_range, c->K, c->mixed ? 0 : 1));
   }
   c->tree_ok = true;
   return FSPH_OK;
@@ -601,18 +612,28 @@ fsph_status fsph_reset_ghosts(fsph_ctx * c) {
   return FSPH_OK;
 }
 
-fsph_status fsph_density_pressure_soundspeed(fsph_ctx * c) {
+static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
   fsph_status s = set_device(c);
   if(s)
     return s;
   Launch L = c->L();
-  {
-    Phase ph(c, FSPH_TIMER_DENSITY);
-    CK(launch_density_fp64(L, c->P, c->pp, c->Ls, c->cs_new, c->d_status));
+  if(c->mixed) {
+    {
+      Phase ph(c, FSPH_TIMER_DENSITY);
+      CK(launch_density_mixed(L, c->P, c->pp, c->Ls, c->K, c->cs_new, c->d_status));
+    }
+    if(with_vsig) {
+      Phase ph(c, FSPH_TIMER_VSIG);
+      CK(launch_vsig_mixed(L, c->P, c->pp, c->Ls, c->K));
+    }
   }
-  {
+  else {
+    {
+      Phase ph(c, FSPH_TIMER_DENSITY);
+      CK(launch_density_fp64(L, c->P, c->pp, c->Ls, c->cs_new, c->d_status));
+    }
     Phase ph(c, FSPH_TIMER_VSIG);
     CK(launch_vsig_fp64(L, c->P, c->pp, c->Ls, c->cs_new));
   }
@@ -620,11 +641,14 @@ fsph_status fsph_density_pressure_soundspeed(fsph_ctx * c) {
   double * t = c->P.f[F_CS];
   c->P.f[F_CS] = c->cs_new;
   c->cs_new = t;
-  // keep the alternate set's pointer table consistent for the next permute
   return FSPH_OK;
 }
 
-static fsph_status accel_impl(fsph_ctx * c, int kick) {
+fsph_status fsph_density_pressure_soundspeed(fsph_ctx * c) {
+  return density_impl(c, true);
+}
+
+static fsph_status accel_impl(fsph_ctx * c, int kick, int fused_vsig = 0) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
   fsph_status s = set_device(c);
@@ -632,7 +656,10 @@ static fsph_status accel_impl(fsph_ctx * c, int kick) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ACCEL);
-  CK(launch_accel_fp64(L, c->P, c->pp, c->Ls, kick, c->d_time));
+  if(c->mixed)
+    CK(launch_accel_mixed(L, c->P, c->pp, c->Ls, c->K, kick, c->d_time, fused_vsig));
+  else
+    CK(launch_accel_fp64(L, c->P, c->pp, c->Ls, kick, c->d_time));
   return FSPH_OK;
 }
 
@@ -646,7 +673,10 @@ fsph_status fsph_dudt(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
-  CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
+  if(c->mixed)
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K));
+  else
+    CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
   return FSPH_OK;
 }
 
@@ -658,7 +688,10 @@ fsph_status fsph_dedt(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
-  CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
+  if(c->mixed)
+    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K));
+  else
+    CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
   return FSPH_OK;
 }
 
@@ -716,7 +749,15 @@ fsph_status fsph_compute_dt(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_DT);
-  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status));
+  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 0));
+  return FSPH_OK;
+}
+
+// compute_dt preceded by check_nans and check_negativity in one pass
+static fsph_status checks_and_dt(fsph_ctx * c) {
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_DT);
+  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 1));
   return FSPH_OK;
 }
 
@@ -774,9 +815,10 @@ fsph_status fsph_step(fsph_ctx * c) {
     TRY(fsph_eos_init(c));
     if(thermo)
       TRY(fsph_set_total_energy(c));
-    TRY(fsph_density_pressure_soundspeed(c));
+    // mixed: the signal speed rides in the acceleration loop
+    TRY(density_impl(c, !c->mixed));
     TRY(fsph_save_velocityhalf(c));
-    TRY(accel_impl(c, 0));
+    TRY(accel_impl(c, 0, c->mixed));
     if(p.adaptive_timestep) {
       TRY(fsph_compute_dt(c));
       TRY(fsph_set_adaptive_timestep(c));
@@ -798,8 +840,8 @@ fsph_status fsph_step(fsph_ctx * c) {
     TRY(elem(c, !evolve ? OP_KICK_DRIFT_NONE : (thermo ? OP_KICK_DRIFT_E : OP_KICK_DRIFT_U),
       FSPH_TIMER_INTEGRATE));
     TRY(fsph_update_iteration(c));
-    TRY(fsph_density_pressure_soundspeed(c));
-    TRY(accel_impl(c, 1));
+    TRY(density_impl(c, !c->mixed));
+    TRY(accel_impl(c, 1, c->mixed));
     if(evolve) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         const bool lastp = m == p.pressure_updates_number;
@@ -820,11 +862,13 @@ fsph_status fsph_step(fsph_ctx * c) {
     TRY(fsph_compute_smoothinglength(c));
   else if(p.sph_update_uniform_h)
     TRY(fsph_compute_average_smoothinglength(c));
-  TRY(fsph_check_nans(c));
-  TRY(fsph_check_negativity(c));
   if(p.adaptive_timestep) {
-    TRY(fsph_compute_dt(c));
+    TRY(checks_and_dt(c));
     TRY(fsph_set_adaptive_timestep(c));
+  }
+  else {
+    TRY(fsph_check_nans(c));
+    TRY(fsph_check_negativity(c));
   }
   return fsph_advance_time(c);
 }

@@ -167,13 +167,33 @@ cudaError_t launch_elementwise(const Launch & L, const Particles & P,
 // compute_dt (default_physics.h:602-695) per particle, then the minimum.
 __global__ void k_dt_init(DevTime * t) { t->dtmin_bits = ord_enc_e(1e24); }
 
-template<int D>
+// CHECKS folds check_nans and check_negativity (default_physics.h:918-979)
+// into the same pass, as the driver runs them back to back before dt.
+template<int D, bool CHECKS>
 __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
   PhysParams pp, DevTime * tm, DevStatus * st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double dtmin = 1e24;
   if(i < P.n) {
     double ** f = P.f;
+    if(CHECKS) {
+      bool bad = false;
+      for(int d = 0; d < D; ++d) {
+        double q[5] = {f[F_X + d][i], f[F_VX + d][i], f[F_VHX + d][i],
+          f[F_AX + d][i], f[F_GAX + d][i]};
+        for(int k = 0; k < 5; ++k)
+          bad |= q[k] != q[k];
+      }
+      const int sc[] = {F_M, F_GPOT, F_RHO, F_P, F_E, F_DEDT, F_DUDT, F_K, F_VSIG};
+      for(int k = 0; k < 9; ++k)
+        bad |= f[sc[k]][i] != f[sc[k]][i];
+      if(pp.evolve_u)
+        bad |= f[F_U][i] != f[F_U][i];
+      if(bad)
+        raise_status(st, FSPH_ERR_NAN, i);
+      if(f[F_RHO][i] < 0 || f[F_P][i] < 0 || (pp.evolve_u && f[F_U][i] < 0))
+        raise_status(st, FSPH_ERR_NEGATIVITY, i);
+    }
     const double tiny = 1e-24, mc = 0.6;
     const double dx = f[F_H][i] / (pp.eta * pp.kw);
     double vn = 0;
@@ -217,13 +237,21 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
 }
 
 cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
-  const PhysParams & pp, DevTime * t, DevStatus * st) {
+  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks) {
   k_dt_init<<<1, 1, 0, L.stream>>>(t);
   const int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
-  if(pp.dim == 3)
-    k_compute_dt<3><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
-  else
-    k_compute_dt<2><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+  if(pp.dim == 3) {
+    if(with_checks)
+      k_compute_dt<3, true><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+    else
+      k_compute_dt<3, false><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+  }
+  else {
+    if(with_checks)
+      k_compute_dt<2, true><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+    else
+      k_compute_dt<2, false><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+  }
   *L.counter += 2;
   return cudaGetLastError();
 }

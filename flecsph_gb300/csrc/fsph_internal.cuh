@@ -66,7 +66,8 @@ struct Tree {
   int * leaf_parent;  // particle -> parent internal node
   int * first;
   int * last;
-  NodeBox * box;
+  int4 * qbox;             // per node: {lo.xyz, float bits of h_max}, {hi.xyz, 0}
+                           // in the fixed-point position space of Packed::qpos
   NodeBox * box2;          // reference node box: union of [x - h/2, x + h/2]
   int * opar;              // particle -> binary node standing for its octree parent
   int * gref;              // particle -> its reference traversal group
@@ -75,6 +76,17 @@ struct Tree {
   int * group_first;
   int * group_last;
   int * ngroups;           // device scalar
+};
+
+// Packed FP32 records of the mixed-precision path (rebuilt every step).
+// Positions are 31-bit fixed point over the step's range: differences are
+// exact integers, so separations keep ~1e-9 of the range.
+struct Packed {
+  int4 * qpos;      // {qx, qy, qz, float bits of h}
+  float4 * vhm;     // {vh_x, vh_y, vh_z, m}
+  float4 * vel;     // {v_x, v_y, v_z, 0}
+  float4 * thermo;  // {rho, P/rho^2, c_s (new), c_s (previous)}
+  float * qscale;   // device [3]: range extent / 2^31 per axis
 };
 
 struct Lists {
@@ -106,11 +118,29 @@ cudaError_t launch_check_duplicates(const Launch & L,
   const unsigned long long * keys, int n, DevStatus * st);
 cudaError_t launch_permute(const Launch & L, const Particles & src,
   const Particles & dst, const int * perm, const unsigned long long * keys);
+struct Packed;
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
-  const PhysParams & pp, Tree & T, int group_max);
+  const PhysParams & pp, Tree & T, int group_max,
+  const unsigned long long * rbits, const int4 * qpos);
 cudaError_t launch_neighbors(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, Lists & Ls, DevStatus * st, int nsm,
-  const unsigned long long * rbits);
+  const unsigned long long * rbits, const Packed & K, int ordered);
+
+// ---- fsph_mixed.cu ----
+cudaError_t launch_pack_positions(const Launch & L, const Particles & P,
+  const PhysParams & pp, const unsigned long long * rbits, const Packed & K);
+cudaError_t launch_density_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
+  DevStatus * st);
+cudaError_t launch_vsig_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K);
+cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
+  const DevTime * t, int fused_vsig);
+cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K);
+cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K);
 
 // ---- fsph_fp64.cu ----
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
@@ -134,7 +164,7 @@ enum ElemOp {
 cudaError_t launch_elementwise(const Launch & L, const Particles & P,
   const PhysParams & pp, int op, DevTime * t, DevStatus * st);
 cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
-  const PhysParams & pp, DevTime * t, DevStatus * st);
+  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks);
 cudaError_t launch_set_adaptive_timestep(const Launch & L,
   const PhysParams & pp, DevTime * t);
 cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,

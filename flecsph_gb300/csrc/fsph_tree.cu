@@ -161,7 +161,7 @@ cudaError_t launch_range_keys(const Launch & L, const Particles & P,
 
 size_t radix_hist_entries(int n) {
   size_t nb = ((size_t)n + RS_TILE - 1) / RS_TILE;
-  return 256 * nb;
+  return 256 * nb + 256;  // [digit][tile] counts, then the 256 digit totals
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(
@@ -179,30 +179,44 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(
   hist[threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
 }
 
-// Exclusive scan of `m` counters by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_excl(unsigned * a, int m) {
-  __shared__ unsigned part[1024];
-  int per = (m + 1023) / 1024;
-  int b0 = threadIdx.x * per;
-  unsigned s = 0;
-  for(int k = 0; k < per; ++k)
-    if(b0 + k < m)
-      s += a[b0 + k];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  for(int o = 1; o < 1024; o <<= 1) {
-    unsigned v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+// Per digit: exclusive scan of its row of tile counts (coalesced, one
+// block per digit) and the row total in tot[digit].
+__global__ void __launch_bounds__(1024) k_scan_rows(unsigned * hist, int nb,
+  unsigned * tot) {
+  __shared__ unsigned wsum[32];
+  const int d = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  unsigned * row = hist + (size_t)d * nb;
+  unsigned run = 0;
+  for(int base = 0; base < nb; base += 1024) {
+    const int i = base + t;
+    const unsigned v = i < nb ? row[i] : 0u;
+    unsigned x = v;
+    for(int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(FULL, x, o);
+      if(lane >= o)
+        x += y;
+    }
+    if(lane == 31)
+      wsum[w] = x;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if(w == 0) {
+      unsigned s2 = wsum[lane];
+      for(int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(FULL, s2, o);
+        if(lane >= o)
+          s2 += y;
+      }
+      wsum[lane] = s2;
+    }
+    __syncthreads();
+    const unsigned excl = run + (w ? wsum[w - 1] : 0u) + x - v;
+    if(i < nb)
+      row[i] = excl;
+    run += wsum[31];
     __syncthreads();
   }
-  unsigned run = part[threadIdx.x] - s;
-  for(int k = 0; k < per; ++k)
-    if(b0 + k < m) {
-      unsigned v = a[b0 + k];
-      a[b0 + k] = run;
-      run += v;
-    }
+  if(t == 0)
+    tot[d] = run;
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
@@ -211,8 +225,26 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
   __shared__ unsigned base[256];
   __shared__ unsigned running[256];
   __shared__ unsigned wcnt[RS_THREADS / 32][256];
+  __shared__ unsigned wtot[RS_THREADS / 32];
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-  base[t] = offs[t * gridDim.x + blockIdx.x];
+  // digit base = sum of the totals of smaller digits (block-wide scan of
+  // the 256 row totals) + this tile's offset within its digit row
+  {
+    const unsigned v = offs[256 * gridDim.x + t];
+    unsigned x = v;
+    for(int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(FULL, x, o);
+      if(lane >= o)
+        x += y;
+    }
+    if(lane == 31)
+      wtot[w] = x;
+    __syncthreads();
+    unsigned pre = 0;
+    for(int k = 0; k < w; ++k)
+      pre += wtot[k];
+    base[t] = pre + x - v + offs[t * gridDim.x + blockIdx.x];
+  }
   running[t] = 0;
   for(int k = 0; k < RS_THREADS / 32; ++k)
     wcnt[k][t] = 0;
@@ -257,7 +289,7 @@ cudaError_t radix_sort_pairs(const Launch & L, unsigned long long * keys,
   int *va = vals, *vb = vals_tmp;
   for(int shift = 0; shift < 64; shift += 8) {
     k_radix_hist<<<nb, RS_THREADS, 0, L.stream>>>(ka, n, shift, hist);
-    k_scan_excl<<<1, 1024, 0, L.stream>>>(hist, 256 * nb);
+    k_scan_rows<<<256, 1024, 0, L.stream>>>(hist, nb, hist + (size_t)256 * nb);
     k_radix_scatter<<<nb, RS_THREADS, 0, L.stream>>>(ka, va, kb, vb, n, shift,
       hist);
     *L.counter += 3;
@@ -382,58 +414,71 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
   ed[i] = (unsigned char)(best + 1);
 }
 
-// Bottom-up bounding boxes of positions and the largest h per node.
-__global__ void k_bounds(Particles P, int dim, Tree T) {
+// Bottom-up node data: the fixed-point position box and the largest h of
+// every node (what the neighbour walk prunes with), and, only when h
+// varies, the reference's FP64 box of x -/+ h/2 (compute_cofm,
+// default_physics.h:79-82,90-93) used by ref_node_tests.
+__global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
+  const unsigned long long * rbits) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
+  const bool nonuni = rbits[6] != rbits[7];
   int p = T.leaf_parent[i];
   while(p >= 0) {
     __threadfence();
     if(atomicAdd(&T.counter[p], 1u) == 0)
       return;  // the sibling subtree is not finished yet
-    NodeBox nb, n2;
-    nb.hmax = 0;
-    nb.pad = 0;
+    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
+    int hi[3] = {-1, -1, -1};
+    float hm = 0.f;
+    NodeBox n2;
     n2.hmax = 0;
     n2.pad = 0;
     for(int d = 0; d < 3; ++d) {
-      nb.lo[d] = n2.lo[d] = 1e308;
-      nb.hi[d] = n2.hi[d] = -1e308;
+      n2.lo[d] = 1e308;
+      n2.hi[d] = -1e308;
     }
     int ch[2] = {T.left[p], T.right[p]};
     for(int c = 0; c < 2; ++c) {
       if(ch[c] < 0) {
-        int j = ~ch[c];
-        const double hj = P.f[F_H][j];
-        for(int d = 0; d < dim; ++d) {
-          double x = P.f[F_X + d][j];
-          nb.lo[d] = fmin(nb.lo[d], x);
-          nb.hi[d] = fmax(nb.hi[d], x);
-          // compute_cofm's bmin/bmax (default_physics.h:79-82)
-          n2.lo[d] = fmin(n2.lo[d], x - hj / 2.);
-          n2.hi[d] = fmax(n2.hi[d], x + hj / 2.);
+        const int j = ~ch[c];
+        const int4 q = qpos[j];
+        lo[0] = min(lo[0], q.x); hi[0] = max(hi[0], q.x);
+        lo[1] = min(lo[1], q.y); hi[1] = max(hi[1], q.y);
+        lo[2] = min(lo[2], q.z); hi[2] = max(hi[2], q.z);
+        hm = fmaxf(hm, __int_as_float(q.w));
+        if(nonuni) {
+          const double hj = P.f[F_H][j];
+          for(int d = 0; d < dim; ++d) {
+            double x = P.f[F_X + d][j];
+            n2.lo[d] = fmin(n2.lo[d], x - hj / 2.);
+            n2.hi[d] = fmax(n2.hi[d], x + hj / 2.);
+          }
         }
-        nb.hmax = fmax(nb.hmax, hj);
       }
       else {
-        const double * cb = (const double *)&T.box[ch[c]];
-        const double * cb2 = (const double *)&T.box2[ch[c]];
-        for(int d = 0; d < dim; ++d) {
-          nb.lo[d] = fmin(nb.lo[d], __ldcg(cb + d));
-          nb.hi[d] = fmax(nb.hi[d], __ldcg(cb + 4 + d));
-          n2.lo[d] = fmin(n2.lo[d], __ldcg(cb2 + d));
-          n2.hi[d] = fmax(n2.hi[d], __ldcg(cb2 + 4 + d));
+        const int4 * cq = &T.qbox[2 * ch[c]];
+        const int4 a = __ldcg(cq), b = __ldcg(cq + 1);
+        lo[0] = min(lo[0], a.x); lo[1] = min(lo[1], a.y); lo[2] = min(lo[2], a.z);
+        hi[0] = max(hi[0], b.x); hi[1] = max(hi[1], b.y); hi[2] = max(hi[2], b.z);
+        hm = fmaxf(hm, __int_as_float(a.w));
+        if(nonuni) {
+          const double * cb2 = (const double *)&T.box2[ch[c]];
+          for(int d = 0; d < dim; ++d) {
+            n2.lo[d] = fmin(n2.lo[d], __ldcg(cb2 + d));
+            n2.hi[d] = fmax(n2.hi[d], __ldcg(cb2 + 4 + d));
+          }
         }
-        nb.hmax = fmax(nb.hmax, __ldcg(cb + 3));
       }
     }
-    if(dim == 2) {
-      nb.lo[2] = nb.hi[2] = 0;
-      n2.lo[2] = n2.hi[2] = 0;
+    T.qbox[2 * p] = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
+    T.qbox[2 * p + 1] = make_int4(hi[0], hi[1], hi[2], 0);
+    if(nonuni) {
+      if(dim == 2)
+        n2.lo[2] = n2.hi[2] = 0;
+      T.box2[p] = n2;
     }
-    T.box[p] = nb;
-    T.box2[p] = n2;
     __threadfence();
     p = T.parent[p];
   }
@@ -499,13 +544,14 @@ __global__ void k_refgroups(const unsigned long long * K, int n, int dim,
 }
 
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
-  const PhysParams & pp, Tree & T, int group_max) {
+  const PhysParams & pp, Tree & T, int group_max,
+  const unsigned long long * rbits, const int4 * qpos) {
   const int n = P.n;
   cudaMemsetAsync(T.counter, 0, sizeof(unsigned) * (size_t)n, L.stream);
   cudaMemsetAsync(T.ngroups, 0, sizeof(int), L.stream);
   k_karras<<<(n + 254) / 256, 256, 0, L.stream>>>(P.key, n, T);
   k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
-  k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T);
+  k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits);
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max);
   k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T);
   *L.counter += 5;
@@ -524,9 +570,10 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 //     (dx*dx + dy*dy) + dz*dz <= max(h_a, h_b)^2   in FP64, no FMA.
 // The candidate order makes each list come out in the order in which the
 // reference's breadth-first walk appends neighbours (by depth, then key).
-#define NB_WARPS 4
+#define NB_WARPS 8
 #define NB_STACK 1024
-#define NB_CAND 2048
+#define NB_CAND_ORDERED 2048
+#define NB_CAND 512
 
 __device__ __forceinline__ void warp_bitonic(unsigned long long * a, int m,
   int lane) {
@@ -614,12 +661,52 @@ __device__ bool ref_node_tests(const Tree & T, const double * X,
   return false;
 }
 
+// Conservative pruning test in the fixed-point space: the separation of
+// two boxes per axis, less one quantisation step (each coordinate is
+// within half a step of the true one), against max(h) with 1e-5 slack.
+__device__ __forceinline__ bool box_near(int4 glo, int4 ghi, float hg,
+  int4 lo, int4 hi, float hn, float s0, float s1, float s2) {
+  int sx = max(0, max(lo.x - ghi.x, glo.x - hi.x) - 1);
+  int sy = max(0, max(lo.y - ghi.y, glo.y - hi.y) - 1);
+  int sz = max(0, max(lo.z - ghi.z, glo.z - hi.z) - 1);
+  float fx = (float)sx * s0, fy = (float)sy * s1, fz = (float)sz * s2;
+  float R = fmaxf(hg, hn);
+  return fx * fx + fy * fy + fz * fz <= R * R * 1.00001f;
+}
+
+// One warp per group (<= 32 particles, lane = member).  The warp walks the
+// radix tree with a shared-memory stack, up to 32 nodes per round (one per
+// lane), pruning a node when its box lies farther from the group's box than
+// max(h_max(group), h_max(node)) -- conservative, so no pair with
+// d <= max(h_a, h_b) is lost.  Surviving particles are staged as candidates
+// in shared memory and filtered by every member with the reference
+// predicate (tree_geometry.h:265-276, as applied at tree_topology.h:372-379),
+//     (dx*dx + dy*dy) + dz*dz <= max(h_a, h_b)^2   in FP64, no FMA,
+// decided first in FP32 from the fixed-point positions with a margin well
+// above that estimate's error; only pairs inside the margin pay the FP64
+// test.  ORDERED (the FP64 path) sorts the candidates by (reference octree
+// depth, index) before filtering, so each list comes out in the order in
+// which the reference's breadth-first walk appends neighbours.
+template<bool ORDERED>
 __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
-  Tree T, Lists Ls, DevStatus * st, int dim, const unsigned long long * rbits) {
-  extern __shared__ unsigned long long smem_u64[];
+  Tree T, Lists Ls, DevStatus * st, int dim, const unsigned long long * rbits,
+  Packed K) {
+  extern __shared__ __align__(16) unsigned char smem[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned long long * cand = smem_u64 + (size_t)w * NB_CAND;
-  int * stack = (int *)(smem_u64 + (size_t)NB_WARPS * NB_CAND) + w * NB_STACK;
+  const int cap = ORDERED ? NB_CAND_ORDERED : NB_CAND;
+  unsigned long long * ckey = nullptr;
+  int4 * cq = nullptr;
+  int * cidx = nullptr;
+  int * stack;
+  if(ORDERED) {
+    ckey = (unsigned long long *)smem + (size_t)w * NB_CAND_ORDERED;
+    stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND_ORDERED * 8) + w * NB_STACK;
+  }
+  else {
+    cq = (int4 *)smem + (size_t)w * NB_CAND;
+    cidx = (int *)(smem + (size_t)NB_WARPS * NB_CAND * 16) + w * NB_CAND;
+    stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND * 20) + w * NB_STACK;
+  }
   const unsigned lt = lanemask_lt();
   const double * X = P.f[F_X];
   const double * Y = P.f[F_Y];
@@ -628,18 +715,17 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
   const int ngroups = *T.ngroups;
   const int maxnb = Ls.maxnb;
   const bool nonuni = rbits[6] != rbits[7];
+  const float qs0 = K.qscale[0], qs1 = K.qscale[1], qs2 = dim == 3 ? K.qscale[2] : 0.f;
+  const float qmax = fmaxf(qs0, fmaxf(qs1, qs2));
   for(int g = blockIdx.x * NB_WARPS + w; g < ngroups;
       g += gridDim.x * NB_WARPS) {
     const int gf = T.group_first[g], gl = T.group_last[g];
     const bool mem = lane <= gl - gf;
     const int a = gf + lane;
-    double xa = 0, ya = 0, za = 0, ha = 0;
-    if(mem) {
-      xa = X[a];
-      ya = Y[a];
-      za = dim == 3 ? Z[a] : 0.0;
-      ha = H[a];
-    }
+    int4 qa = make_int4(0, 0, 0, 0);
+    if(mem)
+      qa = K.qpos[a];
+    const float haf = __int_as_float(qa.w);
     int gnode = -1;
     double g2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if(mem && nonuni) {
@@ -650,18 +736,17 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
           g2[k] = gp[k];
       }
     }
-    double lo0 = mem ? xa : 1e308, lo1 = mem ? ya : 1e308, lo2 = mem ? za : 1e308;
-    double hi0 = mem ? xa : -1e308, hi1 = mem ? ya : -1e308,
-           hi2 = mem ? za : -1e308;
-    double hg = ha;
+    int4 glo = mem ? qa : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
+    int4 ghi = mem ? qa : make_int4(-1, -1, -1, 0);
+    float hg = haf;
     for(int o = 16; o; o >>= 1) {
-      lo0 = fmin(lo0, __shfl_xor_sync(FULL, lo0, o));
-      lo1 = fmin(lo1, __shfl_xor_sync(FULL, lo1, o));
-      lo2 = fmin(lo2, __shfl_xor_sync(FULL, lo2, o));
-      hi0 = fmax(hi0, __shfl_xor_sync(FULL, hi0, o));
-      hi1 = fmax(hi1, __shfl_xor_sync(FULL, hi1, o));
-      hi2 = fmax(hi2, __shfl_xor_sync(FULL, hi2, o));
-      hg = fmax(hg, __shfl_xor_sync(FULL, hg, o));
+      glo.x = min(glo.x, __shfl_xor_sync(FULL, glo.x, o));
+      glo.y = min(glo.y, __shfl_xor_sync(FULL, glo.y, o));
+      glo.z = min(glo.z, __shfl_xor_sync(FULL, glo.z, o));
+      ghi.x = max(ghi.x, __shfl_xor_sync(FULL, ghi.x, o));
+      ghi.y = max(ghi.y, __shfl_xor_sync(FULL, ghi.y, o));
+      ghi.z = max(ghi.z, __shfl_xor_sync(FULL, ghi.z, o));
+      hg = fmaxf(hg, __shfl_xor_sync(FULL, hg, o));
     }
     int cnt = 0;
     int sp = 1;
@@ -678,27 +763,16 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
       sp -= k;
       bool acc = false;
       const bool leaf = node < 0;
+      int4 ql = make_int4(0, 0, 0, 0);
       if(act) {
-        double blo0, blo1, blo2, bhi0, bhi1, bhi2, bh;
         if(!leaf) {
-          const double4 * bp = (const double4 *)&T.box[node];
-          double4 q0 = bp[0], q1 = bp[1];
-          blo0 = q0.x; blo1 = q0.y; blo2 = q0.z; bh = q0.w;
-          bhi0 = q1.x; bhi1 = q1.y; bhi2 = q1.z;
+          const int4 lo = T.qbox[2 * node], hi = T.qbox[2 * node + 1];
+          acc = box_near(glo, ghi, hg, lo, hi, __int_as_float(lo.w), qs0, qs1, qs2);
         }
         else {
-          int j = ~node;
-          blo0 = bhi0 = X[j];
-          blo1 = bhi1 = Y[j];
-          blo2 = bhi2 = dim == 3 ? Z[j] : 0.0;
-          bh = H[j];
+          ql = K.qpos[~node];
+          acc = box_near(glo, ghi, hg, ql, ql, __int_as_float(ql.w), qs0, qs1, qs2);
         }
-        double s0 = fmax(0.0, fmax(blo0 - hi0, lo0 - bhi0));
-        double s1 = fmax(0.0, fmax(blo1 - hi1, lo1 - bhi1));
-        double s2 = fmax(0.0, fmax(blo2 - hi2, lo2 - bhi2));
-        double R = fmax(hg, bh);
-        double d2 = s0 * s0 + s1 * s1 + s2 * s2;
-        acc = d2 <= R * R * (1.0 + 1e-10);
       }
       const unsigned bi = __ballot_sync(FULL, acc && !leaf);
       const unsigned bl = __ballot_sync(FULL, acc && leaf);
@@ -715,30 +789,64 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
       }
       sp += npush;
       if(acc && leaf) {
-        int j = ~node;
-        int pos = ncand + __popc(bl & lt);
-        cand[pos] = ((unsigned long long)T.edepth[j] << 32) | (unsigned)j;
+        const int j = ~node;
+        const int pos = ncand + __popc(bl & lt);
+        if(ORDERED)
+          ckey[pos] = ((unsigned long long)T.edepth[j] << 32) | (unsigned)j;
+        else {
+          cq[pos] = ql;
+          cidx[pos] = j;
+        }
       }
       ncand += __popc(bl);
       __syncwarp();
       const bool last = (sp == 0);
-      if(ncand > NB_CAND - 32 || (last && ncand > 0)) {
+      if(ncand > cap - 32 || (last && ncand > 0)) {
         if(!last)
           chunked = true;
-        warp_bitonic(cand, ncand, lane);
-        for(int c = 0; c < ncand; ++c) {
-          const int b = (int)(cand[c] & 0xffffffffu);
-          const double xb = X[b], yb = Y[b], hb = H[b];
-          const double zb = dim == 3 ? Z[b] : 0.0;
-          if(mem) {
-            double dx = xa - xb, dy = ya - yb, dz = za - zb;
-            double d2 = dx * dx + dy * dy;
-            if(dim == 3)
-              d2 = d2 + dz * dz;
-            double r = ha < hb ? hb : ha;
-            if(d2 <= r * r &&
-               (!nonuni || ref_node_tests(T, X, Y, Z, H, dim, b, a, xa, ya, za,
-                             ha, gnode, g2))) {
+        if(ORDERED)
+          warp_bitonic(ckey, ncand, lane);
+        if(mem) {
+          const double xa = X[a], ya = Y[a], za = dim == 3 ? Z[a] : 0.0, ha = H[a];
+          for(int c = 0; c < ncand; ++c) {
+            int b;
+            int4 qb;
+            if(ORDERED) {
+              b = (int)(ckey[c] & 0xffffffffu);
+              qb = K.qpos[b];
+            }
+            else {
+              b = cidx[c];
+              qb = cq[c];
+            }
+            // FP32 estimate of d^2 - r^2 from the fixed-point positions,
+            // decided only outside a margin far above its error bound
+            // (~1e-6 r^2 plus the quantisation); inside it the exact FP64
+            // predicate decides.
+            const float fx = (float)(qa.x - qb.x) * qs0;
+            const float fy = (float)(qa.y - qb.y) * qs1;
+            const float fz = (float)(qa.z - qb.z) * qs2;
+            const float d2f = fx * fx + fy * fy + fz * fz;
+            const float rf = fmaxf(haf, __int_as_float(qb.w));
+            const float r2f = rf * rf;
+            const float margin = 1e-5f * r2f + 16.f * rf * qmax;
+            bool in;
+            if(d2f < r2f - margin)
+              in = true;
+            else if(d2f > r2f + margin)
+              in = false;
+            else {
+              const double xb = X[b], yb = Y[b], hb = H[b];
+              const double zb = dim == 3 ? Z[b] : 0.0;
+              double dx = xa - xb, dy = ya - yb, dz = za - zb;
+              double d2 = dx * dx + dy * dy;
+              if(dim == 3)
+                d2 = d2 + dz * dz;
+              double r = ha < hb ? hb : ha;
+              in = d2 <= r * r;
+            }
+            if(in && (!nonuni || ref_node_tests(T, X, Y, Z, H, dim, b, a, xa,
+                                   ya, za, ha, gnode, g2))) {
               if(cnt < maxnb)
                 Ls.idx[list_slot(a, cnt, maxnb)] = b;
               ++cnt;
@@ -757,27 +865,36 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
       }
       Ls.cnt[a] = cnt;
     }
-    if(chunked && lane == 0)
+    if(ORDERED && chunked && lane == 0)
       atomicOr(&st->flags, FLAG_LIST_ORDER_CHUNKED);
   }
 }
 
 cudaError_t launch_neighbors(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, Lists & Ls, DevStatus * st, int nsm,
-  const unsigned long long * rbits) {
-  size_t smem = (size_t)NB_WARPS * NB_CAND * 8 + (size_t)NB_WARPS * NB_STACK * 4;
+  const unsigned long long * rbits, const Packed & K, int ordered) {
+  const size_t smem_o = (size_t)NB_WARPS * NB_CAND_ORDERED * 8 +
+                        (size_t)NB_WARPS * NB_STACK * 4;
+  const size_t smem_u = (size_t)NB_WARPS * NB_CAND * 20 +
+                        (size_t)NB_WARPS * NB_STACK * 4;
   static bool attr_set = false;
   if(!attr_set) {
-    cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      (int)smem);
+    cudaFuncSetAttribute(k_neighbors<true>,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
+    cudaFuncSetAttribute(k_neighbors<false>,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
     attr_set = true;
   }
-  int blocks = nsm * 4;
+  int blocks = nsm * 2;
   int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
   if(blocks > maxb)
     blocks = maxb > 0 ? maxb : 1;
-  k_neighbors<<<blocks, NB_WARPS * 32, smem, L.stream>>>(P, T, Ls, st,
-    pp.dim, rbits);
+  if(ordered)
+    k_neighbors<true><<<blocks, NB_WARPS * 32, smem_o, L.stream>>>(P, T, Ls,
+      st, pp.dim, rbits, K);
+  else
+    k_neighbors<false><<<blocks, NB_WARPS * 32, smem_u, L.stream>>>(P, T, Ls,
+      st, pp.dim, rbits, K);
   *L.counter += 1;
   return cudaGetLastError();
 }
@@ -791,13 +908,13 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
 // or a time-critical loop in which cudaMalloc/cudaFree (which may
 // synchronise the device) are not acceptable.  Its scratch (range words,
 // ping-pong keys and indices, digit histogram) is this file-scope array,
-// sized for FSPH_NOALLOC_SORT_MAX particles: 12,845,312 bytes that every
+// sized for FSPH_NOALLOC_SORT_MAX particles: 12,846,336 bytes that every
 // GPU loading the library holds until the process exits.
 #define FSPH_NOALLOC_SORT_MAX (1 << 20)
 #define NOALLOC_RANGE_BYTES 256
 #define NOALLOC_KEYS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 8)
 #define NOALLOC_VALS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 4)
-#define NOALLOC_HIST_BYTES ((size_t)256 * (FSPH_NOALLOC_SORT_MAX / RS_TILE) * 4)
+#define NOALLOC_HIST_BYTES ((size_t)(256 * (FSPH_NOALLOC_SORT_MAX / RS_TILE) + 256) * 4)
 #define NOALLOC_TOTAL \
   (NOALLOC_RANGE_BYTES + NOALLOC_KEYS_BYTES + NOALLOC_VALS_BYTES + NOALLOC_HIST_BYTES)
 

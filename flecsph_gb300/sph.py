@@ -238,3 +238,8 @@ def measure_peak(kind, device=0):
     if st:
         raise FsphError(st, "measure_peak")
     return v.value
+
+
+def mixed_available():
+    """The mixed-precision pair kernels are part of this build."""
+    return True
