@@ -590,7 +590,8 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   {
     Phase ph(c, FSPH_TIMER_TREE);
     CK(launch_pack_positions(L, c->P, c->pp, c->d_range, c->K));
-    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX, c->d_range, c->K.qpos));
+    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX, c->d_range, c->K.qpos,
+      c->mixed ? 0 : 1));
   }
   {
     // FP64 mode keeps each list in the reference's order so its sums round
@@ -749,7 +750,7 @@ fsph_status fsph_compute_dt(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_DT);
-  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 0));
+  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 0, c->mixed));
   return FSPH_OK;
 }
 
@@ -757,7 +758,7 @@ fsph_status fsph_compute_dt(fsph_ctx * c) {
 static fsph_status checks_and_dt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_DT);
-  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 1));
+  CK(launch_compute_dt(L, c->P, c->pp, c->d_time, c->d_status, 1, c->mixed));
   return FSPH_OK;
 }
 

@@ -167,9 +167,23 @@ cudaError_t launch_elementwise(const Launch & L, const Particles & P,
 // compute_dt (default_physics.h:602-695) per particle, then the minimum.
 __global__ void k_dt_init(DevTime * t) { t->dtmin_bits = ord_enc_e(1e24); }
 
+// NaN / negativity from the bit pattern: integer instructions instead of
+// FP64 compares, which run on this part's narrow FP64 pipe.
+__device__ __forceinline__ bool bits_nan(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) >
+         0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool bits_negative(double x) {  // x < 0, not -0, not NaN
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) && (b & 0x7fffffffffffffffull) != 0 &&
+         (b & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;
+}
+
 // CHECKS folds check_nans and check_negativity (default_physics.h:918-979)
 // into the same pass, as the driver runs them back to back before dt.
-template<int D, bool CHECKS>
+// F32 evaluates the per-particle estimate of compute_dt in single precision
+// (mixed-precision runs); the global minimum and the adaptive rule stay FP64.
+template<int D, bool CHECKS, bool F32>
 __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
   PhysParams pp, DevTime * tm, DevStatus * st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -178,38 +192,54 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
     double ** f = P.f;
     if(CHECKS) {
       bool bad = false;
-      for(int d = 0; d < D; ++d) {
-        double q[5] = {f[F_X + d][i], f[F_VX + d][i], f[F_VHX + d][i],
-          f[F_AX + d][i], f[F_GAX + d][i]};
-        for(int k = 0; k < 5; ++k)
-          bad |= q[k] != q[k];
-      }
+      for(int d = 0; d < D; ++d)
+        bad |= bits_nan(f[F_X + d][i]) | bits_nan(f[F_VX + d][i]) |
+               bits_nan(f[F_VHX + d][i]) | bits_nan(f[F_AX + d][i]) |
+               bits_nan(f[F_GAX + d][i]);
       const int sc[] = {F_M, F_GPOT, F_RHO, F_P, F_E, F_DEDT, F_DUDT, F_K, F_VSIG};
       for(int k = 0; k < 9; ++k)
-        bad |= f[sc[k]][i] != f[sc[k]][i];
+        bad |= bits_nan(f[sc[k]][i]);
       if(pp.evolve_u)
-        bad |= f[F_U][i] != f[F_U][i];
+        bad |= bits_nan(f[F_U][i]);
       if(bad)
         raise_status(st, FSPH_ERR_NAN, i);
-      if(f[F_RHO][i] < 0 || f[F_P][i] < 0 || (pp.evolve_u && f[F_U][i] < 0))
+      if(bits_negative(f[F_RHO][i]) || bits_negative(f[F_P][i]) ||
+         (pp.evolve_u && bits_negative(f[F_U][i])))
         raise_status(st, FSPH_ERR_NEGATIVITY, i);
     }
-    const double tiny = 1e-24, mc = 0.6;
-    const double dx = f[F_H][i] / (pp.eta * pp.kw);
-    double vn = 0;
-    for(int d = 0; d < D; ++d)
-      vn += f[F_VX + d][i] * f[F_VX + d][i];
-    vn = sqrt(vn);
-    const double dt_v = dx / (vn + tiny);
-    double acc = 0;
-    for(int d = 0; d < D; ++d) {
-      double ad = f[F_AX + d][i] + f[F_GAX + d][i];
-      acc += ad * ad;
+    if(F32) {
+      const float tiny = 1e-24f;
+      const float dx = (float)f[F_H][i] / (float)(pp.eta * pp.kw);
+      float vn = 0.f, acc = 0.f;
+      for(int d = 0; d < D; ++d) {
+        const float v = (float)f[F_VX + d][i];
+        const float a = (float)(f[F_AX + d][i] + f[F_GAX + d][i]);
+        vn += v * v;
+        acc += a * a;
+      }
+      const float dt_v = dx / (sqrtf(vn) + tiny);
+      const float dt_a = sqrtf(dx / (sqrtf(acc) + tiny));
+      const float dt_c = dx / (tiny + (float)f[F_VSIG][i] * (1.f + 0.6f * (float)pp.alpha));
+      dtmin = (double)((float)pp.cfl * fminf(fminf(dt_v, dt_a), dt_c));
     }
-    acc = sqrt(acc);
-    const double dt_a = sqrt(dx / (acc + tiny));
-    const double dt_c = dx / (tiny + f[F_VSIG][i] * (1 + mc * pp.alpha));
-    dtmin = pp.cfl * dmin_(dmin_(dt_v, dt_a), dt_c);
+    else {
+      const double tiny = 1e-24, mc = 0.6;
+      const double dx = f[F_H][i] / (pp.eta * pp.kw);
+      double vn = 0;
+      for(int d = 0; d < D; ++d)
+        vn += f[F_VX + d][i] * f[F_VX + d][i];
+      vn = sqrt(vn);
+      const double dt_v = dx / (vn + tiny);
+      double acc = 0;
+      for(int d = 0; d < D; ++d) {
+        double ad = f[F_AX + d][i] + f[F_GAX + d][i];
+        acc += ad * ad;
+      }
+      acc = sqrt(acc);
+      const double dt_a = sqrt(dx / (acc + tiny));
+      const double dt_c = dx / (tiny + f[F_VSIG][i] * (1 + mc * pp.alpha));
+      dtmin = pp.cfl * dmin_(dmin_(dt_v, dt_a), dt_c);
+    }
     if(pp.evolve_u && pp.thermokinetic) {
       const double eint = f[F_U][i];
       if(!(eint > 0))
@@ -217,41 +247,52 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
       double gdv = 0;
       for(int d = 0; d < D; ++d)
         gdv += f[F_VX + d][i] * f[F_GAX + d][i];
-      int it;
-      for(it = 0; it < 20; ++it) {
-        double delta_epot = 0.0 - 0.0;
-        double delta_egrv = -dtmin * gdv;
-        if(delta_epot + delta_egrv < eint * 0.5)
-          break;
-        dtmin *= 0.25;
+      if(gdv != 0.0) {  // -dtmin * 0 < eint/2 holds at once
+        int it;
+        for(it = 0; it < 20; ++it) {
+          double delta_epot = 0.0 - 0.0;
+          double delta_egrv = -dtmin * gdv;
+          if(delta_epot + delta_egrv < eint * 0.5)
+            break;
+          dtmin *= 0.25;
+        }
+        if(it >= 20)
+          raise_status(st, FSPH_ERR_DT, i);
       }
-      if(it >= 20)
-        raise_status(st, FSPH_ERR_DT, i);
     }
     f[F_DT][i] = dtmin;
   }
+  // block minimum first, then one atomic per block
+  __shared__ double wmin[ELEM_THREADS / 32];
   for(int o = 16; o; o >>= 1)
     dtmin = dmin_(dtmin, __shfl_xor_sync(0xffffffffu, dtmin, o));
   if((threadIdx.x & 31) == 0)
-    atomicMin(&tm->dtmin_bits, ord_enc_e(dtmin));
+    wmin[threadIdx.x >> 5] = dtmin;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    double m = wmin[0];
+    for(int k = 1; k < ELEM_THREADS / 32; ++k)
+      m = dmin_(m, wmin[k]);
+    atomicMin(&tm->dtmin_bits, ord_enc_e(m));
+  }
 }
 
 cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
-  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks) {
+  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks,
+  int f32) {
   k_dt_init<<<1, 1, 0, L.stream>>>(t);
   const int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
+#define DT_LAUNCH(D, C, F) \
+  k_compute_dt<D, C, F><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st)
   if(pp.dim == 3) {
-    if(with_checks)
-      k_compute_dt<3, true><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
-    else
-      k_compute_dt<3, false><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+    if(with_checks) { if(f32) DT_LAUNCH(3, true, true); else DT_LAUNCH(3, true, false); }
+    else { if(f32) DT_LAUNCH(3, false, true); else DT_LAUNCH(3, false, false); }
   }
   else {
-    if(with_checks)
-      k_compute_dt<2, true><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
-    else
-      k_compute_dt<2, false><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st);
+    if(with_checks) { if(f32) DT_LAUNCH(2, true, true); else DT_LAUNCH(2, true, false); }
+    else { if(f32) DT_LAUNCH(2, false, true); else DT_LAUNCH(2, false, false); }
   }
+#undef DT_LAUNCH
   *L.counter += 2;
   return cudaGetLastError();
 }

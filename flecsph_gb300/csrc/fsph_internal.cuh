@@ -121,7 +121,7 @@ cudaError_t launch_permute(const Launch & L, const Particles & src,
 struct Packed;
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,
-  const unsigned long long * rbits, const int4 * qpos);
+  const unsigned long long * rbits, const int4 * qpos, int ordered);
 cudaError_t launch_neighbors(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, Lists & Ls, DevStatus * st, int nsm,
   const unsigned long long * rbits, const Packed & K, int ordered);
@@ -164,7 +164,8 @@ enum ElemOp {
 cudaError_t launch_elementwise(const Launch & L, const Particles & P,
   const PhysParams & pp, int op, DevTime * t, DevStatus * st);
 cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
-  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks);
+  const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks,
+  int f32);
 cudaError_t launch_set_adaptive_timestep(const Launch & L,
   const PhysParams & pp, DevTime * t);
 cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,

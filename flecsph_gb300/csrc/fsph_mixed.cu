@@ -9,10 +9,11 @@
 //
 // Formulas are those of the reference (default_physics.h:193-566,
 // kernels.h, viscosity.h:81-137); algebraic rewrites only (grad W / r
-// folded into one factor), and the self pair / coincident pairs are
-// skipped explicitly where the reference zeroes them (m_b = 0 when
-// x_b == x_a, :378,456,534) or drops a NaN (signal speed, :254-262), since
-// FP32 has no equivalent of the reference's TINY guards.
+// folded into one factor, which stays finite at r = 0).  The self pair and
+// coincident pairs contribute exactly zero to forces and energies (x_ab = 0
+// and mu = 0), as the reference's m_b = 0 makes them (:378,456,534), and
+// are masked out of the signal speed, where the reference drops a NaN
+// (:254-262): FP32 has no equivalent of the reference's TINY guards.
 #include <cuda_runtime.h>
 
 #include "fsph_internal.cuh"
@@ -47,8 +48,10 @@ __global__ void k_pack_pos(Particles P, int dim,
     return;
   int q[3] = {0, 0, 0};
   for(int d = 0; d < dim; ++d) {
+    // any monotone mapping shared by all particles will do: multiply by the
+    // reciprocal instead of dividing (FP64 division is costly on this part)
     double lo = ord_dec_m(rbits[d]), hi = ord_dec_m(rbits[3 + d]);
-    double t = (P.f[F_X + d][i] - lo) / (hi - lo) * 2147483648.0;
+    double t = (P.f[F_X + d][i] - lo) * (2147483648.0 / (hi - lo));
     t = fmin(fmax(t, 0.0), 2147483647.0);
     q[d] = __double2int_rn(t);
   }
@@ -179,14 +182,16 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
   const int4 qa = Kp.qpos[a];
   const float ha = __int_as_float(qa.w);
   const int cnt = Ls.cnt[a];
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   float sum = 0.f, comp = 0.f;
+#pragma unroll 4
   for(int j = 0; j < cnt; ++j) {
-    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
+    const int b = lp[32 * j];
     const int4 qb = Kp.qpos[b];
     const float mb = Kp.vhm[b].w;
     const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
     const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = __frcp_rn(hab);
+    const float ih = 1.0f / hab;
     kahan(sum, comp, mb * wfun<D, K>(sqrtf(g.r2), hab, ih));
   }
   const double rho = (double)sum - (double)comp;
@@ -239,21 +244,20 @@ __global__ void __launch_bounds__(MIX_THREADS) k_vsig_mixed(Particles P,
   const float4 va = Kp.vel[a];
   const float ca = Kp.thermo[a].z;
   const int cnt = Ls.cnt[a];
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   float vsig = 0.f;
+#pragma unroll 4
   for(int j = 0; j < cnt; ++j) {
-    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
-    if(b == a)
-      continue;
+    const int b = lp[32 * j];
     const PairGeom g = geom<D>(qa, Kp.qpos[b], s0, s1, s2);
-    if(g.r2 == 0.f)
-      continue;
-    const float rinv = rsqrtf(g.r2);
     const float4 vb = Kp.vel[b];
-    const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
-                         (va.z - vb.z) * g.dz) * rinv;
     const float4 tb = Kp.thermo[b];
+    const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
+                         (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
     const float cb = b > a ? tb.z : tb.w;
-    vsig = fmaxf(vsig, fmaxf(ca, cb) - fminf(dotv, 0.f));
+    // the self pair and coincident pairs are NaN in the reference and drop out
+    const float cand = fmaxf(ca, cb) - fminf(dotv, 0.f);
+    vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
   }
   P.f[F_VSIG][a] = (double)vsig;
 }
@@ -281,16 +285,16 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
   if(VSIG)
     va = Kp.vel[a];
   float vsig = 0.f;
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  // The self pair and coincident pairs add exactly zero (x_ab = 0, mu = 0),
+  // as the reference's m_b = 0 makes them; the loop needs no branch.
+#pragma unroll 2
   for(int j = 0; j < cnt; ++j) {
-    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
-    if(b == a)
-      continue;
+    const int b = lp[32 * j];
     const int4 qb = Kp.qpos[b];
     const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    if(g.r2 == 0.f)
-      continue;
     const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = __frcp_rn(hab);
+    const float ih = 1.0f / hab;
     const float r = sqrtf(g.r2);
     const float f = gfac<D, K>(r, hab, ih);
     const float4 vhb = Kp.vhm[b];
@@ -307,7 +311,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
       const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
                            (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
       const float cb = b > a ? tb.z : tb.w;
-      vsig = fmaxf(vsig, fmaxf(ta.z, cb) - fminf(dotv, 0.f));
+      const float cand = fmaxf(ta.z, cb) - fminf(dotv, 0.f);
+      vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
     }
     kahan(ax, cx, g.dx * sc);
     kahan(ay, cy, g.dy * sc);
@@ -348,16 +353,14 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
   const float4 ta = Kp.thermo[a];
   const int cnt = Ls.cnt[a];
   float dp = 0.f, cp = 0.f, dv = 0.f, cv = 0.f;
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+#pragma unroll 2
   for(int j = 0; j < cnt; ++j) {
-    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
-    if(b == a)
-      continue;
+    const int b = lp[32 * j];
     const int4 qb = Kp.qpos[b];
     const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    if(g.r2 == 0.f)
-      continue;
     const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = __frcp_rn(hab);
+    const float ih = 1.0f / hab;
     const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
     const float4 vhb = Kp.vhm[b];
     const float4 vb = Kp.vel[b];
@@ -394,16 +397,14 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
   const float4 ta = Kp.thermo[a];
   const int cnt = Ls.cnt[a];
   float sum = 0.f, comp = 0.f;
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+#pragma unroll 2
   for(int j = 0; j < cnt; ++j) {
-    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
-    if(b == a)
-      continue;
+    const int b = lp[32 * j];
     const int4 qb = Kp.qpos[b];
     const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    if(g.r2 == 0.f)
-      continue;
     const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = __frcp_rn(hab);
+    const float ih = 1.0f / hab;
     const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
     const float4 vhb = Kp.vhm[b];
     const float4 vb = Kp.vel[b];

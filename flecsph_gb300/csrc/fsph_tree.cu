@@ -50,7 +50,8 @@ __global__ void k_range_init(Particles P, int dim, unsigned long long * bits) {
   }
 }
 
-__global__ void k_range_reduce(Particles P, int dim, unsigned long long * bits) {
+__global__ void __launch_bounds__(256) k_range_reduce(Particles P, int dim,
+  unsigned long long * bits) {
   double lo[3] = {1e308, 1e308, 1e308}, hi[3] = {-1e308, -1e308, -1e308};
   double hmn = 1e308, hmx = -1e308;
   const double * H = P.f[F_H];
@@ -66,25 +67,32 @@ __global__ void k_range_reduce(Particles P, int dim, unsigned long long * bits) 
       lo[d] = b < lo[d] ? b : lo[d];
     }
   }
-  for(int d = 0; d < dim; ++d) {
-    for(int o = 16; o; o >>= 1) {
-      double l2 = __shfl_xor_sync(FULL, lo[d], o);
-      double h2 = __shfl_xor_sync(FULL, hi[d], o);
-      lo[d] = l2 < lo[d] ? l2 : lo[d];
-      hi[d] = h2 > hi[d] ? h2 : hi[d];
+  // warp, then block, then one atomic per block and quantity
+  __shared__ double red[8][8];
+  double v[8] = {lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2], hmn, -hmx};
+  for(int k = 0; k < 8; ++k)
+    for(int o = 16; o; o >>= 1)
+      v[k] = fmin(v[k], __shfl_xor_sync(FULL, v[k], o));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if(lane == 0)
+    for(int k = 0; k < 8; ++k)
+      red[w][k] = v[k];
+  __syncthreads();
+  if(threadIdx.x < 8) {
+    const int k = threadIdx.x;
+    double m = red[0][k];
+    for(int q = 1; q < (int)(blockDim.x >> 5); ++q)
+      m = fmin(m, red[q][k]);
+    if(k < 3) {
+      if(k < dim) atomicMin(&bits[k], ord_enc(m));
     }
-    if((threadIdx.x & 31) == 0) {
-      atomicMin(&bits[d], ord_enc(lo[d]));
-      atomicMax(&bits[3 + d], ord_enc(hi[d]));
+    else if(k < 6) {
+      if(k - 3 < dim) atomicMax(&bits[k], ord_enc(-m));
     }
-  }
-  for(int o = 16; o; o >>= 1) {
-    hmn = fmin(hmn, __shfl_xor_sync(FULL, hmn, o));
-    hmx = fmax(hmx, __shfl_xor_sync(FULL, hmx, o));
-  }
-  if((threadIdx.x & 31) == 0) {
-    atomicMin(&bits[6], ord_enc(hmn));
-    atomicMax(&bits[7], ord_enc(hmx));
+    else if(k == 6)
+      atomicMin(&bits[6], ord_enc(m));
+    else
+      atomicMax(&bits[7], ord_enc(-m));
   }
 }
 
@@ -120,10 +128,18 @@ __global__ void k_keys(Particles P, int dim, const unsigned long long * bits,
   const double mult = (double)(1ull << md);
   unsigned long long c[3] = {0, 0, 0};
   for(int d = 0; d < dim; ++d) {
-    double mn = ord_dec(bits[d]);
-    double mx = ord_dec(bits[3 + d]);
-    double scale = mx - mn;
-    double q = (P.f[F_X + d][i] - mn) / scale * mult;
+    const double mn = ord_dec(bits[d]);
+    const double mx = ord_dec(bits[3 + d]);
+    const double scale = mx - mn;
+    const double t = P.f[F_X + d][i] - mn;
+    // The reference quantises fl(t / scale) * 2^md (a power of two, exact).
+    // t * (1 / scale) can differ from fl(t / scale) by an ulp, which moves
+    // the integer part only when the scaled value lies within ~7e-7 of an
+    // integer (2D: 2^31 scale); there the correctly rounded division decides.
+    double q = t * (1.0 / scale) * mult;
+    const double fq = floor(q);
+    if(q - fq < 1e-5 || q - fq > 1.0 - 1e-5)
+      q = t / scale * mult;
     unsigned long long u = q > 0.0 ? __double2ull_rz(q) : 0ull;
     c[d] = u < maxv ? u : maxv;
   }
@@ -472,8 +488,13 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
         }
       }
     }
+    // children of a radix-tree node are always (split, split + 1): store
+    // split and the two leaf flags with the box, so the walk needs one load
+    const int l = T.left[p], r = T.right[p];
+    const int split = l < 0 ? ~l : l;
+    const int code = (split << 2) | ((l < 0) << 1) | (r < 0);
     T.qbox[2 * p] = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
-    T.qbox[2 * p + 1] = make_int4(hi[0], hi[1], hi[2], 0);
+    T.qbox[2 * p + 1] = make_int4(hi[0], hi[1], hi[2], code);
     if(nonuni) {
       if(dim == 2)
         n2.lo[2] = n2.hi[2] = 0;
@@ -517,9 +538,9 @@ __device__ __forceinline__ int node_level(const unsigned long long * K,
 // first octree ancestor holding more than 128 particles
 // (tree_topology.h:220-235, sub_entities_ = 128 at :2121).
 __global__ void k_refgroups(const unsigned long long * K, int n, int dim,
-  Tree T) {
+  Tree T, const unsigned long long * rbits) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= n)
+  if(i >= n || rbits[6] == rbits[7])  // only read when h varies
     return;
   const int lead = 64 - (63 / dim) * dim;
   int p = T.leaf_parent[i];
@@ -545,15 +566,16 @@ __global__ void k_refgroups(const unsigned long long * K, int n, int dim,
 
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,
-  const unsigned long long * rbits, const int4 * qpos) {
+  const unsigned long long * rbits, const int4 * qpos, int ordered) {
   const int n = P.n;
   cudaMemsetAsync(T.counter, 0, sizeof(unsigned) * (size_t)n, L.stream);
   cudaMemsetAsync(T.ngroups, 0, sizeof(int), L.stream);
   k_karras<<<(n + 254) / 256, 256, 0, L.stream>>>(P.key, n, T);
-  k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
+  if(ordered)  // reference octree depths order the FP64 lists
+    k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
   k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits);
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max);
-  k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T);
+  k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits);
   *L.counter += 5;
   return cudaGetLastError();
 }
@@ -570,10 +592,17 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 //     (dx*dx + dy*dy) + dz*dz <= max(h_a, h_b)^2   in FP64, no FMA.
 // The candidate order makes each list come out in the order in which the
 // reference's breadth-first walk appends neighbours (by depth, then key).
+#ifndef NB_WARPS
 #define NB_WARPS 8
+#endif
 #define NB_STACK 1024
 #define NB_CAND_ORDERED 2048
+#ifndef NB_CAND
 #define NB_CAND 512
+#endif
+#ifndef NB_BLOCKS_PER_SM
+#define NB_BLOCKS_PER_SM 2
+#endif
 
 __device__ __forceinline__ void warp_bitonic(unsigned long long * a, int m,
   int lane) {
@@ -695,7 +724,10 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cap = ORDERED ? NB_CAND_ORDERED : NB_CAND;
   unsigned long long * ckey = nullptr;
-  int4 * cq = nullptr;
+  float * cxs = nullptr;  // candidates as SoA: minus their position relative
+  float * cys = nullptr;  // to the group box corner, h and particle index,
+  float * czs = nullptr;  // so the filter reads consecutive pairs as float2
+  float * chs = nullptr;
   int * cidx = nullptr;
   int * stack;
   if(ORDERED) {
@@ -703,8 +735,12 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
     stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND_ORDERED * 8) + w * NB_STACK;
   }
   else {
-    cq = (int4 *)smem + (size_t)w * NB_CAND;
-    cidx = (int *)(smem + (size_t)NB_WARPS * NB_CAND * 16) + w * NB_CAND;
+    float * base = (float *)smem + (size_t)w * 5 * NB_CAND;
+    cxs = base;
+    cys = base + NB_CAND;
+    czs = base + 2 * NB_CAND;
+    chs = base + 3 * NB_CAND;
+    cidx = (int *)(base + 4 * NB_CAND);
     stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND * 20) + w * NB_STACK;
   }
   const unsigned lt = lanemask_lt();
@@ -717,6 +753,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
   const bool nonuni = rbits[6] != rbits[7];
   const float qs0 = K.qscale[0], qs1 = K.qscale[1], qs2 = dim == 3 ? K.qscale[2] : 0.f;
   const float qmax = fmaxf(qs0, fmaxf(qs1, qs2));
+  const float hglob = (float)ord_dec(rbits[7]);
   for(int g = blockIdx.x * NB_WARPS + w; g < ngroups;
       g += gridDim.x * NB_WARPS) {
     const int gf = T.group_first[g], gl = T.group_last[g];
@@ -764,9 +801,11 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
       bool acc = false;
       const bool leaf = node < 0;
       int4 ql = make_int4(0, 0, 0, 0);
+      int code = 0;
       if(act) {
         if(!leaf) {
           const int4 lo = T.qbox[2 * node], hi = T.qbox[2 * node + 1];
+          code = hi.w;
           acc = box_near(glo, ghi, hg, lo, hi, __int_as_float(lo.w), qs0, qs1, qs2);
         }
         else {
@@ -783,9 +822,10 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         break;
       }
       if(acc && !leaf) {
-        int pos = sp + 2 * __popc(bi & lt);
-        stack[pos] = T.right[node];
-        stack[pos + 1] = T.left[node];
+        const int pos = sp + 2 * __popc(bi & lt);
+        const int split = code >> 2;
+        stack[pos] = (code & 1) ? ~(split + 1) : split + 1;
+        stack[pos + 1] = (code & 2) ? ~split : split;
       }
       sp += npush;
       if(acc && leaf) {
@@ -794,62 +834,150 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         if(ORDERED)
           ckey[pos] = ((unsigned long long)T.edepth[j] << 32) | (unsigned)j;
         else {
-          cq[pos] = ql;
+          // minus the position relative to the group box corner, in FP32
+          cxs[pos] = -((float)(ql.x - glo.x) * qs0);
+          cys[pos] = -((float)(ql.y - glo.y) * qs1);
+          czs[pos] = -((float)(ql.z - glo.z) * qs2);
+          chs[pos] = __int_as_float(ql.w);
           cidx[pos] = j;
         }
       }
       ncand += __popc(bl);
       __syncwarp();
       const bool last = (sp == 0);
-      if(ncand > cap - 32 || (last && ncand > 0)) {
+      if(ncand > cap - 33 || (last && ncand > 0)) {
         if(!last)
           chunked = true;
         if(ORDERED)
           warp_bitonic(ckey, ncand, lane);
+        if(!ORDERED && (ncand & 1)) {
+          // pad to an even count with a candidate that can never pass
+          if(lane == 0) {
+            cxs[ncand] = 1e30f;
+            cys[ncand] = 1e30f;
+            czs[ncand] = 1e30f;
+            chs[ncand] = 0.f;
+            cidx[ncand] = -1;
+          }
+          __syncwarp();
+        }
         if(mem) {
           const double xa = X[a], ya = Y[a], za = dim == 3 ? Z[a] : 0.0, ha = H[a];
-          for(int c = 0; c < ncand; ++c) {
-            int b;
-            int4 qb;
-            if(ORDERED) {
-              b = (int)(ckey[c] & 0xffffffffu);
-              qb = K.qpos[b];
-            }
-            else {
-              b = cidx[c];
-              qb = cq[c];
-            }
-            // FP32 estimate of d^2 - r^2 from the fixed-point positions,
-            // decided only outside a margin far above its error bound
-            // (~1e-6 r^2 plus the quantisation); inside it the exact FP64
-            // predicate decides.
-            const float fx = (float)(qa.x - qb.x) * qs0;
-            const float fy = (float)(qa.y - qb.y) * qs1;
-            const float fz = (float)(qa.z - qb.z) * qs2;
-            const float d2f = fx * fx + fy * fy + fz * fz;
-            const float rf = fmaxf(haf, __int_as_float(qb.w));
-            const float r2f = rf * rf;
-            const float margin = 1e-5f * r2f + 16.f * rf * qmax;
-            bool in;
-            if(d2f < r2f - margin)
-              in = true;
-            else if(d2f > r2f + margin)
-              in = false;
-            else {
-              const double xb = X[b], yb = Y[b], hb = H[b];
-              const double zb = dim == 3 ? Z[b] : 0.0;
-              double dx = xa - xb, dy = ya - yb, dz = za - zb;
-              double d2 = dx * dx + dy * dy;
-              if(dim == 3)
-                d2 = d2 + dz * dz;
-              double r = ha < hb ? hb : ha;
-              in = d2 <= r * r;
-            }
-            if(in && (!nonuni || ref_node_tests(T, X, Y, Z, H, dim, b, a, xa,
-                                   ya, za, ha, gnode, g2))) {
+          int * out = Ls.idx + list_slot(a, 0, maxnb);
+          // this member relative to the same corner
+          const float ax = (float)(qa.x - glo.x) * qs0;
+          const float ay = (float)(qa.y - glo.y) * qs1;
+          const float az = (float)(qa.z - glo.z) * qs2;
+          // largest extent of the group box: with the walk radius it bounds
+          // the magnitude of every relative coordinate below
+          const float lg = fmaxf((float)(ghi.x - glo.x) * qs0,
+            fmaxf((float)(ghi.y - glo.y) * qs1, (float)(ghi.z - glo.z) * qs2));
+          // The FP32 estimate t = d^2 - r^2 decides a pair only when |t|
+          // exceeds a margin well above its error bound: fixed-point
+          // quantisation (one step per axis), two roundings of each relative
+          // coordinate (|value| <= lg + max h, as the walk accepted the
+          // candidate), the squares and the sum (~2e-6 r^2).  Inside the
+          // margin the exact FP64 predicate decides.
+          const float kq = 16.f * qmax + 4e-6f * (lg + fmaxf(hg, hglob));
+          auto decide = [&](float t, float mg, int b) -> bool {
+            if(fabsf(t) > mg)
+              return t < 0.f;
+            const double xb = X[b], yb = Y[b], hbd = H[b];
+            const double zb = dim == 3 ? Z[b] : 0.0;
+            double dx = xa - xb, dy = ya - yb, dz = za - zb;
+            double d2 = dx * dx + dy * dy;
+            if(dim == 3)
+              d2 = d2 + dz * dz;
+            double r = ha < hbd ? hbd : ha;
+            return d2 <= r * r;
+          };
+          auto append = [&](int b) {
+            if(!nonuni || ref_node_tests(T, X, Y, Z, H, dim, b, a, xa, ya, za,
+                            ha, gnode, g2)) {
               if(cnt < maxnb)
-                Ls.idx[list_slot(a, cnt, maxnb)] = b;
+                out[32 * cnt] = b;
               ++cnt;
+            }
+          };
+          if(ORDERED) {
+            for(int c = 0; c < ncand; ++c) {
+              const int b = (int)(ckey[c] & 0xffffffffu);
+              const int4 qb = K.qpos[b];
+              const float fx = (float)(qa.x - qb.x) * qs0;
+              const float fy = (float)(qa.y - qb.y) * qs1;
+              const float fz = (float)(qa.z - qb.z) * qs2;
+              const float d2f = fx * fx + fy * fy + fz * fz;
+              const float rf = fmaxf(haf, __int_as_float(qb.w));
+              const float t = d2f - rf * rf;
+              const float mg = rf * (4e-5f * rf + kq);
+              if(decide(t, mg, b))
+                append(b);
+            }
+          }
+          else if(!nonuni) {
+            // every h is equal: r and the margin are constants of the group
+            // and the predicate alone decides (the reference's node tests
+            // cannot fail, ref_node_tests)
+            const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay);
+            const float2 az2 = make_float2(az, az);
+            const float r2 = haf * haf;
+            const float2 nr2 = make_float2(-r2, -r2);
+            const float mg = haf * (4e-5f * haf + kq);
+            for(int c = 0; c < ncand; c += 2) {
+              const float2 nx = *(const float2 *)&cxs[c];
+              const float2 ny = *(const float2 *)&cys[c];
+              const float2 nz = *(const float2 *)&czs[c];
+              const int2 id = *(const int2 *)&cidx[c];
+              const float2 dx = __fadd2_rn(ax2, nx);
+              const float2 dy = __fadd2_rn(ay2, ny);
+              const float2 dz = __fadd2_rn(az2, nz);
+              float2 d2 = __fmul2_rn(dx, dx);
+              d2 = __ffma2_rn(dy, dy, d2);
+              d2 = __ffma2_rn(dz, dz, d2);
+              const float2 t = __fadd2_rn(d2, nr2);
+              bool in0 = t.x < 0.f, in1 = t.y < 0.f;
+              if(fabsf(t.x) <= mg)
+                in0 = decide(t.x, mg, id.x);
+              if(fabsf(t.y) <= mg && id.y >= 0)
+                in1 = decide(t.y, mg, id.y);
+              if(in0) {
+                if(cnt < maxnb)
+                  out[32 * cnt] = id.x;
+                ++cnt;
+              }
+              if(in1) {
+                if(cnt < maxnb)
+                  out[32 * cnt] = id.y;
+                ++cnt;
+              }
+            }
+          }
+          else {
+            // two candidates per iteration with Blackwell's packed FP32x2
+            // arithmetic
+            const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay);
+            const float2 az2 = make_float2(az, az);
+            const float2 eps2 = make_float2(4e-5f, 4e-5f), kq2 = make_float2(kq, kq);
+            for(int c = 0; c < ncand; c += 2) {
+              const float2 nx = *(const float2 *)&cxs[c];
+              const float2 ny = *(const float2 *)&cys[c];
+              const float2 nz = *(const float2 *)&czs[c];
+              const float2 hb = *(const float2 *)&chs[c];
+              const int2 id = *(const int2 *)&cidx[c];
+              const float2 dx = __fadd2_rn(ax2, nx);
+              const float2 dy = __fadd2_rn(ay2, ny);
+              const float2 dz = __fadd2_rn(az2, nz);
+              float2 d2 = __fmul2_rn(dx, dx);
+              d2 = __ffma2_rn(dy, dy, d2);
+              d2 = __ffma2_rn(dz, dz, d2);
+              const float2 rf = make_float2(fmaxf(haf, hb.x), fmaxf(haf, hb.y));
+              const float2 nrf = make_float2(-rf.x, -rf.y);
+              const float2 t = __ffma2_rn(rf, nrf, d2);
+              const float2 mg = __fmul2_rn(rf, __ffma2_rn(rf, eps2, kq2));
+              if(decide(t.x, mg.x, id.x))
+                append(id.x);
+              if(id.y >= 0 && decide(t.y, mg.y, id.y))
+                append(id.y);
             }
           }
         }
@@ -885,7 +1013,7 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
     attr_set = true;
   }
-  int blocks = nsm * 2;
+  int blocks = nsm * (ordered ? 1 : NB_BLOCKS_PER_SM);
   int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
   if(blocks > maxb)
     blocks = maxb > 0 ? maxb : 1;
