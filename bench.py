@@ -35,7 +35,36 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FLOPS = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
+# Algorithmic work per particle and timer phase (include/fsph_work.h): flops
+# per neighbour pair for the pair passes, compulsory HBM bytes for the rest.
+FLOPS_PAIR = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
+HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
+
+
+def work_model(phase, nb, mixed):
+    """(kind, amount per particle) for a timer phase; kind 'flop' or 'byte'."""
+    if phase in FLOPS_PAIR:
+        f = FLOPS_PAIR[phase]
+        if phase == "accel" and mixed:  # the signal speed rides in this pass
+            f += FLOPS_PAIR["vsig"]
+        return "flop", f * nb
+    fields = 8  # bytes per FP64 field
+    bytes_pp = {
+        # read positions + h and the previous order, write keys + indices
+        "range_keys": 4 * fields * 2 + 12,
+        # 8 LSD passes of (key, index): histogram read + scatter read/write,
+        # then one gather of 31 arrays
+        "sort": 8 * 36 + 31 * fields * 2,
+        # packed record + radix tree nodes (children, ranges, boxes)
+        "tree": 64 + 4 * 6 + 64,
+        # packed record read, list of nb ints and the count written
+        "neighbors": 64 + 4 * nb + 4,
+        # elementwise kicks/drift/EOS: ~24 fields read or written twice a step
+        "integrate": 2 * 24 * fields,
+        # checks + dt: ~22 fields read, dt written
+        "dt": 23 * fields,
+    }.get(phase)
+    return ("byte", bytes_pp) if bytes_pp else (None, None)
 
 
 def parse():
@@ -287,24 +316,33 @@ def gpu_arm(args):
     head = results["mixed" if "mixed" in results else "fp64"]
     K = args.steps
     value = world * n * K / (head["ms"] * 1e-3)
-    # dominant kernel and its roofline
+    # dominant kernel and its roofline; every phase's fraction beside it
     t = head["timers"]
-    top = max((k for k in t if t[k][1] > 0), key=lambda k: t[k][0])
+    mixed_run = "mixed" in results
     fp64_peak = sph.measure_peak(0, local)
     fp32_peak = sph.measure_peak(1, local)
-    pk = fp32_peak if "mixed" in results else fp64_peak
-    if top in FLOPS:
-        per_launch_ms = t[top][0] / t[top][1]
-        flops = n * head["nb_mean"] * FLOPS[top]
-        achieved = flops / (per_launch_ms * 1e-3) / 1e12
-        roof = {"bound": "fp32" if "mixed" in results else "fp64", "kernel": top,
-                "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
-                "frac": achieved / pk,
-                "peak_source": "in-repo FMA-chain probe (fsph_measure_peak), measured this run",
-                "traffic": None}
-    else:
-        roof = {"bound": "hbm", "kernel": top, "achieved": None, "peak": 6815.2,
-                "unit": "GB/s", "frac": None, "traffic": None}
+    pk_flop = fp32_peak if mixed_run else fp64_peak
+    per_phase = {}
+    for ph, (ms_tot, calls) in t.items():
+        if not calls:
+            continue
+        kind, amount = work_model(ph, head["nb_mean"], mixed_run)
+        per_launch_s = ms_tot / calls * 1e-3
+        if kind == "flop":
+            ach = n * amount / per_launch_s / 1e12
+            per_phase[ph] = {"bound": "fp32" if mixed_run else "fp64", "achieved": ach,
+                             "peak": pk_flop, "unit": "TFLOP/s", "frac": ach / pk_flop}
+        elif kind == "byte":
+            ach = n * amount / per_launch_s / 1e9
+            per_phase[ph] = {"bound": "hbm", "achieved": ach, "peak": HBM_PEAK,
+                             "unit": "GB/s", "frac": ach / HBM_PEAK}
+    top = max((k for k in t if t[k][1] > 0), key=lambda k: t[k][0])
+    roof = dict(per_phase.get(top, {"bound": "hbm", "achieved": None,
+                                    "peak": HBM_PEAK, "unit": "GB/s", "frac": None}))
+    roof["kernel"] = top
+    roof["traffic"] = None
+    roof["peak_source"] = ("MEASURED_PEAKS.json hbm_gbs" if roof.get("bound") == "hbm" else
+                           "in-repo FMA-chain probe (fsph_measure_peak), measured this run")
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": K, "warmup": args.warmup,
@@ -319,6 +357,7 @@ def gpu_arm(args):
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],
         "roofline": roof,
+        "roofline_all": per_phase,
         "per_kernel_ms_per_step": {k: v[0] / K for k, v in t.items() if v[1]},
     }
     if "fp64" in results:
