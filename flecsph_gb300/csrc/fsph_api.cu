@@ -42,6 +42,9 @@ struct fsph_ctx {
   Lists Ls{};
   Packed K{};
   bool mixed = false;
+  GravNode * gnodes = nullptr;
+  double * gbox = nullptr;
+  unsigned * gcounter = nullptr;
   DevTime * d_time = nullptr;
   DevStatus * d_status = nullptr;
   double * d_cons = nullptr;
@@ -189,6 +192,11 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "periodic boundaries not implemented";
     return false;
   }
+  if(p->enable_fmm && (p->dimension != 3 || p->gravity_order < 1 ||
+                        p->gravity_order > 2 || !(p->fmm_macangle > 0))) {
+    *why = "gravity needs 3D, gravity_order 1 or 2 and fmm_macangle > 0";
+    return false;
+  }
   if(p->max_neighbors < 8 || p->max_neighbors > 4096) {
     *why = "max_neighbors out of [8, 4096]";
     return false;
@@ -330,6 +338,11 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.vel, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.thermo, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
+  if(p->enable_fmm) {
+    ok &= dalloc(c, &c->gnodes, N) == cudaSuccess;
+    ok &= dalloc(c, &c->gbox, 6 * N) == cudaSuccess;
+    ok &= dalloc(c, &c->gcounter, N) == cudaSuccess;
+  }
   c->mixed = p->precision_mode == FSPH_PRECISION_MIXED;
   c->Ls.maxnb = p->max_neighbors;
   ok &= dalloc(c, &c->Ls.idx, Npad * (size_t)p->max_neighbors) == cudaSuccess;
@@ -788,8 +801,18 @@ fsph_status fsph_advance_time(fsph_ctx * c) {
 fsph_status fsph_gravitation(fsph_ctx * c) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
-  c->last_error = "gravity is not available in this build";
-  return FSPH_ERR_ARG;
+  if(!c->gnodes) {
+    c->last_error = "context created without enable_fmm";
+    return FSPH_ERR_STATE;
+  }
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_GRAVITY);
+  CK(launch_gravity(L, c->P, c->pp, c->T, c->gnodes, c->gbox, c->gcounter,
+    c->p.fmm_macangle, c->p.gravity_order, c->mixed ? 1 : 0, c->d_status, c->nsm));
+  return FSPH_OK;
 }
 
 #define TRY(x)                                                                 \
@@ -809,8 +832,7 @@ fsph_status fsph_step(fsph_ctx * c) {
   const fsph_params & p = c->p;
   const bool thermo = p.thermokinetic_formulation;
   const bool evolve = p.evolve_internal_energy;
-  if(p.enable_fmm)
-    return FSPH_ERR_ARG;
+  const bool grav = p.enable_fmm;
   if(c->iteration == p.initial_iteration) {
     TRY(fsph_update_iteration(c));
     TRY(fsph_eos_init(c));
@@ -820,6 +842,12 @@ fsph_status fsph_step(fsph_ctx * c) {
     TRY(density_impl(c, !c->mixed));
     TRY(fsph_save_velocityhalf(c));
     TRY(accel_impl(c, 0, c->mixed));
+    if(grav) {
+      // newtonian/main_driver.cc:137-151: gravity, then total energy again
+      TRY(fsph_gravitation(c));
+      if(thermo)
+        TRY(fsph_set_total_energy(c));
+    }
     if(p.adaptive_timestep) {
       TRY(fsph_compute_dt(c));
       TRY(fsph_set_adaptive_timestep(c));
@@ -842,7 +870,15 @@ fsph_status fsph_step(fsph_ctx * c) {
       FSPH_TIMER_INTEGRATE));
     TRY(fsph_update_iteration(c));
     TRY(density_impl(c, !c->mixed));
-    TRY(accel_impl(c, 1, c->mixed));
+    if(grav) {
+      // newtonian/main_driver.cc:217-227: gravity between the hydro
+      // acceleration and the velocity kick
+      TRY(accel_impl(c, 0, c->mixed));
+      TRY(fsph_gravitation(c));
+      TRY(fsph_leapfrog_kick_v(c));
+    }
+    else
+      TRY(accel_impl(c, 1, c->mixed));
     if(evolve) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         const bool lastp = m == p.pressure_updates_number;

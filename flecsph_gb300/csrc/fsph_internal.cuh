@@ -89,6 +89,16 @@ struct Packed {
   float * qscale;   // device [3]: range extent / 2^31 per axis
 };
 
+// Multipole of a radix-tree node (FP64): mass, centre of mass, traceless
+// quadrupole {xx, yy, zz, xy, xz, yz} about it, bounding radius.
+struct GravNode {
+  double m;
+  double c[3];
+  double q[6];
+  double rmax;
+  double pad;
+};
+
 struct Lists {
   int * idx;   // interleaved: [(i>>5)][slot][i&31]
   int * cnt;
@@ -141,6 +151,12 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
+
+// ---- fsph_gravity.cu ----
+cudaError_t launch_gravity(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Tree & T, GravNode * gn, double * gbox,
+  unsigned * counter, double theta, int order, int mixed, DevStatus * st,
+  int nsm);
 
 // ---- fsph_fp64.cu ----
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
