@@ -29,7 +29,7 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
 TIMER_NAMES = ["range_keys", "sort", "tree", "neighbors", "density", "vsig",
-               "accel", "energy", "integrate", "dt", "gravity"]
+               "accel", "energy", "integrate", "dt", "gravity", "periodic"]
 TIMER_COUNT = 16
 
 

@@ -25,6 +25,7 @@ SOURCES = {
     "fsph_elementwise.cu": ["-fmad=false"],
     "fsph_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "fsph_gravity.cu": [],
+    "fsph_periodic.cu": ["-fmad=false"],
     "fsph_peak.cu": [],
     "fsph_api.cu": [],
 }

@@ -45,6 +45,10 @@ struct fsph_ctx {
   GravNode * gnodes = nullptr;
   double * gbox = nullptr;
   unsigned * gcounter = nullptr;
+  // periodic boundaries: real particles hold ids [0, nreal)
+  bool periodic = false;
+  long long nreal = 0;
+  PeriodicScratch PS{};
   DevTime * d_time = nullptr;
   DevStatus * d_status = nullptr;
   double * d_cons = nullptr;
@@ -188,9 +192,15 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "relaxation_steps must be 0";
     return false;
   }
-  if(p->periodic_boundary_x || p->periodic_boundary_y || p->periodic_boundary_z) {
-    *why = "periodic boundaries not implemented";
-    return false;
+  {
+    const int per[3] = {p->periodic_boundary_x, p->periodic_boundary_y,
+      p->periodic_boundary_z};
+    const double len[3] = {p->box_length, p->box_width, p->box_height};
+    for(int d = 0; d < 3; ++d)
+      if(per[d] && (d >= p->dimension || !(len[d] > 0))) {
+        *why = "a periodic axis needs d < dimension and a positive box size";
+        return false;
+      }
   }
   if(p->enable_fmm && (p->dimension != 3 || p->gravity_order < 1 ||
                         p->gravity_order > 2 || !(p->fmm_macangle > 0))) {
@@ -338,6 +348,16 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.vel, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.thermo, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
+  c->periodic = p->periodic_boundary_x || p->periodic_boundary_y ||
+                p->periodic_boundary_z;
+  if(c->periodic) {
+    ok &= dalloc(c, &c->PS.flag, N) == cudaSuccess;
+    ok &= dalloc(c, &c->PS.pos, N) == cudaSuccess;
+    ok &= dalloc(c, &c->PS.perm, N) == cudaSuccess;
+    ok &= dalloc(c, &c->PS.tiles, (size_t)scan_tiles((int)N) + 1) == cudaSuccess;
+    ok &= dalloc(c, &c->PS.total, 1) == cudaSuccess;
+    ok &= dalloc(c, &c->PS.hbits, 1) == cudaSuccess;
+  }
   if(p->enable_fmm) {
     ok &= dalloc(c, &c->gnodes, N) == cudaSuccess;
     ok &= dalloc(c, &c->gbox, 6 * N) == cudaSuccess;
@@ -394,6 +414,19 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   if(s)
     return s;
   const int n = (int)v->n;
+  if(c->periodic) {
+    // the copies are told apart by id: the real particles must hold 0..n-1
+    std::vector<char> seen((size_t)n, 0);
+    for(int i = 0; i < n; ++i) {
+      const long long id = v->id[i];
+      if(id < 0 || id >= n || seen[(size_t)id]) {
+        c->last_error = "periodic boundaries need the ids 0 .. n-1";
+        return FSPH_ERR_ARG;
+      }
+      seen[(size_t)id] = 1;
+    }
+  }
+  c->nreal = n;
   c->n = n;
   c->P.n = c->Palt.n = n;
   const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
@@ -585,6 +618,25 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   if(s)
     return s;
   Launch L = c->L();
+  if(c->periodic) {
+    // boundary::pboundary_clean + pboundary_generate (bodies_system.h:160-169)
+    Phase ph(c, FSPH_TIMER_PERIODIC);
+    const double len[3] = {c->p.box_length, c->p.box_width, c->p.box_height};
+    const int per[3] = {c->p.periodic_boundary_x, c->p.periodic_boundary_y,
+      c->p.periodic_boundary_z};
+    int ntot = 0;
+    const char * why = nullptr;
+    CK(launch_periodic(L, c->P, c->Palt, c->pp, len, per, c->nreal, (int)c->cap,
+      c->PS, &ntot, &why));
+    if(why) {
+      c->last_error = std::string(why) + ": need " + std::to_string(ntot) +
+                      ", capacity " + std::to_string(c->cap);
+      c->tree_ok = false;
+      c->n = c->P.n;  // the copies of the last iteration are gone
+      return FSPH_ERR_ARG;
+    }
+    c->n = ntot;
+  }
   const int n = c->n;
   {
     Phase ph(c, FSPH_TIMER_RANGE_KEYS);
@@ -944,7 +996,8 @@ fsph_status fsph_conserved_sums(fsph_ctx * c, fsph_conserved * out) {
   if(s)
     return s;
   Launch L = c->L();
-  CK(launch_conserved(L, c->P, c->pp, c->d_cons));
+  CK(launch_conserved(L, c->P, c->pp, c->d_cons,
+    c->periodic ? c->nreal : (long long)INT64_MAX));
   s = fsph_sync(c);
   if(s)
     return s;
@@ -1002,5 +1055,15 @@ fsph_status fsph_timers_reset(fsph_ctx * c) {
 }
 
 int64_t fsph_launch_count(const fsph_ctx * c) { return c ? c->launches : 0; }
+
+fsph_status fsph_particle_count(fsph_ctx * c, int64_t * total, int64_t * real) {
+  if(!c)
+    return FSPH_ERR_ARG;
+  if(total)
+    *total = c->n;
+  if(real)
+    *real = c->uploaded ? c->nreal : 0;
+  return FSPH_OK;
+}
 
 }  // extern "C"

@@ -390,11 +390,13 @@ cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t) {
 // Conserved totals (analysis.h:56-214): mass, energy, momentum (3),
 // angular momentum (3); one block, fixed order (deterministic).
 __global__ void __launch_bounds__(512) k_conserved(Particles P, PhysParams pp,
-  double * out) {
+  double * out, long long nreal) {
   __shared__ double part[8][512];
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int D = pp.dim;
   for(int i = threadIdx.x; i < P.n; i += 512) {
+    if(P.id[i] >= nreal)  // periodic copies (WALL) are not counted
+      continue;
     double m = P.f[F_M][i];
     double x[3] = {P.f[F_X][i], P.f[F_Y][i], D == 3 ? P.f[F_Z][i] : 0.0};
     double v[3] = {P.f[F_VX][i], P.f[F_VY][i], D == 3 ? P.f[F_VZ][i] : 0.0};
@@ -424,8 +426,8 @@ __global__ void __launch_bounds__(512) k_conserved(Particles P, PhysParams pp,
 }
 
 cudaError_t launch_conserved(const Launch & L, const Particles & P,
-  const PhysParams & pp, double * out8) {
-  k_conserved<<<1, 512, 0, L.stream>>>(P, pp, out8);
+  const PhysParams & pp, double * out8, long long nreal) {
+  k_conserved<<<1, 512, 0, L.stream>>>(P, pp, out8, nreal);
   *L.counter += 1;
   return cudaGetLastError();
 }

@@ -158,6 +158,26 @@ cudaError_t launch_gravity(const Launch & L, const Particles & P,
   unsigned * counter, double theta, int order, int mixed, DevStatus * st,
   int nsm);
 
+// ---- fsph_periodic.cu ----
+struct PeriodicScratch {
+  int * flag;     // cap: real flags, then copy counts
+  int * pos;      // cap: exclusive scan
+  int * perm;     // cap: compaction gather
+  int * tiles;    // scan_tiles(cap)
+  int * total;    // 1
+  unsigned long long * hbits;  // 1: max h of the real particles (bits)
+};
+int scan_tiles(int n);
+cudaError_t launch_exclusive_scan(const Launch & L, const int * in, int * out,
+  int n, int * tile_sums, int * total);
+// Drops the copies (ids >= nreal) keeping the order of the rest, teleports
+// and appends the new copies; P.n / Palt.n become the new total (also in
+// *n_out).  If cap is too small nothing is appended and *why says so.
+cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
+  const PhysParams & pp, const double * box_len, const int * periodic,
+  long long nreal, int cap, PeriodicScratch & S, int * n_out,
+  const char ** why);
+
 // ---- fsph_fp64.cu ----
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st);
@@ -188,6 +208,6 @@ cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,
   DevTime * t);
 cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t);
 cudaError_t launch_conserved(const Launch & L, const Particles & P,
-  const PhysParams & pp, double * out8);
+  const PhysParams & pp, double * out8, long long nreal);
 
 }  // namespace fsph

@@ -153,20 +153,21 @@ def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0):
 
 
 def kh3d(n1d=256, gamma=5.0 / 3.0, eta=1.44, amp=0.01, seed=7):
-    """Kelvin-Helmholtz in the periodic unit box, cubic lattice n1d^3.
+    """Kelvin-Helmholtz in the periodic unit box [-0.5, 0.5]^3 (the box the
+    reference's periodic boundaries assume, boundary.h:130-144), cubic
+    lattice n1d^3.
 
-    The band |y| < 0.25 read periodically (y in [0,0.25) or (0.75,1)) has
-    rho = 2, vx = +0.5; elsewhere rho = 1, vx = -0.5; density by particle
-    mass on one lattice; P = 2.5; vy = amp sin(4 pi x).  `seed` is recorded
-    but unused: the perturbation is deterministic.
+    The band |y| < 0.25 has rho = 2, vx = +0.5; elsewhere rho = 1,
+    vx = -0.5; density by particle mass on one lattice; P = 2.5;
+    vy = amp sin(4 pi x).  `seed` is recorded but unused: the perturbation
+    is deterministic.
     """
     dx = 1.0 / n1d
-    pos = _lattice(n1d, n1d, n1d, (0.0, 0.0, 0.0), dx)
+    pos = _lattice(n1d, n1d, n1d, (-0.5, -0.5, -0.5), dx)
     n = len(pos)
     s = new_state(n)
     s["x"][:], s["y"][:], s["z"][:] = pos[:, 0], pos[:, 1], pos[:, 2]
-    y = pos[:, 1]
-    band = (y < 0.25) | (y > 0.75)
+    band = np.abs(pos[:, 1]) < 0.25
     rho = np.where(band, 2.0, 1.0)
     s["m"][:] = rho * dx**3
     s["rho"][:] = rho
@@ -180,7 +181,35 @@ def kh3d(n1d=256, gamma=5.0 / 3.0, eta=1.44, amp=0.01, seed=7):
                              periodic_boundary_x=1, periodic_boundary_y=1,
                              periodic_boundary_z=1, box_length=1.0, box_width=1.0,
                              box_height=1.0, adaptive_timestep=1, initial_dt=1e-6)
-    meta = dict(problem="kh3d", n=n, dx=dx, seed=seed, band="y<0.25 or y>0.75")
+    meta = dict(problem="kh3d", n=n, dx=dx, seed=seed, band="|y| < 0.25",
+                box="[-0.5, 0.5]^3")
+    return s, params, meta
+
+
+def kh2d(n1d=128, gamma=5.0 / 3.0, eta=1.5, amp=0.01):
+    """2D analogue of kh3d on [-0.5, 0.5]^2, periodic in x and y."""
+    dx = 1.0 / n1d
+    ix = (np.arange(n1d) + 0.5) * dx - 0.5
+    Y, X = np.meshgrid(ix, ix, indexing="ij")
+    x, y = X.ravel(), Y.ravel()
+    n = len(x)
+    s = new_state(n)
+    s["x"][:], s["y"][:] = x, y
+    band = np.abs(y) < 0.25
+    rho = np.where(band, 2.0, 1.0)
+    s["m"][:] = rho * dx**2
+    s["rho"][:] = rho
+    s["P"][:] = 2.5
+    s["u"][:] = 2.5 / ((gamma - 1.0) * rho)
+    s["vx"][:] = np.where(band, 0.5, -0.5)
+    s["vy"][:] = amp * np.sin(4.0 * np.pi * x)
+    s["h"][:] = eta * KERNEL_WIDTH * dx
+    params = Params.defaults(dimension=2, sph_kernel=KERNEL_WENDLAND_C6,
+                             eos_type=EOS_IDEAL, poly_gamma=gamma, sph_eta=eta,
+                             periodic_boundary_x=1, periodic_boundary_y=1,
+                             box_length=1.0, box_width=1.0, adaptive_timestep=1,
+                             initial_dt=1e-6)
+    meta = dict(problem="kh2d", n=n, dx=dx, band="|y| < 0.25", box="[-0.5, 0.5]^2")
     return s, params, meta
 
 

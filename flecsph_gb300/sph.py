@@ -71,6 +71,8 @@ def library():
     lib.fsph_timers.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
     lib.fsph_launch_count.argtypes = [C.c_void_p]
     lib.fsph_launch_count.restype = C.c_int64
+    lib.fsph_particle_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)]
     lib.fsph_upload_fields.argtypes = [C.c_void_p, C.POINTER(SoAView)]
     lib.fsph_host_register.argtypes = [C.c_void_p, C.c_int64]
     lib.fsph_host_unregister.argtypes = [C.c_void_p]
@@ -93,7 +95,6 @@ class BodySystem:
         if not self.ctx:
             raise FsphError(st.value, "fsph_create")
         self.lib = lib
-        self.n = 0
         self.capacity = capacity
 
     def close(self):
@@ -129,11 +130,22 @@ class BodySystem:
         raise AttributeError(name)
 
     # -- data movement ---------------------------------------------------
+    @property
+    def n(self):
+        """Particles held, periodic copies included (what download returns)."""
+        return self.count()[0]
+
+    def count(self):
+        """(total, real): total includes the periodic copies."""
+        t, r = C.c_int64(), C.c_int64()
+        self._check(self.lib.fsph_particle_count(self.ctx, C.byref(t), C.byref(r)),
+                    "particle_count")
+        return t.value, r.value
+
     def read_bodies(self, state):
         """Upload a particle state (dict of numpy arrays, FP64 SoA)."""
         keep = {k: np.ascontiguousarray(v) for k, v in state.items()}
         self._keep = keep
-        self.n = len(keep["x"])
         v = make_view(keep)
         self._check(self.lib.fsph_upload(self.ctx, C.byref(v)), "upload")
 
@@ -218,6 +230,14 @@ class BodySystem:
 
     def gravitation_fmm(self):
         self.gravitation()
+
+
+def capacity_for(params, n):
+    """Capacity that holds n real particles and every periodic copy: a
+    particle gets at most one copy per non-empty subset of its periodic
+    axes (faces, edges, corner), so n * 2^k with k periodic axes."""
+    k = sum(int(bool(getattr(params, f"periodic_boundary_{a}"))) for a in "xyz")
+    return n << k
 
 
 def host_register(arr):

@@ -182,6 +182,7 @@ enum {
   FSPH_TIMER_INTEGRATE = 8,
   FSPH_TIMER_DT = 9,
   FSPH_TIMER_GRAVITY = 10,
+  FSPH_TIMER_PERIODIC = 11,
   FSPH_TIMER_COUNT = 16
 };
 
@@ -200,9 +201,13 @@ const char * fsph_last_error(const fsph_ctx * ctx);
 
 /* -- data movement ------------------------------------------------------- */
 /* Host -> device copy of a full particle set (mpisph/bodies_system.h:83-89
- * read_bodies analogue); resets iteration/time to the params' initial ones. */
+ * read_bodies analogue); resets iteration/time to the params' initial ones.
+ * With a periodic axis the set holds the real particles only, with ids
+ * 0 .. n-1 (the reference's id-sum check, boundary.h:241-246), and the
+ * capacity must leave room for the copies update_iteration appends. */
 fsph_status fsph_upload(fsph_ctx * ctx, const fsph_soa_view * host);
-/* Device -> host copy, current (sorted) order.  Synchronous. */
+/* Device -> host copy, current (sorted) order, periodic copies included
+ * (host->n = the total of fsph_particle_count).  Synchronous. */
 fsph_status fsph_download(fsph_ctx * ctx, fsph_soa_view * host);
 /* Host -> device copy of the non-NULL fields of `host` (host->n must equal
  * the uploaded count) into the current particle order, keeping time,
@@ -267,6 +272,11 @@ fsph_status fsph_conserved_sums(fsph_ctx * ctx, fsph_conserved * out);
 fsph_status fsph_timers(fsph_ctx * ctx, double * ms, int32_t count,
   int64_t * launches);
 fsph_status fsph_timers_reset(fsph_ctx * ctx);
+/* Particles held: *total includes the periodic copies (WALL particles of
+ * boundary.h) made by the last fsph_update_iteration, *real does not.
+ * fsph_download wants total.  Without periodic axes both equal the uploaded
+ * count. */
+fsph_status fsph_particle_count(fsph_ctx * ctx, int64_t * total, int64_t * real);
 /* Number of kernel launches this context has issued (all kinds). */
 int64_t fsph_launch_count(const fsph_ctx * ctx);
 /* Record CUDA event `slot` (0..63) on the context's stream; elapsed device

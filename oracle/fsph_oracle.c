@@ -74,6 +74,7 @@ struct orc_ctx {
   fsph_params p;
   int D;
   int64_t n, cap;
+  int64_t nreal; /* real particles hold ids [0, nreal); WALL copies above */
   double *x[3], *v[3], *vh[3], *a[3], *ga[3];
   double *gpot, *m, *h, *rho, *P, *cs, *u, *e, *dudt, *dedt, *K, *alpha, *vsig,
     *dtp;
@@ -358,6 +359,11 @@ static void init_time(orc_ctx * c) {
   }
 }
 
+static int is_periodic(const orc_ctx * c) {
+  return c->p.periodic_boundary_x || c->p.periodic_boundary_y ||
+         c->p.periodic_boundary_z;
+}
+
 #define CPY_IN(dst, src)                                                       \
   do {                                                                         \
     if(src) memcpy(dst, src, sizeof(double) * n);                              \
@@ -397,7 +403,26 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
   CPY_IN(c->dedt, v->dedt); CPY_IN(c->K, v->K); CPY_IN(c->alpha, v->alpha);
   CPY_IN(c->vsig, v->vsig); CPY_IN(c->dtp, v->dt);
   memcpy(c->id, v->id, 8 * n);
+  c->nreal = n;
+  if(is_periodic(c)) {
+    /* the reference's id-sum check (boundary.h:241-246) wants 0..n-1 */
+    char * seen = (char *)xalloc(n);
+    for(int64_t i = 0; i < n; ++i) {
+      if(c->id[i] < 0 || c->id[i] >= n || seen[c->id[i]]) {
+        free(seen);
+        return FSPH_ERR_ARG;
+      }
+      seen[c->id[i]] = 1;
+    }
+    free(seen);
+  }
   init_time(c);
+  return FSPH_OK;
+}
+
+int orc_particle_count(orc_ctx * c, int64_t * total, int64_t * real) {
+  if(total) *total = c->n;
+  if(real) *real = c->nreal;
   return FSPH_OK;
 }
 
@@ -618,12 +643,162 @@ static void collect_groups(orc_ctx * c, int64_t node) {
   }
 }
 
+/* Every per-particle array, for moves of whole particles. */
+#define ORC_NFIELDS 27
+static void field_list(orc_ctx * c, double *** out) {
+  int k = 0;
+  for(int d = 0; d < 3; ++d) {
+    out[k++] = &c->x[d]; out[k++] = &c->v[d]; out[k++] = &c->vh[d];
+    out[k++] = &c->a[d]; out[k++] = &c->ga[d];
+  }
+  out[k++] = &c->gpot; out[k++] = &c->m; out[k++] = &c->h; out[k++] = &c->rho;
+  out[k++] = &c->P; out[k++] = &c->cs; out[k++] = &c->u; out[k++] = &c->e;
+  out[k++] = &c->dudt; out[k++] = &c->dedt; out[k++] = &c->K;
+  out[k++] = &c->alpha;
+}
+
+static void ensure_cap(orc_ctx * c, int64_t need) {
+  if(need <= c->cap)
+    return;
+  int64_t cap = need + need / 4;
+  double ** fs[ORC_NFIELDS];
+  field_list(c, fs);
+  for(int k = 0; k < ORC_NFIELDS; ++k)
+    *fs[k] = (double *)realloc(*fs[k], 8 * cap);
+  double ** more[] = {&c->vsig, &c->dtp, &c->csnew};
+  for(int k = 0; k < 3; ++k)
+    *more[k] = (double *)realloc(*more[k], 8 * cap);
+  c->id = (int64_t *)realloc(c->id, 8 * cap);
+  c->key = (uint64_t *)realloc(c->key, 8 * cap);
+  c->cap = cap;
+}
+
+static void copy_particle(orc_ctx * c, int64_t dst, int64_t src) {
+  double ** fs[ORC_NFIELDS];
+  field_list(c, fs);
+  for(int k = 0; k < ORC_NFIELDS; ++k)
+    (*fs[k])[dst] = (*fs[k])[src];
+  c->vsig[dst] = c->vsig[src];
+  c->dtp[dst] = c->dtp[src];
+  c->csnew[dst] = c->csnew[src];
+  c->id[dst] = c->id[src];
+  c->key[dst] = c->key[src];
+}
+
+/* Copy of particle i with the given position appended as a WALL particle. */
+static void append_copy(orc_ctx * c, int64_t i, const double * pos) {
+  const int64_t j = c->n++;
+  copy_particle(c, j, i);
+  for(int d = 0; d < c->D; ++d)
+    c->x[d][j] = pos[d];
+  c->id[j] = j; /* c->nreal + running index of the copies (boundary.h:236-240) */
+}
+
+/* boundary::add_corner_XX / add_corner_XXX (boundary.h:72-118): the copy
+ * across the corner of the axes in dims[0..k). */
+static void add_corner(orc_ctx * c, const int * on_edge, const int * dims,
+  int k, const double (*box)[3], double halo, int64_t i) {
+  for(int t = 0; t < k; ++t)
+    if(!on_edge[dims[t]])
+      return;
+  double pos[3] = {c->x[0][i], c->x[1][i], c->D == 3 ? c->x[2][i] : 0.0};
+  for(int t = 0; t < k; ++t) {
+    const int d = dims[t];
+    const double x = c->x[d][i];
+    if(x + halo > box[1][d])
+      pos[d] = box[0][d] - fabs(x + box[0][d]);
+    else
+      pos[d] = box[1][d] + fabs(x + box[1][d]);
+  }
+  append_copy(c, i, pos);
+}
+
+/* boundary::pboundary_clean + pboundary_generate (boundary.h:45-248), as
+ * body_system::update_iteration calls them (bodies_system.h:160-169). */
+static int periodic_boundaries(orc_ctx * c) {
+  const int D = c->D;
+  /* clean: keep the real particles in their order (stable_partition) */
+  int64_t w = 0;
+  for(int64_t i = 0; i < c->n; ++i)
+    if(c->id[i] < c->nreal) {
+      if(w != i)
+        copy_particle(c, w, i);
+      ++w;
+    }
+  if(w == 0)
+    return FSPH_ERR_STATE;
+  c->n = w;
+  /* getSmoothinglength (bodies_system.h:112-124): the largest h */
+  double hmax = 0;
+  for(int64_t i = 0; i < c->n; ++i)
+    if(hmax < c->h[i])
+      hmax = c->h[i];
+  const double halo = 2.5 * hmax;
+  const int periodic[3] = {c->p.periodic_boundary_x, c->p.periodic_boundary_y,
+    c->p.periodic_boundary_z};
+  const double half = 0.5;
+  double box[2][3];
+  box[0][0] = -half * c->p.box_length;
+  box[1][0] = half * c->p.box_length;
+  box[0][1] = -half * c->p.box_width;
+  box[1][1] = half * c->p.box_width;
+  box[0][2] = -half * c->p.box_height;
+  box[1][2] = half * c->p.box_height;
+  /* step 1: teleport to the other side */
+  for(int64_t i = 0; i < c->n; ++i)
+    for(int d = 0; d < D; ++d) {
+      if(!periodic[d])
+        continue;
+      if(c->x[d][i] > box[1][d])
+        c->x[d][i] -= box[1][d] - box[0][d];
+      else if(c->x[d][i] <= box[0][d])
+        c->x[d][i] += box[1][d] - box[0][d];
+    }
+  /* copies near the faces, then edges and corners */
+  const int64_t nreal_now = c->n;
+  for(int64_t i = 0; i < nreal_now; ++i) {
+    int on_edge[3] = {0, 0, 0};
+    for(int d = 0; d < D; ++d) {
+      if(!periodic[d])
+        continue;
+      const double x = c->x[d][i];
+      if(x + halo > box[1][d] || x - halo <= box[0][d]) {
+        on_edge[d] = 1;
+        double pos[3] = {c->x[0][i], c->x[1][i], D == 3 ? c->x[2][i] : 0.0};
+        if(x + halo > box[1][d])
+          pos[d] -= (box[1][d] - box[0][d]);
+        else
+          pos[d] += (box[1][d] - box[0][d]);
+        ensure_cap(c, c->n + 1);
+        append_copy(c, i, pos);
+      }
+    }
+    ensure_cap(c, c->n + 4);
+    const int d01[2] = {0, 1}, d02[2] = {0, 2}, d21[2] = {2, 1};
+    const int d012[3] = {0, 1, 2};
+    if(D == 2)
+      add_corner(c, on_edge, d01, 2, (const double (*)[3])box, halo, i);
+    if(D == 3) {
+      add_corner(c, on_edge, d01, 2, (const double (*)[3])box, halo, i);
+      add_corner(c, on_edge, d02, 2, (const double (*)[3])box, halo, i);
+      add_corner(c, on_edge, d21, 2, (const double (*)[3])box, halo, i);
+      add_corner(c, on_edge, d012, 3, (const double (*)[3])box, halo, i);
+    }
+  }
+  return FSPH_OK;
+}
+
 int orc_update_iteration(orc_ctx * c) {
   const int D = c->D;
+  free_tree(c);
+  if(is_periodic(c)) {
+    int st = periodic_boundaries(c);
+    if(st)
+      return st;
+  }
   const int64_t n = c->n;
   if(n < 2)
     return FSPH_ERR_STATE;
-  free_tree(c);
   /* mpi_compute_range (bodies_system.h:231-268) */
   double lo[3], hi[3];
   for(int d = 0; d < D; ++d)

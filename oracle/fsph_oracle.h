@@ -36,6 +36,10 @@ int orc_get_time(orc_ctx * c, double * dt, double * totaltime, int64_t * it);
 int orc_set_time(orc_ctx * c, double dt, double totaltime, int64_t it);
 int orc_get_range(orc_ctx * c, double * range);
 
+/* Particles held: total includes the periodic copies (WALL) of the last
+ * update_iteration; real = the uploaded count. */
+int orc_particle_count(orc_ctx * c, int64_t * total, int64_t * real);
+
 int orc_update_iteration(orc_ctx * c);
 int orc_reset_ghosts(orc_ctx * c);
 int orc_density_pressure_soundspeed(orc_ctx * c);

@@ -73,6 +73,8 @@ def _load(path):
     lib.orc_gravity_direct.argtypes = [C.c_void_p, C.c_int64, C.c_int64]
     lib.orc_get_neighbors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
     lib.orc_get_order.argtypes = [C.c_void_p, C.c_void_p]
+    lib.orc_particle_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]
     _libs[path] = lib
     return lib
 
@@ -88,7 +90,6 @@ class Oracle:
             raise FsphError(1, "orc_create")
         if threads:
             self.lib.orc_set_threads(self.ctx, threads)
-        self.n = 0
 
     def close(self):
         if self.ctx:
@@ -112,9 +113,18 @@ class Oracle:
             return call
         raise AttributeError(name)
 
+    @property
+    def n(self):
+        """Particles held, periodic copies included."""
+        return self.count()[0]
+
+    def count(self):
+        t, r = C.c_int64(), C.c_int64()
+        self.lib.orc_particle_count(self.ctx, C.byref(t), C.byref(r))
+        return t.value, r.value
+
     def upload(self, state):
         self._keep = {k: np.ascontiguousarray(v) for k, v in state.items()}
-        self.n = len(self._keep["x"])
         v = make_view(self._keep)
         st = self.lib.orc_upload(self.ctx, C.byref(v))
         if st:

@@ -64,6 +64,12 @@ static void set_params(const fsph_params * p) {
   _sph_update_uniform_h = p->sph_update_uniform_h;
   _relaxation_steps = p->relaxation_steps;
   _enable_fmm = p->enable_fmm;
+  _box_length = p->box_length;
+  _box_width = p->box_width;
+  _box_height = p->box_height;
+  _periodic_boundary_x = p->periodic_boundary_x;
+  _periodic_boundary_y = p->periodic_boundary_y;
+  _periodic_boundary_z = p->periodic_boundary_z;
   fmm::gc = p->gravitational_constant;
   kernels::select();
   viscosity::select();
@@ -237,9 +243,31 @@ static void compute_range(std::vector<body> & bodies, range_t & range) {
   range = lrange;
 }
 
+int orc_particle_count(orc_ctx * c, int64_t * total, int64_t * real) {
+  auto & ents = c->tree->entities();
+  int64_t r = 0;
+  for(auto & b : ents)
+    r += b.getType() == NORMAL;
+  if(total)
+    *total = (int64_t)ents.size();
+  if(real)
+    *real = r;
+  return FSPH_OK;
+}
+
 int orc_update_iteration(orc_ctx * c) {
   tree_topology_t & t = *c->tree;
   t.clean();
+  if(param::periodic_boundary_x || param::periodic_boundary_y ||
+     param::periodic_boundary_z) {
+    // bodies_system.h:160-169 with getSmoothinglength (:112-124) inlined
+    boundary::pboundary_clean(t.entities());
+    double smoothinglength = 0;
+    for(size_t i = 0; i < t.entities().size(); ++i)
+      if(smoothinglength < t.entity(i).radius())
+        smoothinglength = t.entity(i).radius();
+    boundary::pboundary_generate(t.entities(), 2.5 * smoothinglength);
+  }
   compute_range(t.entities(), c->range);
   if(c->range[0] == c->range[1])
     return FSPH_ERR_ARG;

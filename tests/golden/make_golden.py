@@ -4,7 +4,7 @@ Runs the laristra/flecsph hot path compiled here (oracle/_ref, built from the
 reference sources by oracle/Makefile) on small seeded inputs and stores
 inputs and outputs as compressed .npz files next to this script:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [--only NAME ...]
 
 Each fixture holds: the input state (in a shuffled order), the parameter
 block, and after update_iteration the Morton keys, sorted ids, range and
@@ -47,13 +47,36 @@ def cases():
     yield "sod2d_1000", setups.shuffled(s, 5), p, 2
     s, p, m = setups.noh2d(40)
     yield "noh2d_1264", setups.shuffled(s, 6), p, 2
+    # periodic boundaries: copies regenerated at every update_iteration;
+    # a few particles start outside the box and are teleported back
+    s, p, m = setups.kh2d(40)
+    yield "kh2d_periodic_1600", setups.shuffled(_outside(s), 7), p, 2
+    s, p, m = setups.kh3d(12)
+    p.periodic_boundary_y = p.periodic_boundary_z = 0
+    yield "kh3d_periodic_x_1728", setups.shuffled(_outside(s), 8), p, 2
+
+
+def _outside(s):
+    """Move a few particles out of the box, off the lattice."""
+    s = {k: v.copy() for k, v in s.items()}
+    s["x"][:5] += 0.6137
+    s["x"][5:8] -= 0.5419
+    return s
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = sys.argv[1:]
+    only = None
+    if "--only" in args:
+        k = args.index("--only")
+        only = set(args[k + 1:])
+        args = args[:k]
+    ref_root = args[0] if args else "/root/reference"
     if not pyoracle.build_ref(ref_root):
         sys.exit(f"reference sources not found at {ref_root}")
     for name, state, params, steps in cases():
+        if only is not None and name not in only:
+            continue
         o = pyoracle.Oracle("reference", params)
         o.upload(state)
         out = {}

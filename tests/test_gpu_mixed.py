@@ -26,10 +26,10 @@ DEDT_TOL = 1e-5
 
 def _run_passes(state, params, mode, steps=0):
     from flecsph_gb300 import build
-    from flecsph_gb300.sph import BodySystem
+    from flecsph_gb300.sph import BodySystem, capacity_for
     build.build()
     params.precision_mode = mode
-    bs = BodySystem(params, len(state["x"]))
+    bs = BodySystem(params, capacity_for(params, len(state["x"])))
     bs.read_bodies(state)
     for _ in range(steps):
         bs.step()
@@ -54,21 +54,24 @@ def accel_err(a, b):
     return np.linalg.norm(A - B, axis=1) / np.maximum(mag, 1e-3 * rms)
 
 
-@pytest.mark.parametrize("problem", ["sod", "sedov", "polytrope"])
+@pytest.mark.parametrize("problem", ["sod", "sedov", "polytrope", "kh"])
 def test_mixed_matches_fp64(problem):
     if problem == "sod":
         s, p, m = setups.sod3d(40, 10, 10)
     elif problem == "sedov":
         s, p, m = setups.sedov3d(32)
+    elif problem == "kh":
+        s, p, m = setups.kh3d(24)   # periodic copies on every axis
     else:
         s, p, m = setups.polytrope3d(20000)
         p.enable_fmm = 0
         p.max_neighbors = 1024
     s = setups.shuffled(s, 3)
-    two_pi = 2 * np.pi
-    s["vx"][:] = 0.05 * np.sin(two_pi * s["y"])
-    s["vy"][:] = 0.05 * np.sin(two_pi * s["z"])
-    s["vz"][:] = 0.05 * np.sin(two_pi * s["x"])
+    if problem != "kh":
+        two_pi = 2 * np.pi
+        s["vx"][:] = 0.05 * np.sin(two_pi * s["y"])
+        s["vy"][:] = 0.05 * np.sin(two_pi * s["z"])
+        s["vz"][:] = 0.05 * np.sin(two_pi * s["x"])
     r64, l64 = _run_passes(s, p, PRECISION_FP64)
     rmx, lmx = _run_passes(s, p, PRECISION_MIXED)
     assert np.array_equal(r64["id"], rmx["id"])
@@ -84,7 +87,9 @@ def test_mixed_matches_fp64(problem):
     normwise = np.abs(AMX - A64).max() / np.abs(A64).max()
     print(problem, "accel rel err max", e.max(), "median", np.median(e),
           "normwise", normwise, "rho", rho_err.max())
-    if problem == "sod":
+    if problem in ("sod", "kh"):
+        # lattices: interior accelerations cancel to ~0, so the bound is
+        # normwise there
         assert normwise <= ACCEL_TOL, normwise
     else:
         assert e.max() <= ACCEL_TOL, e.max()

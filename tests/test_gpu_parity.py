@@ -18,9 +18,9 @@ FP64_TOL = 1e-12
 
 def _bs(params, n):
     from flecsph_gb300 import build
-    from flecsph_gb300.sph import BodySystem
+    from flecsph_gb300.sph import BodySystem, capacity_for
     build.build()
-    return BodySystem(params, n)
+    return BodySystem(params, capacity_for(params, n))
 
 
 def normwise(a, b):
