@@ -28,6 +28,7 @@ SOURCES = {
     "fsph_periodic.cu": ["-fmad=false"],
     "fsph_peak.cu": [],
     "fsph_api.cu": [],
+    "fsph_ensemble.cu": [],
 }
 
 

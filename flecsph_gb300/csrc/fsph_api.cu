@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "fsph_ctx.cuh"
 #include "fsph_internal.cuh"
 
 using namespace fsph;
@@ -15,60 +16,7 @@ namespace {
 
 const int GROUP_MAX = 32;
 
-struct TimerRec {
-  int phase;
-  int e0, e1;
-};
-
 }  // namespace
-
-struct fsph_ctx {
-  fsph_params p;
-  PhysParams pp;
-  int device = 0;
-  int nsm = 152;
-  cudaStream_t stream = nullptr;
-  int64_t cap = 0;
-  int n = 0;
-  Particles P{}, Palt{};
-  double * cs_new = nullptr;
-  unsigned long long * skeys = nullptr;
-  unsigned long long * skeys_tmp = nullptr;
-  int * svals = nullptr;
-  int * svals_tmp = nullptr;
-  unsigned * hist = nullptr;
-  unsigned long long * d_range = nullptr;
-  Tree T{};
-  Lists Ls{};
-  Packed K{};
-  bool mixed = false;
-  GravNode * gnodes = nullptr;
-  double * gbox = nullptr;
-  unsigned * gcounter = nullptr;
-  // periodic boundaries: real particles hold ids [0, nreal)
-  bool periodic = false;
-  long long nreal = 0;
-  PeriodicScratch PS{};
-  DevTime * d_time = nullptr;
-  DevStatus * d_status = nullptr;
-  double * d_cons = nullptr;
-  int64_t iteration = 0;
-  bool tree_ok = false;
-  bool uploaded = false;
-  long long launches = 0;
-  // timers
-  bool timing = false;
-  std::vector<cudaEvent_t> events;
-  int ev_used = 0;
-  std::vector<TimerRec> pending;
-  double timer_ms[FSPH_TIMER_COUNT] = {0};
-  long long timer_calls[FSPH_TIMER_COUNT] = {0};
-  std::string last_error;
-  std::vector<void *> allocs;
-  cudaEvent_t marks[64] = {};
-
-  Launch L() { return Launch{stream, &launches}; }
-};
 
 namespace {
 
@@ -376,13 +324,8 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   }
   if(cudaMemset(c->d_status, 0, sizeof(DevStatus)) != cudaSuccess)
     return fail(FSPH_ERR_CUDA);
-  c->events.resize(4096);
-  for(auto & e : c->events)
-    if(cudaEventCreate(&e) != cudaSuccess)
-      return fail(FSPH_ERR_CUDA);
-  for(auto & e : c->marks)
-    if(cudaEventCreate(&e) != cudaSuccess)
-      return fail(FSPH_ERR_CUDA);
+  // timer and mark events are made on first use: an ensemble holds hundreds
+  // of contexts that never time themselves
   *status = FSPH_OK;
   return c;
 }
@@ -494,6 +437,8 @@ fsph_status fsph_mark(fsph_ctx * c, int32_t slot) {
   fsph_status s = set_device(c);
   if(s)
     return s;
+  if(!c->marks[slot])
+    CK(cudaEventCreate(&c->marks[slot]));
   CK(cudaEventRecord(c->marks[slot], c->stream));
   return FSPH_OK;
 }
@@ -504,6 +449,8 @@ fsph_status fsph_mark_elapsed(fsph_ctx * c, int32_t a, int32_t b, double * ms) {
   fsph_status s = set_device(c);
   if(s)
     return s;
+  if(!c->marks[a] || !c->marks[b])
+    return FSPH_ERR_STATE;
   CK(cudaEventSynchronize(c->marks[b]));
   float f = 0;
   CK(cudaEventElapsedTime(&f, c->marks[a], c->marks[b]));
@@ -1044,6 +991,11 @@ fsph_status fsph_timers_reset(fsph_ctx * c) {
   if(s)
     return s;
   CK(cudaStreamSynchronize(c->stream));
+  if(c->events.empty()) {
+    c->events.resize(4096);
+    for(auto & e : c->events)
+      CK(cudaEventCreate(&e));
+  }
   c->pending.clear();
   c->ev_used = 0;
   for(int k = 0; k < FSPH_TIMER_COUNT; ++k) {

@@ -1,0 +1,65 @@
+// fsph_ctx.cuh -- the context behind the opaque fsph_ctx handle of
+// include/fsph.h, shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "fsph_internal.cuh"
+
+namespace fsph {
+struct TimerRec {
+  int phase;
+  int e0, e1;
+};
+}  // namespace fsph
+
+struct fsph_ctx {
+  fsph_params p;
+  fsph::PhysParams pp;
+  int device = 0;
+  int nsm = 152;
+  cudaStream_t stream = nullptr;
+  int64_t cap = 0;
+  int n = 0;
+  fsph::Particles P{}, Palt{};
+  double * cs_new = nullptr;
+  unsigned long long * skeys = nullptr;
+  unsigned long long * skeys_tmp = nullptr;
+  int * svals = nullptr;
+  int * svals_tmp = nullptr;
+  unsigned * hist = nullptr;
+  unsigned long long * d_range = nullptr;
+  fsph::Tree T{};
+  fsph::Lists Ls{};
+  fsph::Packed K{};
+  bool mixed = false;
+  fsph::GravNode * gnodes = nullptr;
+  double * gbox = nullptr;
+  unsigned * gcounter = nullptr;
+  // periodic boundaries: real particles hold ids [0, nreal)
+  bool periodic = false;
+  long long nreal = 0;
+  fsph::PeriodicScratch PS{};
+  fsph::DevTime * d_time = nullptr;
+  fsph::DevStatus * d_status = nullptr;
+  double * d_cons = nullptr;
+  int64_t iteration = 0;
+  bool tree_ok = false;
+  bool uploaded = false;
+  long long launches = 0;
+  // timers
+  bool timing = false;
+  std::vector<cudaEvent_t> events;
+  int ev_used = 0;
+  std::vector<fsph::TimerRec> pending;
+  double timer_ms[FSPH_TIMER_COUNT] = {0};
+  long long timer_calls[FSPH_TIMER_COUNT] = {0};
+  std::string last_error;
+  std::vector<void *> allocs;
+  cudaEvent_t marks[64] = {};
+
+  fsph::Launch L() { return fsph::Launch{stream, &launches}; }
+};

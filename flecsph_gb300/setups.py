@@ -263,6 +263,27 @@ def noh2d(n1d=100, gamma=5.0 / 3.0, eta=1.5, P0=1e-6):
     return s, params, dict(problem="noh2d", n=n, dx=dx)
 
 
+def ensemble2d(nproblems=256, nmin=2000, nmax=200000, seed=2024):
+    """Many independent 2D problems: particle counts log-uniform in
+    [nmin, nmax] (seeded), alternately a Sod tube (10:1 lattice) and a Noh
+    disc, all in mixed precision.  Returns a list of (state, params, meta);
+    the actual counts follow from the lattices (recorded in meta)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    target = np.exp(rng.uniform(math.log(nmin), math.log(nmax), nproblems))
+    out = []
+    for k, nt in enumerate(target):
+        if k % 2 == 0:
+            ny = max(4, int(round(math.sqrt(nt / 10.0))))
+            s, p, m = sod2d(10 * ny, ny)
+        else:
+            n1d = max(8, int(round(math.sqrt(4.0 * nt / math.pi))))
+            s, p, m = noh2d(n1d)
+        p.precision_mode = 1
+        m["target_n"] = float(nt)
+        out.append((s, p, m))
+    return out
+
+
 def shuffled(state, seed=99):
     """The same particles in a seeded random order (ids travel along)."""
     n = len(state["x"])

@@ -71,6 +71,23 @@ def library():
     lib.fsph_timers.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
     lib.fsph_launch_count.argtypes = [C.c_void_p]
     lib.fsph_launch_count.restype = C.c_int64
+    lib.fsph_ensemble_create.restype = C.c_void_p
+    lib.fsph_ensemble_create.argtypes = [C.c_int32, C.POINTER(C.c_int)]
+    lib.fsph_ensemble_add.restype = C.c_void_p
+    lib.fsph_ensemble_add.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int64,
+                                      C.POINTER(C.c_int)]
+    lib.fsph_ensemble_step.argtypes = [C.c_void_p, C.c_int32]
+    lib.fsph_ensemble_sync.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    lib.fsph_ensemble_set_lanes.argtypes = [C.c_void_p, C.c_int32]
+    lib.fsph_ensemble_tune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_double)]
+    lib.fsph_ensemble_last_error.restype = C.c_char_p
+    lib.fsph_ensemble_last_error.argtypes = [C.c_void_p]
+    lib.fsph_ensemble_destroy.argtypes = [C.c_void_p]
+    lib.fsph_ensemble_destroy.restype = None
+    lib.fsph_ensemble_size.argtypes = [C.c_void_p]
+    lib.fsph_ensemble_member.restype = C.c_void_p
+    lib.fsph_ensemble_member.argtypes = [C.c_void_p, C.c_int32]
     lib.fsph_particle_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
                                         C.POINTER(C.c_int64)]
     lib.fsph_upload_fields.argtypes = [C.c_void_p, C.POINTER(SoAView)]
@@ -87,19 +104,26 @@ def library():
 class BodySystem:
     """One particle system on one GPU (mirror of body_system<double, D>)."""
 
-    def __init__(self, params, capacity, device=0):
+    def __init__(self, params, capacity, device=0, _member_of=None):
         lib = library()
         self.params = params
         st = C.c_int(0)
-        self.ctx = lib.fsph_create(C.byref(params), device, int(capacity), C.byref(st))
+        if _member_of is None:
+            self.ctx = lib.fsph_create(C.byref(params), device, int(capacity),
+                                       C.byref(st))
+        else:
+            self.ctx = lib.fsph_ensemble_add(_member_of, C.byref(params),
+                                             int(capacity), C.byref(st))
         if not self.ctx:
             raise FsphError(st.value, "fsph_create")
         self.lib = lib
         self.capacity = capacity
+        self._owned = _member_of is None
 
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.fsph_destroy(self.ctx)
+            if self._owned:
+                self.lib.fsph_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
@@ -230,6 +254,59 @@ class BodySystem:
 
     def gravitation_fmm(self):
         self.gravitation()
+
+
+class Ensemble:
+    """Many independent problems on one GPU, stepped together as CUDA graphs
+    (fsph_ensemble_* of include/fsph.h).  Members are BodySystem objects
+    owned by the ensemble."""
+
+    def __init__(self, device=0):
+        lib = library()
+        st = C.c_int(0)
+        self.ens = lib.fsph_ensemble_create(device, C.byref(st))
+        if not self.ens:
+            raise FsphError(st.value, "fsph_ensemble_create")
+        self.lib = lib
+        self.members = []
+
+    def add(self, params, capacity):
+        m = BodySystem(params, capacity, _member_of=self.ens)
+        self.members.append(m)
+        return m
+
+    def _check(self, st, where):
+        if st:
+            raise FsphError(st, where, self.lib.fsph_ensemble_last_error(self.ens).decode())
+
+    def step(self, nsteps=1):
+        self._check(self.lib.fsph_ensemble_step(self.ens, nsteps), "ensemble_step")
+
+    def sync(self):
+        failed = C.c_int32(-1)
+        self._check(self.lib.fsph_ensemble_sync(self.ens, C.byref(failed)), "ensemble_sync")
+
+    def set_lanes(self, lanes):
+        self._check(self.lib.fsph_ensemble_set_lanes(self.ens, lanes), "ensemble_set_lanes")
+
+    def tune(self, steps_per_trial=3):
+        lanes, ms = C.c_int32(0), C.c_double(0)
+        self._check(self.lib.fsph_ensemble_tune(self.ens, steps_per_trial, C.byref(lanes),
+                                                C.byref(ms)), "ensemble_tune")
+        return lanes.value, ms.value
+
+    def close(self):
+        if getattr(self, "ens", None):
+            for m in self.members:
+                m.ctx = None
+            self.lib.fsph_ensemble_destroy(self.ens)
+            self.ens = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def capacity_for(params, n):

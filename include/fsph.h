@@ -305,6 +305,37 @@ fsph_status fsph_sort_keys_noalloc(const double * x, const double * y,
  * in TFLOP/s (2 flops per FMA), from a register-resident FMA chain kernel. */
 fsph_status fsph_measure_peak(int32_t device, int32_t kind, double * tflops);
 
+/* -- ensembles ----------------------------------------------------------- */
+/* Many independent problems on one GPU (the reference runs one problem per
+ * MPI job, app/drivers/hydro/main_driver.cc; a parameter study is many jobs).
+ * Each member is an ordinary fsph_ctx owned by the ensemble: upload, download
+ * and query it with the calls above.  fsph_ensemble_step advances every
+ * member by whole driver iterations (fsph_step); after each member's initial
+ * iteration and one regular one, the regular iteration of all members runs
+ * as CUDA graphs, one launch per lane (stream).  Periodic members and
+ * members with timers on step eagerly.  Members' own calls between steps are
+ * allowed; a change of a member's state re-captures the graphs. */
+typedef struct fsph_ensemble fsph_ensemble;
+fsph_ensemble * fsph_ensemble_create(int32_t device, fsph_status * status);
+/* Adds a problem with its own parameters and capacity; the returned context
+ * is owned by the ensemble (never fsph_destroy it). */
+fsph_ctx * fsph_ensemble_add(fsph_ensemble * ens, const fsph_params * params,
+  int64_t capacity, fsph_status * status);
+int32_t fsph_ensemble_size(const fsph_ensemble * ens);
+fsph_ctx * fsph_ensemble_member(fsph_ensemble * ens, int32_t k);
+fsph_status fsph_ensemble_step(fsph_ensemble * ens, int32_t nsteps);
+/* Waits for every member; the first member with a device-side error gives
+ * the status and its index (else -1). */
+fsph_status fsph_ensemble_sync(fsph_ensemble * ens, int32_t * failed_member);
+/* Members are spread over `lanes` streams by particle count. */
+fsph_status fsph_ensemble_set_lanes(fsph_ensemble * ens, int32_t lanes);
+/* Times steps_per_trial steps for 1, 2, 4, 8, 16 lanes (advancing every
+ * member meanwhile) and keeps the fastest. */
+fsph_status fsph_ensemble_tune(fsph_ensemble * ens, int32_t steps_per_trial,
+  int32_t * lanes_chosen, double * ms_per_step);
+const char * fsph_ensemble_last_error(const fsph_ensemble * ens);
+void fsph_ensemble_destroy(fsph_ensemble * ens);
+
 #ifdef __cplusplus
 }
 #endif
