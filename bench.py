@@ -2,6 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
                     [--n1d 128] [--precision mixed|fp64]
+                    [--workload sedov|kh|polytrope|ensemble]
 
 Workload: the 3D Sedov blast, 128^3 = 2,097,152 particles on a 1%-jittered
 lattice (seeded), Wendland C6, ideal gas gamma 5/3, thermokinetic energy,
@@ -15,6 +16,15 @@ so no explicit flush is needed between steps.
 `value` is measured with CUDA events on the library's stream around K
 steps; `e2e` repeats the measurement through the C ABI with host buffers,
 copying each step's inputs from pinned host memory and its results back.
+Other workloads (not the default line): `kh` -- Kelvin-Helmholtz in the
+periodic box, 256^3 by default, with the energy and momentum drift of the
+timed steps in both precisions; `polytrope` -- the n=1 polytrope with tree
+gravity (quadrupole, theta 0.5), 4M particles by default, with the gravity
+error of 64 sampled blocks of sinks against direct FP64 summation over all
+sources on the host cores; `ensemble` -- 256 independent 2D problems (Sod and
+Noh, log-uniform sizes 2k-200k) stepped as CUDA graphs, against the same
+members stepped one by one.
+
 `--impl reference` times the reference algorithm on the host cores instead
 (the CPU oracle: the reference compiled from its sources where those exist
 on this machine, otherwise the plain-C restatement), on a 64^3 sample of
@@ -73,7 +83,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
-    ap.add_argument("--n1d", type=int, default=128)
+    ap.add_argument("--workload", default="sedov",
+                    choices=["sedov", "kh", "polytrope", "ensemble"])
+    ap.add_argument("--n1d", type=int, default=None,
+                    help="lattice size (sedov 128, kh 256)")
+    ap.add_argument("--n", type=int, default=None, help="particles (polytrope 4M)")
+    ap.add_argument("--problems", type=int, default=256, help="ensemble members")
     ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -229,6 +244,115 @@ OUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "vhx", "vhy", "vhz", "ax", "ay", 
               "dt", "h"]
 
 
+def drift(c0, c1, s, s1=None):
+    """Relative change of the conserved sums over the timed steps: energy
+    against |E0|, momentum against sum m|v| (the larger of the input's and
+    the final state's, for problems that start at rest)."""
+    def mv(t):
+        return float((t["m"] * np.sqrt(t["vx"] ** 2 + t["vy"] ** 2 + t["vz"] ** 2)).sum())
+    scale_p = max(mv(s), mv(s1) if s1 is not None else 0.0)
+    dp = np.array(c1["momentum"]) - np.array(c0["momentum"])
+    return {"energy": abs(c1["energy"] - c0["energy"]) / abs(c0["energy"]),
+            "momentum": float(np.linalg.norm(dp)) / max(scale_p, 1e-300),
+            "mass": abs(c1["mass"] - c0["mass"]) / c0["mass"]}
+
+
+def gravity_check(bs, p, blocks=64, block=1024, seed=7):
+    """Tree gravity of the current state against direct FP64 summation over
+    all sources (the oracle, on every host core) for `blocks` blocks of
+    `block` consecutive sinks at seeded offsets of the sorted order."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build_port()
+    st = bs.download()
+    n = len(st["x"])
+    o = pyoracle.Oracle("port", p, threads=os.cpu_count() or 1)
+    o.upload(st)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    starts = np.sort(rng.choice(max(1, n // block), size=min(blocks, n // block),
+                                replace=False)) * block
+    t0 = time.perf_counter()
+    for a in starts:
+        o.gravity_direct(int(a), int(min(n, a + block)))
+    el = time.perf_counter() - t0
+    ref = o.download()
+    o.close()
+    idx = np.concatenate([np.arange(a, min(n, a + block)) for a in starts])
+    G = np.stack([st[k][idx] for k in ("gax", "gay", "gaz")], 1)
+    R = np.stack([ref[k][idx] for k in ("gax", "gay", "gaz")], 1)
+    mag = np.linalg.norm(R, axis=1)
+    rms = np.sqrt((mag ** 2).mean())
+    err = np.linalg.norm(G - R, axis=1) / np.maximum(mag, 1e-3 * rms)
+    pot = np.abs(st["gpot"][idx] - ref["gpot"][idx]) / np.abs(ref["gpot"][idx])
+    return {"sinks": int(len(idx)), "sources": n, "theta": p.fmm_macangle,
+            "order": p.gravity_order, "accel_rel_err_median": float(np.median(err)),
+            "accel_rel_err_p99": float(np.percentile(err, 99)),
+            "accel_rel_err_max": float(err.max()),
+            "potential_rel_err_median": float(np.median(pot)),
+            "direct_sum_seconds": el}
+
+
+def ensemble_arm(args):
+    """Config 4: independent 2D problems stepped together as CUDA graphs,
+    against the same members stepped one by one (graphs off)."""
+    rank, world, local = dist_info()
+    dist = init_dist(world)
+    from flecsph_gb300 import build, setups
+    if rank == 0:
+        build.build()
+    barrier(dist)
+    from flecsph_gb300 import sph
+    probs = setups.ensemble2d(args.problems)
+    ntot = sum(m["n"] for _, _, m in probs)
+    ens = sph.Ensemble(device=local)
+    members = [ens.add(p, m["n"]) for s, p, m in probs]
+    for mb, (s, p, m) in zip(members, probs):
+        mb.read_bodies(s)
+    ens.step(1 + args.warmup)
+    ens.sync()
+    res = {}
+    for mode in ("one_by_one", "graphs"):
+        if mode == "graphs":
+            lanes, _ = ens.tune(2)
+        else:
+            ens.set_lanes(0)
+            lanes = 0
+        ens.step(2)
+        ens.sync()
+        l0 = sum(mb.launch_count() for mb in members)
+        barrier(dist)
+        with Clocks(local) as clk:
+            t0 = time.perf_counter()
+            ens.step(args.steps)
+            ens.sync()
+            el = time.perf_counter() - t0
+        el = max_over_ranks(dist, el)
+        res[mode] = dict(seconds=el, lanes=lanes, clocks=clk.summary(),
+                         launches=sum(mb.launch_count() for mb in members) - l0)
+    ens.close()
+    if rank != 0:
+        return
+    K = args.steps
+    g = res["graphs"]
+    sizes = [m["n"] for _, _, m in probs]
+    line = {
+        "metric": "particle-steps/s", "value": world * ntot * K / g["seconds"],
+        "unit": "particle-steps/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": 1e3 * g["seconds"] / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"ensemble2d_{len(probs)}_sod_noh",
+                   "problems": len(probs), "n_particles_total": ntot,
+                   "n_min": min(sizes), "n_max": max(sizes), "precision": "mixed",
+                   "lanes": g["lanes"], "timing": "host wall clock around K steps "
+                   "with a device sync on both sides (many streams)"},
+        "one_by_one": {"value": world * ntot * K / res["one_by_one"]["seconds"],
+                       "ms_per_step": 1e3 * res["one_by_one"]["seconds"] / K},
+        "gpu_launches": g["launches"],
+        "clocks": g["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def gpu_arm(args):
     rank, world, local = dist_info()
     dist = init_dist(world)
@@ -239,8 +363,21 @@ def gpu_arm(args):
     barrier(dist)
     from flecsph_gb300 import sph
 
-    s, p, meta = setups.sedov3d(args.n1d)
+    if args.workload == "kh":
+        n1d = args.n1d or 256
+        s, p, meta = setups.kh3d(n1d)
+        wname = f"kh3d_{n1d}^3_periodic"
+    elif args.workload == "polytrope":
+        npart = args.n or (1 << 22)
+        s, p, meta = setups.polytrope3d(npart, rho_floor=1e-2)
+        p.max_neighbors = 512
+        wname = f"polytrope3d_{npart}_gravity_quadrupole_theta0.5"
+    else:
+        n1d = args.n1d or 128
+        s, p, meta = setups.sedov3d(n1d)
+        wname = f"sedov3d_{n1d}^3"
     n = meta["n"]
+    cap = sph.capacity_for(p, n, s)
     mixed_ok = sph.mixed_available() if hasattr(sph, "mixed_available") else False
     prec = args.precision
     if prec == "auto":
@@ -253,15 +390,17 @@ def gpu_arm(args):
         modes = ["mixed"]
     for mode in modes:
         p.precision_mode = PRECISION_MIXED if mode == "mixed" else PRECISION_FP64
-        bs = sph.BodySystem(p, n, device=local)
+        bs = sph.BodySystem(p, cap, device=local)
         bs.read_bodies(s)
         bs.step()  # initial iteration
         for _ in range(args.warmup):
             bs.step()
         bs.sync()
-        off = np.zeros(n + 1, np.int64)
+        ntot = bs.count()[0]
+        off = np.zeros(ntot + 1, np.int64)
         bs.lib.fsph_get_neighbors(bs.ctx, off.ctypes.data, None, 0)
-        nb_mean = float(off[-1]) / n
+        nb_mean = float(off[-1]) / ntot
+        cons0 = bs.conserved()
         bs.timers_reset()
         launches0 = bs.launch_count()
         barrier(dist)
@@ -275,9 +414,26 @@ def gpu_arm(args):
         launches = bs.launch_count() - launches0
         ms = max_over_ranks(dist, ms)
         timers = bs.timers()
-        state = bs.download(fields=["ax", "ay", "az", "id"])
+        cons1 = bs.conserved()
+        state = bs.download(fields=["m", "vx", "vy", "vz", "id"])
         results[mode] = dict(ms=ms, timers=timers, launches=launches, nb_mean=nb_mean,
-                             clocks=clk.summary(), accel=state)
+                             clocks=clk.summary(), ntot=ntot,
+                             drift=drift(cons0, cons1, s, state))
+        # the accelerations of one pass from the input state
+        bs.read_bodies(s)
+        bs.update_iteration()
+        bs.eos_init()
+        if p.thermokinetic_formulation:
+            bs.set_total_energy()
+        bs.density_pressure_soundspeed()
+        bs.save_velocityhalf()
+        bs.acceleration()
+        if p.enable_fmm:
+            bs.gravitation()
+        results[mode]["same_state"] = bs.download(
+            fields=["ax", "ay", "az", "gax", "gay", "gaz", "id"])
+        if args.workload == "polytrope" and rank == 0 and mode == modes[-1]:
+            results[mode]["gravity_check"] = gravity_check(bs, p)
         # end to end through the C ABI with pinned host buffers
         if not args.no_e2e:
             host = bs.download()
@@ -293,8 +449,8 @@ def gpu_arm(args):
                 regs.append(host[f])
             vin = make_view(host, fields=set(IN_FIELDS) | {"id"})
             vout = make_view(host, fields=set(OUT_FIELDS) | {"id", "key"})
-            h2d = 8 * n * (len(IN_FIELDS) + 1)
-            d2h = 8 * n * (len(OUT_FIELDS) + 2)
+            h2d = 8 * ntot * (len(IN_FIELDS) + 1)
+            d2h = 8 * ntot * (len(OUT_FIELDS) + 2)
             barrier(dist)
             t0 = time.perf_counter()
             bs.mark(2)
@@ -349,8 +505,9 @@ def gpu_arm(args):
         "ms_per_step": head["ms"] / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if "mixed" in results else "f64",
         "data": "synthetic",
-        "config": {"workload": f"sedov3d_{args.n1d}^3", "n_particles": n,
-                   "kernel": "wendland_c6", "gamma": 5.0 / 3.0, "eta": meta["eta"],
+        "config": {"workload": wname, "n_particles": n,
+                   "n_with_periodic_copies": head["ntot"],
+                   "kernel": "wendland_c6", "gamma": p.poly_gamma, "eta": p.sph_eta,
                    "mean_neighbors": head["nb_mean"], "parallelism": f"replicas{world}",
                    "l2": "inputs exceed L2 (state ~0.5 GB, lists ~0.8 GB); no flush",
                    "precision": "mixed" if "mixed" in results else "fp64"},
@@ -364,8 +521,10 @@ def gpu_arm(args):
         line["fp64"] = {"value": world * n * K / (results["fp64"]["ms"] * 1e-3),
                         "ms_per_step": results["fp64"]["ms"] / K}
     if "mixed" in results and "fp64" in results:
-        a64 = results["fp64"]["accel"]
-        am = results["mixed"]["accel"]
+        # one pass of each precision from the same state (after K steps the
+        # two runs have drifted apart, which says nothing about one pass)
+        a64 = results["fp64"]["same_state"]
+        am = results["mixed"]["same_state"]
         o64 = np.argsort(a64["id"])
         om = np.argsort(am["id"])
         A64 = np.stack([a64[k][o64] for k in ("ax", "ay", "az")], 1)
@@ -373,14 +532,31 @@ def gpu_arm(args):
         mag = np.linalg.norm(A64, axis=1)
         rms = np.sqrt((mag ** 2).mean())
         err = np.linalg.norm(AM - A64, axis=1) / np.maximum(mag, 1e-3 * rms)
+        norm = float(np.abs(AM - A64).max() / np.abs(A64).max())
         line["mixed_vs_fp64"] = {"speedup": results["fp64"]["ms"] / results["mixed"]["ms"],
                                  "accel_rel_err_max": float(err.max()),
-                                 "accel_rel_err_median": float(np.median(err))}
+                                 "accel_rel_err_median": float(np.median(err)),
+                                 "accel_normwise": norm,
+                                 "measured_on": "one acceleration pass of each precision "
+                                                "from the input state; per-particle "
+                                                "|da|/max(|a|, 1e-3 rms|a|)"}
+        if p.enable_fmm:
+            G64 = np.stack([a64[k][o64] for k in ("gax", "gay", "gaz")], 1)
+            GM = np.stack([am[k][om] for k in ("gax", "gay", "gaz")], 1)
+            gm = np.linalg.norm(G64, axis=1)
+            ge = np.linalg.norm(GM - G64, axis=1) / np.maximum(gm, 1e-3 * np.sqrt((gm ** 2).mean()))
+            line["mixed_vs_fp64"]["gravity_rel_err_max"] = float(ge.max())
+            line["mixed_vs_fp64"]["gravity_rel_err_median"] = float(np.median(ge))
     if "e2e" in head:
         e = head["e2e"]
         line["e2e"] = {"value": world * n * K / (e["ms"] * 1e-3), "unit": "particle-steps/s",
                        "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"]}
-    if not args.no_cpu:
+    if args.workload == "kh":
+        line["drift"] = {m: results[m]["drift"] for m in results}
+    if args.workload == "polytrope":
+        line["gravity_check"] = head.get("gravity_check")
+        line["drift"] = {m: results[m]["drift"] for m in results}
+    if not args.no_cpu and args.workload == "sedov":
         cpu = run_cpu_oracle(64, None, os.cpu_count() or 1, min_seconds=10.0)
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line["peaks_measured"] = {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}
@@ -391,6 +567,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "ensemble":
+        ensemble_arm(args)
     else:
         gpu_arm(args)
 

@@ -85,6 +85,7 @@ struct fsph_ensemble {
   std::vector<Member> m;
   int lanes = 1;
   bool lanes_assigned = false;
+  bool eager = false;  // lanes set to 0: no graphs, every member on its own
   std::vector<cudaStream_t> lane_stream;
   std::vector<std::vector<cudaGraphExec_t>> exec;  // [cycle position][lane]
   int cycle = 0;
@@ -120,6 +121,7 @@ void drop_graphs(fsph_ensemble * e) {
 }
 
 fsph_status set_lanes(fsph_ensemble * e, int lanes) {
+  e->eager = lanes == 0;
   lanes = std::max(1, std::min(lanes, (int)std::max<size_t>(1, e->m.size())));
   drop_graphs(e);
   while((int)e->lane_stream.size() < lanes) {
@@ -355,7 +357,7 @@ fsph_status fsph_ensemble_step(fsph_ensemble * e, int32_t nsteps) {
   bool need_wait = true;       // members' own streams have queued work
   bool graph_pending = false;  // lanes hold work the members must wait for
   for(int32_t step = 0; step < nsteps; ++step) {
-    bool all_ready = true;
+    bool all_ready = !e->eager;
     for(auto & mb : e->m)
       all_ready &= graph_ready(mb.c);
     if(!all_ready) {
@@ -430,7 +432,7 @@ fsph_status fsph_ensemble_sync(fsph_ensemble * e, int32_t * failed) {
 }
 
 fsph_status fsph_ensemble_set_lanes(fsph_ensemble * e, int32_t lanes) {
-  if(!e || lanes < 1)
+  if(!e || lanes < 0)
     return FSPH_ERR_ARG;
   ECK(cudaSetDevice(e->device));
   return set_lanes(e, lanes);

@@ -102,7 +102,7 @@ def sedov3d(n1d=128, gamma=5.0 / 3.0, eta=1.495, jitter=0.01, seed=12345,
     return s, params, meta
 
 
-def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0):
+def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0, rho_floor=1e-3):
     """n=1 polytrope: rho(r) = rho_c sin(pi r)/(pi r), R = 1, M = 1, G = 1.
 
     Radii by inverse-CDF sampling of M(r) ~ sin(pi r) - pi r cos(pi r)
@@ -110,7 +110,10 @@ def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0):
     (so the enclosed mass is M), polytropic EOS with gamma = 2 and
     K = 2 G R^2 / pi (hydrostatic equilibrium), v = 0, h from the local
     density.  The density is the analytic profile (the SPH sum recomputes it
-    in the first density pass).
+    in the first density pass).  The density that sets h is floored at
+    rho_floor * rho_c: near the surface the profile goes to zero and h with
+    it to the star's size (1e-3 leaves the outermost few particles with
+    thousands of neighbours; 1e-2 keeps every list under ~200).
     """
     rng = np.random.Generator(np.random.PCG64(seed))
     t = rng.random(n)
@@ -134,7 +137,7 @@ def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0):
     rho_c = math.pi * M / (4.0 * R**3)
     pr = np.pi * r / R
     rho = rho_c * np.where(pr > 1e-12, np.sin(pr) / np.maximum(pr, 1e-300), 1.0)
-    rho = np.maximum(rho, 1e-3 * rho_c)
+    rho = np.maximum(rho, rho_floor * rho_c)
     K = 2.0 * G * R**2 / math.pi
     m = M / n
     s["m"][:] = m

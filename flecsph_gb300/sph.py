@@ -309,12 +309,28 @@ class Ensemble:
             pass
 
 
-def capacity_for(params, n):
-    """Capacity that holds n real particles and every periodic copy: a
-    particle gets at most one copy per non-empty subset of its periodic
-    axes (faces, edges, corner), so n * 2^k with k periodic axes."""
-    k = sum(int(bool(getattr(params, f"periodic_boundary_{a}"))) for a in "xyz")
-    return n << k
+def capacity_for(params, n, state=None, margin=0.25):
+    """Capacity that holds n real particles and their periodic copies.
+
+    A particle within the halo (2.5 h_max) of the faces of k periodic axes
+    gets one copy per non-empty subset of them (faces, edges, corner):
+    2^k - 1.  Without `state` this is the bound n * 2^k; with it, the copies
+    the current positions make, plus `margin` for particles that move into
+    the halo later."""
+    axes = [a for a in range(3) if getattr(params, "periodic_boundary_" + "xyz"[a])]
+    if not axes:
+        return n
+    if state is None:
+        return n << len(axes)
+    halo = 2.5 * float(np.max(state["h"]))
+    size = [params.box_length, params.box_width, params.box_height]
+    k = np.zeros(n, np.int64)
+    for a in axes:
+        x = state["xyz"[a]]
+        hi, lo = 0.5 * size[a], -0.5 * size[a]
+        k += ((x + halo > hi) | (x - halo <= lo)).astype(np.int64)
+    copies = int(((1 << k) - 1).sum())
+    return min(n << len(axes), n + int(copies * (1.0 + margin)) + 1024)
 
 
 def host_register(arr):

@@ -327,7 +327,8 @@ fsph_status fsph_ensemble_step(fsph_ensemble * ens, int32_t nsteps);
 /* Waits for every member; the first member with a device-side error gives
  * the status and its index (else -1). */
 fsph_status fsph_ensemble_sync(fsph_ensemble * ens, int32_t * failed_member);
-/* Members are spread over `lanes` streams by particle count. */
+/* Members are spread over `lanes` streams by particle count; 0 turns the
+ * graphs off (every member steps eagerly on its own stream). */
 fsph_status fsph_ensemble_set_lanes(fsph_ensemble * ens, int32_t lanes);
 /* Times steps_per_trial steps for 1, 2, 4, 8, 16 lanes (advancing every
  * member meanwhile) and keeps the fastest. */
