@@ -284,6 +284,7 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->T.last, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.qbox, 2 * N) == cudaSuccess;
   ok &= dalloc(c, &c->T.box2, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.fbox2, 2 * N) == cudaSuccess;
   ok &= dalloc(c, &c->T.opar, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.gref, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.counter, N) == cudaSuccess;

@@ -31,10 +31,9 @@ struct DevTime {
 // First device-side error: code (fsph_status) and the particle it concerns.
 struct DevStatus {
   int code;
-  int flags;  // informational bits (FLAG_*)
+  int flags;  // reserved
   long long index;
 };
-enum { FLAG_LIST_ORDER_CHUNKED = 1 };
 
 struct Particles {
   double * f[NF];
@@ -69,6 +68,8 @@ struct Tree {
   int4 * qbox;             // per node: {lo.xyz, float bits of h_max}, {hi.xyz, 0}
                            // in the fixed-point position space of Packed::qpos
   NodeBox * box2;          // reference node box: union of [x - h/2, x + h/2]
+  float4 * fbox2;          // the same box in FP32 relative to the range's
+                           // lower corner, rounded outwards (lo, hi pairs)
   int * opar;              // particle -> binary node standing for its octree parent
   int * gref;              // particle -> its reference traversal group
   unsigned * counter;

@@ -499,6 +499,14 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       if(dim == 2)
         n2.lo[2] = n2.hi[2] = 0;
       T.box2[p] = n2;
+      float fl[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
+      for(int d = 0; d < dim; ++d) {
+        const double r0 = ord_dec(rbits[d]);
+        fl[d] = __double2float_rd(n2.lo[d] - r0);
+        fh[d] = __double2float_ru(n2.hi[d] - r0);
+      }
+      T.fbox2[2 * p] = make_float4(fl[0], fl[1], fl[2], 0.f);
+      T.fbox2[2 * p + 1] = make_float4(fh[0], fh[1], fh[2], 0.f);
     }
     __threadfence();
     p = T.parent[p];
@@ -662,30 +670,96 @@ __device__ __forceinline__ bool box_box(const double * a, const double * b,
   return !sep;
 }
 
+// FP32 versions of the two node tests, for answers that are certain.  Boxes
+// are the outward-rounded FP32 copies (fbox2) relative to the range's lower
+// corner and points are FP32 roundings of the same relative coordinates, so
+// every FP32 box face and point lies within `tol` (a few FP32 ulps of the
+// range's extent) of its FP64 value; an answer that a perturbation of that
+// size could flip returns -1 and the caller runs the FP64 test.
+__device__ __forceinline__ int box_box_f(const float4 & alo, const float4 & ahi,
+  const float4 & blo, const float4 & bhi, int dim, float tol) {
+  float g = fmaxf(fmaxf(blo.x - ahi.x, alo.x - bhi.x),
+    fmaxf(blo.y - ahi.y, alo.y - bhi.y));
+  if(dim == 3)
+    g = fmaxf(g, fmaxf(blo.z - ahi.z, alo.z - bhi.z));
+  if(g > 0.f)  // outer boxes apart: the exact boxes are apart
+    return 0;
+  if(g < -2.f * tol)  // overlap by more than both roundings on every axis
+    return 1;
+  return -1;
+}
+
+__device__ __forceinline__ int sphere_box_f(const float4 & lo,
+  const float4 & hi, float cx, float cy, float cz, float r, int dim,
+  float tol) {
+  const float dx = fmaxf(0.f, fmaxf(lo.x - cx, cx - hi.x));
+  const float dy = fmaxf(0.f, fmaxf(lo.y - cy, cy - hi.y));
+  const float dz = dim == 3 ? fmaxf(0.f, fmaxf(lo.z - cz, cz - hi.z)) : 0.f;
+  const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+  // box faces and the point each within tol per axis; 1e-6 relative covers
+  // the FP32 rounding of the distance and of r
+  const float slack = 3.5f * tol + 1e-6f * (d + r) + 3e-15f;
+  if(d + slack < r)
+    return 1;
+  if(d - slack > r)
+    return 0;
+  return -1;
+}
+
 // With varying h the reference's walk drops a candidate b of particle a
 // unless the box of b's octree parent passes both node tests against a's
 // traversal group G (tree_topology.h:323-355): box-box with G's box when G
 // is a node, and sphere-box with at least one member of G.  Neither test
-// can fail for a pair passing the predicate when every h is equal.
-__device__ bool ref_node_tests(const Tree & T, const double * X,
-  const double * Y, const double * Z, const double * H, int dim, int b,
-  int a, double xa, double ya, double za, double ha, int gnode,
-  const double * g2) {
-  const double * b2 = (const double *)&T.box2[T.opar[b]];
-  double bb[8];
-  for(int k = 0; k < 8; ++k)
-    bb[k] = b2[k];
-  if(gnode >= 0 && !box_box(bb, g2, dim))
-    return false;
-  if(sphere_box(bb, xa, ya, za, ha, dim))
+// can fail for a pair passing the predicate when every h is equal.  Each
+// test is decided in FP32 first and in FP64 (box_box, sphere_box) only when
+// the FP32 answer is not certain, so the answers are the FP64 ones.
+__device__ bool ref_node_tests_mixed(const Tree & T, const double * X,
+  const double * Y, const double * Z, const double * H, int dim, int b, int a,
+  double xa, double ya, double za, double ha, float cax, float cay, float caz,
+  float haf, int gnode, const double * g2, const float4 & glo,
+  const float4 & ghi, const double * rlo, float tol) {
+  const int ob = T.opar[b];
+  const float4 blo = T.fbox2[2 * ob], bhi = T.fbox2[2 * ob + 1];
+  const double * b2 = (const double *)&T.box2[ob];
+  if(gnode >= 0) {
+    const int r = box_box_f(blo, bhi, glo, ghi, dim, tol);
+    if(r == 0)
+      return false;
+    if(r < 0) {
+      double bb[8];
+      for(int k = 0; k < 8; ++k)
+        bb[k] = b2[k];
+      if(!box_box(bb, g2, dim))
+        return false;
+    }
+  }
+  const int s = sphere_box_f(blo, bhi, cax, cay, caz, haf, dim, tol);
+  if(s == 1)
     return true;
+  if(s < 0) {
+    double bb[8];
+    for(int k = 0; k < 8; ++k)
+      bb[k] = b2[k];
+    if(sphere_box(bb, xa, ya, za, ha, dim))
+      return true;
+  }
   if(gnode < 0)
     return false;
   for(int k = T.first[gnode]; k <= T.last[gnode]; ++k) {
     if(k == a)
       continue;
-    if(sphere_box(bb, X[k], Y[k], dim == 3 ? Z[k] : 0.0, H[k], dim))
+    const double xk = X[k], yk = Y[k], zk = dim == 3 ? Z[k] : 0.0, hk = H[k];
+    const int t = sphere_box_f(blo, bhi, (float)(xk - rlo[0]), (float)(yk - rlo[1]),
+      dim == 3 ? (float)(zk - rlo[2]) : 0.f, (float)hk, dim, tol);
+    if(t == 1)
       return true;
+    if(t < 0) {
+      double bb[8];
+      for(int q = 0; q < 8; ++q)
+        bb[q] = b2[q];
+      if(sphere_box(bb, xk, yk, zk, hk, dim))
+        return true;
+    }
   }
   return false;
 }
@@ -715,7 +789,9 @@ __device__ __forceinline__ bool box_near(int4 glo, int4 ghi, float hg,
 // above that estimate's error; only pairs inside the margin pay the FP64
 // test.  ORDERED (the FP64 path) sorts the candidates by (reference octree
 // depth, index) before filtering, so each list comes out in the order in
-// which the reference's breadth-first walk appends neighbours.
+// which the reference's breadth-first walk appends neighbours; when the
+// candidates of a group did not fit one chunk, every member's list is
+// sorted by the same key at the end.
 template<bool ORDERED>
 __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
   Tree T, Lists Ls, DevStatus * st, int dim, const unsigned long long * rbits,
@@ -754,6 +830,15 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
   const float qs0 = K.qscale[0], qs1 = K.qscale[1], qs2 = dim == 3 ? K.qscale[2] : 0.f;
   const float qmax = fmaxf(qs0, fmaxf(qs1, qs2));
   const float hglob = (float)ord_dec(rbits[7]);
+  double rlo[3] = {0.0, 0.0, 0.0};
+  float ext = 0.f;
+  for(int d = 0; d < dim; ++d) {
+    rlo[d] = ord_dec(rbits[d]);
+    ext = fmaxf(ext, (float)(ord_dec(rbits[3 + d]) - rlo[d]));
+  }
+  // FP32 boxes and points lie within a few ulps of the range's extent of
+  // their FP64 values (outward rounding of the boxes, nearest of points)
+  const float ftol = 4e-7f * ext;
   for(int g = blockIdx.x * NB_WARPS + w; g < ngroups;
       g += gridDim.x * NB_WARPS) {
     const int gf = T.group_first[g], gl = T.group_last[g];
@@ -765,13 +850,20 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
     const float haf = __int_as_float(qa.w);
     int gnode = -1;
     double g2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float4 fglo = make_float4(0.f, 0.f, 0.f, 0.f), fghi = fglo;
+    float cax = 0.f, cay = 0.f, caz = 0.f;
     if(mem && nonuni) {
       gnode = T.gref[a];
       if(gnode >= 0) {
         const double * gp = (const double *)&T.box2[gnode];
         for(int k = 0; k < 8; ++k)
           g2[k] = gp[k];
+        fglo = T.fbox2[2 * gnode];
+        fghi = T.fbox2[2 * gnode + 1];
       }
+      cax = (float)(X[a] - rlo[0]);
+      cay = (float)(Y[a] - rlo[1]);
+      caz = dim == 3 ? (float)(Z[a] - rlo[2]) : 0.f;
     }
     int4 glo = mem ? qa : make_int4(0x7fffffff, 0x7fffffff, 0x7fffffff, 0);
     int4 ghi = mem ? qa : make_int4(-1, -1, -1, 0);
@@ -892,8 +984,9 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
             return d2 <= r * r;
           };
           auto append = [&](int b) {
-            if(!nonuni || ref_node_tests(T, X, Y, Z, H, dim, b, a, xa, ya, za,
-                            ha, gnode, g2)) {
+            if(!nonuni || ref_node_tests_mixed(T, X, Y, Z, H, dim, b, a, xa, ya,
+                            za, ha, cax, cay, caz, haf, gnode, g2, fglo, fghi,
+                            rlo, ftol)) {
               if(cnt < maxnb)
                 out[32 * cnt] = b;
               ++cnt;
@@ -992,9 +1085,29 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         cnt = maxnb;
       }
       Ls.cnt[a] = cnt;
+      if(ORDERED && chunked) {
+        // the candidates came in several sorted chunks: put the whole list
+        // in (reference octree depth, index) order (Shell sort, Ciura gaps)
+        int * out = Ls.idx + list_slot(a, 0, maxnb);
+        auto key = [&](int b) {
+          return ((unsigned long long)T.edepth[b] << 32) | (unsigned)b;
+        };
+        const int gaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+        for(int gi = 0; gi < 8; ++gi) {
+          const int gap = gaps[gi];
+          for(int i = gap; i < cnt; ++i) {
+            const int v = out[32 * i];
+            const unsigned long long kv = key(v);
+            int j = i;
+            while(j >= gap && key(out[32 * (j - gap)]) > kv) {
+              out[32 * j] = out[32 * (j - gap)];
+              j -= gap;
+            }
+            out[32 * j] = v;
+          }
+        }
+      }
     }
-    if(ORDERED && chunked && lane == 0)
-      atomicOr(&st->flags, FLAG_LIST_ORDER_CHUNKED);
   }
 }
 

@@ -1,8 +1,8 @@
 """GPU (libfsph_gb300.so through the C ABI) against the golden vectors of the
 reference and against the CPU oracle.
 
-Bars: keys, sort order and range bit-exact; neighbour sets bit-exact (and the
-reference's list order where the walk did not have to chunk); every FP64
+Bars: keys, sort order and range bit-exact; neighbour lists bit-exact in the
+reference's order (FP64 mode) or as sets (mixed path); every FP64
 field within a normwise relative error of 1e-12 of the reference after each
 driver iteration (max |gpu - ref| / max |ref| per field)."""
 import numpy as np
@@ -99,3 +99,52 @@ def test_sod3d_full_size_vs_oracle(oracle_port):
         for f in DOUBLE_FIELDS:
             assert normwise(g[f], r[f]) <= FP64_TOL, (k, f)
         assert bs.time()[2] == o.time()[2]
+
+
+def _cloud(n, dim, seed, spread, base):
+    from flecsph_gb300.abi import new_state
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = new_state(n)
+    s["x"][:] = rng.random(n)
+    s["y"][:] = rng.random(n)
+    if dim == 3:
+        s["z"][:] = rng.random(n)
+    s["m"][:] = 1.0 / n
+    s["h"][:] = base * np.exp(rng.normal(0, spread, n))
+    s["rho"][:] = 1.0
+    s["u"][:] = 1.0 + rng.random(n)
+    s["P"][:] = 0.4 * s["u"]
+    s["id"][:] = rng.permutation(n)
+    return s
+
+
+# mean lists of ~35-80 neighbours; the widest h reach 1,000-3,300
+@pytest.mark.parametrize("dim,seed,spread,base,mode", [
+    (3, 1, 0.5, 0.09, 0), (3, 2, 0.6, 0.08, 1), (2, 3, 0.6, 0.05, 0),
+    (2, 4, 0.8, 0.04, 1), (3, 5, 0.2, 0.1, 1)])
+def test_variable_h_lists_vs_oracle(oracle_port, dim, seed, spread, base, mode):
+    """Strongly varying h: the reference's node tests (octree-parent boxes
+    against the traversal group, tree_topology.h:323-355) decide many pairs;
+    the GPU lists (FP32-first tests with FP64 fallback) must be the oracle's,
+    in the reference's order for FP64 mode and as sets for the mixed path."""
+    from flecsph_gb300.abi import Params
+    s = _cloud(6000 if dim == 3 else 3000, dim, seed, spread, base)
+    p = Params.defaults(dimension=dim, sph_kernel=4, sph_variable_h=1,
+                        adaptive_timestep=1, initial_dt=1e-5, max_neighbors=4096,
+                        precision_mode=mode)
+    o = oracle_port.Oracle("port", p, threads=8)
+    o.upload(s)
+    o.update_iteration()
+    ro, ri = o.neighbors()
+    bs = _bs(p, len(s["x"]))
+    bs.read_bodies(s)
+    bs.update_iteration()
+    go, gi = bs.neighbors()
+    assert np.array_equal(go, ro)
+    if mode == 0:
+        assert np.array_equal(gi, ri)
+    else:
+        for a in range(len(go) - 1):
+            assert np.array_equal(np.sort(gi[go[a]:go[a + 1]]),
+                                  np.sort(ri[ro[a]:ro[a + 1]])), a
+    bs.close()
