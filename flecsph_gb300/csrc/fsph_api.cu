@@ -308,9 +308,10 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
     ok &= dalloc(c, &c->PS.hbits, 1) == cudaSuccess;
   }
   if(p->enable_fmm) {
-    ok &= dalloc(c, &c->gnodes, N) == cudaSuccess;
-    ok &= dalloc(c, &c->gbox, 6 * N) == cudaSuccess;
-    ok &= dalloc(c, &c->gcounter, N) == cudaSuccess;
+    ok &= dalloc(c, &c->grav.gn, N) == cudaSuccess;
+    ok &= dalloc(c, &c->grav.gnf, 4 * N) == cudaSuccess;
+    ok &= dalloc(c, &c->grav.gpk, 2 * N) == cudaSuccess;
+    ok &= dalloc(c, &c->T.gmom, 10 * N) == cudaSuccess;
   }
   c->mixed = p->precision_mode == FSPH_PRECISION_MIXED;
   c->Ls.maxnb = p->max_neighbors;
@@ -801,7 +802,7 @@ fsph_status fsph_advance_time(fsph_ctx * c) {
 fsph_status fsph_gravitation(fsph_ctx * c) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
-  if(!c->gnodes) {
+  if(!c->grav.gn) {
     c->last_error = "context created without enable_fmm";
     return FSPH_ERR_STATE;
   }
@@ -810,8 +811,8 @@ fsph_status fsph_gravitation(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_GRAVITY);
-  CK(launch_gravity(L, c->P, c->pp, c->T, c->gnodes, c->gbox, c->gcounter,
-    c->p.fmm_macangle, c->p.gravity_order, c->mixed ? 1 : 0, c->d_status, c->nsm));
+  CK(launch_gravity(L, c->P, c->pp, c->T, c->grav, c->d_range, c->p.fmm_macangle,
+    c->p.gravity_order, c->mixed ? 1 : 0, c->d_status, c->nsm));
   return FSPH_OK;
 }
 

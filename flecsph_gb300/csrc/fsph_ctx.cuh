@@ -36,9 +36,7 @@ struct fsph_ctx {
   fsph::Lists Ls{};
   fsph::Packed K{};
   bool mixed = false;
-  fsph::GravNode * gnodes = nullptr;
-  double * gbox = nullptr;
-  unsigned * gcounter = nullptr;
+  fsph::GravBuffers grav{};  // allocated when enable_fmm
   // periodic boundaries: real particles hold ids [0, nreal)
   bool periodic = false;
   long long nreal = 0;

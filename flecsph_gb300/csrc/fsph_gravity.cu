@@ -8,22 +8,28 @@
 // applied through fmm_c2p, fmm.h:91-119) in a dual-tree walk; this build
 // expands every accepted cell to quadrupole order (order 1 = monopole only)
 // and walks the tree once per particle group:
-//   upward pass (FP64, k_multipoles): mass, centre of mass, traceless
+//   multipoles (FP64, k_grav_nodes): mass, centre of mass, traceless
 //     quadrupole Q_ij = sum m (3 x_i x_j - r^2 delta_ij) about it and the
-//     radius of the bounding box seen from it, children combined bottom-up;
+//     radius of the bounding box seen from it, from raw mass moments that
+//     the tree's bottom-up pass sums (children add);
 //   walk (k_gravity_walk): one warp per group of <= 32 particles; a cell is
 //     accepted when r_max < theta * d_min, d_min being the distance from
 //     its centre of mass to the group's box (so the test holds for every
 //     member); accepted cells go to a shared-memory multipole list, leaves
 //     of opened cells to a particle list; each lane then sums both lists
-//     for its particle.
+//     for its particle.  The walk itself (acceptance test, list building)
+//     runs in FP32 on copies of the nodes and particles made by the up
+//     pass, in both precisions, so both evaluate the same interaction
+//     lists; positions there are relative to the range's lower corner and
+//     split into FP32 hi + lo words, so that a difference of two of them
+//     keeps FP32 relative accuracy however close the pair.
 // The pair kernel is the reference's unsoftened Newtonian one
 // (fmm.h:37-46): phi += -G m / r, a += -G m (x_a - x_b) / r^3, skipping the
 // particle itself (fmm.h:136-137).  Results are added to g-acceleration
 // and potential (the acceleration pass zeroes them first, as
-// default_physics.h:406-407 does).  FP64 mode evaluates in FP64; the mixed
-// path evaluates in FP32 relative to the group centre with Kahan sums while
-// the multipoles stay FP64.
+// default_physics.h:406-407 does).  FP64 mode evaluates the lists in FP64
+// from the FP64 nodes and positions; the mixed path evaluates them in FP32
+// with Kahan sums (multipoles accumulated in FP64, stored in FP32).
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -32,10 +38,10 @@
 
 namespace fsph {
 
-#define GW_WARPS 4
+#define GW_WARPS 8
 #define GW_STACK 1024
-#define GW_MCAP 128
-#define GW_PCAP 256
+#define GW_MCAP 64
+#define GW_PCAP 128
 #define GFULL 0xffffffffu
 
 __device__ __forceinline__ unsigned lanemask_lt_g() {
@@ -45,84 +51,99 @@ __device__ __forceinline__ unsigned lanemask_lt_g() {
 }
 
 // ---------------------------------------------------------- up pass -----
-__global__ void k_multipoles(Particles P, int dim, Tree T, GravNode * gn,
-  double * gbox, unsigned * counter, int order) {
+__device__ __forceinline__ double ord_dec_g(unsigned long long u) {
+  return (u & 0x8000000000000000ull)
+           ? __longlong_as_double((long long)(u & 0x7fffffffffffffffull))
+           : __longlong_as_double((long long)~u);
+}
+
+__device__ __forceinline__ void split_hi_lo(double v, float & hi, float & lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// Multipoles from the raw moments the tree's bottom-up pass summed
+// (Tree::gmom, about the range centre r_c), one thread per node, no
+// dependency between nodes:
+//   M = S_0, C = r_c + S_1 / M,
+//   sum m y'_i y'_j = S_ij - M c_i c_j   (c = C - r_c, y' = x - C),
+//   Q_ij = 3 sum m y'_i y'_j - delta_ij sum m |y'|^2   (traceless).
+// The cancellation in S_ij - M c_i c_j costs ~1e-16 (|y| / node size)^2
+// relative, ~1e-10 for the smallest nodes of a 4M-particle set.  r_max is
+// the distance from C to the farthest corner of the node's position box
+// (the fixed-point box of the tree, widened by one quantisation step).
+// Every particle also gets its FP32 walk record here.
+__global__ void k_grav_nodes(Particles P, int dim, Tree T, GravBuffers G,
+  const unsigned long long * rbits, int order) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= P.n)
+  const int n = P.n;
+  if(i >= n)
     return;
-  int p = T.leaf_parent[i];
-  while(p >= 0) {
-    __threadfence();
-    if(atomicAdd(&counter[p], 1u) == 0)
-      return;
-    double M = 0, C[3] = {0, 0, 0}, lo[3] = {1e308, 1e308, 1e308},
-           hi[3] = {-1e308, -1e308, -1e308};
-    double cm[2], cc[2][3], cq[2][6];
-    const int ch[2] = {T.left[p], T.right[p]};
-    for(int c = 0; c < 2; ++c) {
-      if(ch[c] < 0) {
-        const int j = ~ch[c];
-        cm[c] = P.f[F_M][j];
-        for(int d = 0; d < 3; ++d) {
-          cc[c][d] = d < dim ? P.f[F_X + d][j] : 0.0;
-          lo[d] = fmin(lo[d], cc[c][d]);
-          hi[d] = fmax(hi[d], cc[c][d]);
-        }
-        for(int k = 0; k < 6; ++k)
-          cq[c][k] = 0.0;
-      }
-      else {
-        const GravNode * g = &gn[ch[c]];
-        cm[c] = __ldcg(&g->m);
-        for(int d = 0; d < 3; ++d) {
-          cc[c][d] = __ldcg(&g->c[d]);
-          lo[d] = fmin(lo[d], __ldcg(&gbox[6 * ch[c] + d]));
-          hi[d] = fmax(hi[d], __ldcg(&gbox[6 * ch[c] + 3 + d]));
-        }
-        for(int k = 0; k < 6; ++k)
-          cq[c][k] = __ldcg(&g->q[k]);
-      }
-      M += cm[c];
-    }
-    for(int d = 0; d < 3; ++d)
-      C[d] = (cm[0] * cc[0][d] + cm[1] * cc[1][d]) / M;
-    double Q[6] = {0, 0, 0, 0, 0, 0};
-    if(order >= 2)
-      for(int c = 0; c < 2; ++c) {
-        // parallel-axis shift of the child's quadrupole to the new centre
-        const double dx = cc[c][0] - C[0], dy = cc[c][1] - C[1], dz = cc[c][2] - C[2];
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        const double m = cm[c];
-        Q[0] += cq[c][0] + m * (3 * dx * dx - r2);
-        Q[1] += cq[c][1] + m * (3 * dy * dy - r2);
-        Q[2] += cq[c][2] + m * (3 * dz * dz - r2);
-        Q[3] += cq[c][3] + m * 3 * dx * dy;
-        Q[4] += cq[c][4] + m * 3 * dx * dz;
-        Q[5] += cq[c][5] + m * 3 * dy * dz;
-      }
-    double rmax2 = 0;
-    for(int k = 0; k < 8; ++k) {
-      const double ex = ((k & 1) ? hi[0] : lo[0]) - C[0];
-      const double ey = ((k & 2) ? hi[1] : lo[1]) - C[1];
-      const double ez = ((k & 4) ? hi[2] : lo[2]) - C[2];
-      rmax2 = fmax(rmax2, ex * ex + ey * ey + ez * ez);
-    }
-    GravNode out;
-    out.m = M;
-    for(int d = 0; d < 3; ++d)
-      out.c[d] = C[d];
-    for(int k = 0; k < 6; ++k)
-      out.q[k] = Q[k];
-    out.rmax = sqrt(rmax2);
-    out.pad = 0;
-    gn[p] = out;
-    for(int d = 0; d < 3; ++d) {
-      gbox[6 * p + d] = lo[d];
-      gbox[6 * p + 3 + d] = hi[d];
-    }
-    __threadfence();
-    p = T.parent[p];
+  double r0[3] = {0.0, 0.0, 0.0}, rc[3] = {0.0, 0.0, 0.0}, step[3] = {0.0, 0.0, 0.0};
+  for(int d = 0; d < dim; ++d) {
+    const double lo = ord_dec_g(rbits[d]), hi = ord_dec_g(rbits[3 + d]);
+    r0[d] = lo;
+    rc[d] = 0.5 * (lo + hi);
+    step[d] = (hi - lo) * (1.0 / 2147483648.0);
   }
+  {
+    // this particle for the walk: position relative to the corner, hi + lo
+    float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+    for(int d = 0; d < dim; ++d)
+      split_hi_lo(P.f[F_X + d][i] - r0[d], h[d], l[d]);
+    G.gpk[2 * i] = make_float4(h[0], h[1], h[2], (float)P.f[F_M][i]);
+    G.gpk[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+  if(i >= n - 1)
+    return;
+  const double * S = T.gmom + 10 * (size_t)i;
+  double Sv[10];
+  for(int k = 0; k < 10; ++k)
+    Sv[k] = S[k];
+  const double M = Sv[0];
+  const double iM = 1.0 / M;
+  const double c[3] = {Sv[1] * iM, Sv[2] * iM, Sv[3] * iM};
+  double Q[6] = {0, 0, 0, 0, 0, 0};
+  if(order >= 2) {
+    const double sxx = Sv[4] - M * c[0] * c[0], syy = Sv[5] - M * c[1] * c[1];
+    const double szz = Sv[6] - M * c[2] * c[2];
+    const double tr = sxx + syy + szz;
+    Q[0] = 3.0 * sxx - tr;
+    Q[1] = 3.0 * syy - tr;
+    Q[2] = 3.0 * szz - tr;
+    Q[3] = 3.0 * (Sv[7] - M * c[0] * c[1]);
+    Q[4] = 3.0 * (Sv[8] - M * c[0] * c[2]);
+    Q[5] = 3.0 * (Sv[9] - M * c[1] * c[2]);
+  }
+  GravNode out;
+  out.m = M;
+  double cr[3];  // centre relative to the corner
+  const int4 qlo = T.qbox[2 * i], qhi = T.qbox[2 * i + 1];
+  const int ql[3] = {qlo.x, qlo.y, qlo.z}, qh[3] = {qhi.x, qhi.y, qhi.z};
+  double rmax2 = 0.0;
+  for(int d = 0; d < 3; ++d) {
+    out.c[d] = d < dim ? rc[d] + c[d] : 0.0;
+    cr[d] = d < dim ? out.c[d] - r0[d] : 0.0;
+    if(d < dim) {
+      const double e = fmax((double)qh[d] * step[d] - cr[d], cr[d] - (double)ql[d] * step[d]) +
+                       step[d];
+      rmax2 += e * e;
+    }
+  }
+  for(int k = 0; k < 6; ++k)
+    out.q[k] = Q[k];
+  out.rmax = sqrt(rmax2);
+  out.pad = 0;
+  G.gn[i] = out;
+  float ch_[3] = {0.f, 0.f, 0.f}, cl_[3] = {0.f, 0.f, 0.f};
+  for(int d = 0; d < dim; ++d)
+    split_hi_lo(cr[d], ch_[d], cl_[d]);
+  // the acceptance radius rounded up, a hair wider for the FP32 tests
+  const float rf = __double2float_ru(out.rmax * (1.0 + 1e-6));
+  G.gnf[4 * i] = make_float4(ch_[0], ch_[1], ch_[2], rf);
+  G.gnf[4 * i + 1] = make_float4((float)M, cl_[0], cl_[1], cl_[2]);
+  G.gnf[4 * i + 2] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
+  G.gnf[4 * i + 3] = make_float4((float)Q[4], (float)Q[5], 0.f, 0.f);
 }
 
 // ------------------------------------------------------------ the walk --
@@ -134,51 +155,62 @@ __device__ __forceinline__ void kahan_g(R & s, R & c, R t) {
   s = u;
 }
 
+// Shared-memory list records, one broadcast 16-byte load per quarter:
+//   mixed cell     {m, c_hi} {c_lo, q0} {q1..q4} {q5, -, -, -}   64 B
+//   mixed particle {x_hi, m} {x_lo, index}                        32 B
+//   FP64 cell      {m, c} {q0..q5}  as five double2              80 B
+//   FP64 particle  {x, m} as two double2, index beside            32 B + 4
+template<bool MIXED>
+__host__ __device__ constexpr size_t gw_cell_bytes() { return MIXED ? 64 : 80; }
+
+template<bool MIXED>
+__host__ __device__ constexpr size_t gw_warp_bytes() {
+  return (size_t)GW_STACK * 4 + (size_t)GW_MCAP * gw_cell_bytes<MIXED>() +
+         (size_t)GW_PCAP * 32 + (MIXED ? 0 : (size_t)GW_PCAP * 4);
+}
+
 template<bool MIXED>
 __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
-  Tree T, const GravNode * gn, double theta, double G, int order, int dim,
+  Tree T, GravBuffers G, float theta, double Gc, int order, int dim,
   DevStatus * st) {
   typedef typename std::conditional<MIXED, float, double>::type R;
   extern __shared__ __align__(16) unsigned char gsm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // particle rows: x, y, z, m (+ the low words of x, y, z in FP32)
-  constexpr int PROWS = MIXED ? 7 : 4;
-  const size_t per_warp = (size_t)GW_STACK * 4 + (size_t)GW_MCAP * 10 * sizeof(R) +
-                          (size_t)GW_PCAP * PROWS * sizeof(R) + (size_t)GW_PCAP * 4;
-  unsigned char * base = gsm + per_warp * w;
+  unsigned char * base = gsm + gw_warp_bytes<MIXED>() * w;
   int * stack = (int *)base;
-  R * mm = (R *)(base + (size_t)GW_STACK * 4);
-  R * pl = mm + GW_MCAP * 10;
-  int * pidx = (int *)(pl + GW_PCAP * PROWS);
+  unsigned char * mrec = base + (size_t)GW_STACK * 4;
+  unsigned char * prec = mrec + (size_t)GW_MCAP * gw_cell_bytes<MIXED>();
+  int * pidx = (int *)(prec + (size_t)GW_PCAP * 32);  // FP64 only
+  float4 * mf = (float4 *)mrec;
+  float4 * pf = (float4 *)prec;
+  double2 * md = (double2 *)mrec;
+  double2 * pd = (double2 *)prec;
   const unsigned lt = lanemask_lt_g();
-  const double * X = P.f[F_X];
-  const double * Y = P.f[F_Y];
-  const double * Z = P.f[F_Z];
-  const double * Mm = P.f[F_M];
   const int ngroups = *T.ngroups;
-  const double th2 = theta * theta;
+  const float th2 = theta * theta;
   for(int g = blockIdx.x * GW_WARPS + w; g < ngroups; g += gridDim.x * GW_WARPS) {
     const int gf = T.group_first[g], gl = T.group_last[g];
     const bool mem = lane <= gl - gf;
     const int a = gf + lane;
-    double xa = mem ? X[a] : 0.0, ya = mem ? Y[a] : 0.0;
-    double za = (mem && dim == 3) ? Z[a] : 0.0;
-    double lo[3] = {mem ? xa : 1e308, mem ? ya : 1e308, mem ? za : 1e308};
-    double hi[3] = {mem ? xa : -1e308, mem ? ya : -1e308, mem ? za : -1e308};
+    float4 ah = make_float4(0.f, 0.f, 0.f, 0.f), al = ah;
+    if(mem) {
+      ah = G.gpk[2 * a];
+      al = G.gpk[2 * a + 1];
+    }
+    // the group's box (FP32, relative frame) for the acceptance test
+    float lo[3] = {mem ? ah.x : 3e38f, mem ? ah.y : 3e38f, mem ? ah.z : 3e38f};
+    float hi[3] = {mem ? ah.x : -3e38f, mem ? ah.y : -3e38f, mem ? ah.z : -3e38f};
     for(int d = 0; d < 3; ++d)
       for(int o = 16; o; o >>= 1) {
-        lo[d] = fmin(lo[d], __shfl_xor_sync(GFULL, lo[d], o));
-        hi[d] = fmax(hi[d], __shfl_xor_sync(GFULL, hi[d], o));
+        lo[d] = fminf(lo[d], __shfl_xor_sync(GFULL, lo[d], o));
+        hi[d] = fmaxf(hi[d], __shfl_xor_sync(GFULL, hi[d], o));
       }
-    const double gc[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]),
-      0.5 * (lo[2] + hi[2])};
-    // this particle relative to the group centre; in FP32 as a hi + lo pair
-    // so that the separation of a close pair keeps its relative accuracy
-    // (the FP32 rounding of each end alone would leave an absolute error of
-    // the group's size times 2^-24 in it)
-    const R ax = (R)(xa - gc[0]), ay = (R)(ya - gc[1]), az = (R)(za - gc[2]);
-    const R axl = (R)((xa - gc[0]) - (double)ax), ayl = (R)((ya - gc[1]) - (double)ay);
-    const R azl = (R)((za - gc[2]) - (double)az);
+    double xa = 0.0, ya = 0.0, za = 0.0;
+    if(!MIXED && mem) {
+      xa = P.f[F_X][a];
+      ya = P.f[F_Y][a];
+      za = dim == 3 ? P.f[F_Z][a] : 0.0;
+    }
     R sx = 0, sy = 0, sz = 0, sp = 0, cx = 0, cy = 0, cz = 0, cp = 0;
     int sptr = 1, nm = 0, np = 0;
     if(lane == 0)
@@ -194,19 +226,17 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
         sptr -= k;
         bool acc = false, open = false, leaf = false;
         int code = 0;
-        GravNode gnd;
         if(act) {
           if(node < 0)
             leaf = true;
           else {
-            gnd = gn[node];
+            const float4 c0 = G.gnf[4 * node];
             code = T.qbox[2 * node + 1].w;
-            double dd = 0;
-            for(int d = 0; d < 3; ++d) {
-              const double e = fmax(0.0, fmax(lo[d] - gnd.c[d], gnd.c[d] - hi[d]));
-              dd += e * e;
-            }
-            acc = dd > 0.0 && gnd.rmax * gnd.rmax < th2 * dd;
+            const float ex = fmaxf(0.f, fmaxf(lo[0] - c0.x, c0.x - hi[0]));
+            const float ey = fmaxf(0.f, fmaxf(lo[1] - c0.y, c0.y - hi[1]));
+            const float ez = fmaxf(0.f, fmaxf(lo[2] - c0.z, c0.z - hi[2]));
+            const float dd = ex * ex + ey * ey + ez * ez;
+            acc = dd > 0.f && c0.w * c0.w < th2 * dd;
             open = !acc;
           }
         }
@@ -228,29 +258,38 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
         sptr += npush;
         if(acc) {
           const int pos = nm + __popc(ba & lt);
-          mm[0 * GW_MCAP + pos] = (R)gnd.m;
-          mm[1 * GW_MCAP + pos] = (R)(gnd.c[0] - gc[0]);
-          mm[2 * GW_MCAP + pos] = (R)(gnd.c[1] - gc[1]);
-          mm[3 * GW_MCAP + pos] = (R)(gnd.c[2] - gc[2]);
-          for(int q = 0; q < 6; ++q)
-            mm[(4 + q) * GW_MCAP + pos] = (R)gnd.q[q];
+          if(MIXED) {
+            // gnf: {c_hi, rmax} {m, c_lo} {q0..q3} {q4, q5}
+            const float4 c0 = G.gnf[4 * node], c1 = G.gnf[4 * node + 1];
+            const float4 q0 = G.gnf[4 * node + 2], q1 = G.gnf[4 * node + 3];
+            mf[4 * pos] = make_float4(c1.x, c0.x, c0.y, c0.z);
+            mf[4 * pos + 1] = make_float4(c1.y, c1.z, c1.w, q0.x);
+            mf[4 * pos + 2] = make_float4(q0.y, q0.z, q0.w, q1.x);
+            mf[4 * pos + 3] = make_float4(q1.y, 0.f, 0.f, 0.f);
+          }
+          else {
+            const GravNode & gnd = G.gn[node];
+            md[5 * pos] = make_double2(gnd.m, gnd.c[0]);
+            md[5 * pos + 1] = make_double2(gnd.c[1], gnd.c[2]);
+            md[5 * pos + 2] = make_double2(gnd.q[0], gnd.q[1]);
+            md[5 * pos + 3] = make_double2(gnd.q[2], gnd.q[3]);
+            md[5 * pos + 4] = make_double2(gnd.q[4], gnd.q[5]);
+          }
         }
         nm += __popc(ba);
         if(leaf) {
           const int j = ~node;
           const int pos = np + __popc(bl & lt);
-          const double ex = X[j] - gc[0], ey = Y[j] - gc[1];
-          const double ez = (dim == 3 ? Z[j] : 0.0) - gc[2];
-          pl[0 * GW_PCAP + pos] = (R)ex;
-          pl[1 * GW_PCAP + pos] = (R)ey;
-          pl[2 * GW_PCAP + pos] = (R)ez;
-          pl[3 * GW_PCAP + pos] = (R)Mm[j];
           if(MIXED) {
-            pl[4 * GW_PCAP + pos] = (R)(ex - (double)(R)ex);
-            pl[5 * GW_PCAP + pos] = (R)(ey - (double)(R)ey);
-            pl[6 * GW_PCAP + pos] = (R)(ez - (double)(R)ez);
+            const float4 h = G.gpk[2 * j], l = G.gpk[2 * j + 1];
+            pf[2 * pos] = h;
+            pf[2 * pos + 1] = make_float4(l.x, l.y, l.z, __int_as_float(j));
           }
-          pidx[pos] = j;
+          else {
+            pd[2 * pos] = make_double2(P.f[F_X][j], P.f[F_Y][j]);
+            pd[2 * pos + 1] = make_double2(dim == 3 ? P.f[F_Z][j] : 0.0, P.f[F_M][j]);
+            pidx[pos] = j;
+          }
         }
         np += __popc(bl);
         __syncwarp();
@@ -259,8 +298,33 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
       const bool flush_p = np > GW_PCAP - 32 || (done && np > 0);
       if(mem && flush_m) {
         for(int k = 0; k < nm; ++k) {
-          const R m = mm[k], dx = ax - mm[GW_MCAP + k], dy = ay - mm[2 * GW_MCAP + k];
-          const R dz = az - mm[3 * GW_MCAP + k];
+          R m, dx, dy, dz, qxx, qyy, qzz, qxy, qxz, qyz;
+          if(MIXED) {
+            // (a_hi - c_hi) + (a_lo - c_lo): the hi difference keeps the
+            // digits that matter when the two are close, the lo words the
+            // rest
+            const float4 r0 = mf[4 * k], r1 = mf[4 * k + 1];
+            m = r0.x;
+            dx = (ah.x - r0.y) + (al.x - r1.x);
+            dy = (ah.y - r0.z) + (al.y - r1.y);
+            dz = (ah.z - r0.w) + (al.z - r1.z);
+            qxx = r1.w;
+            if(order >= 2) {
+              const float4 r2 = mf[4 * k + 2], r3 = mf[4 * k + 3];
+              qyy = r2.x; qzz = r2.y; qxy = r2.z; qxz = r2.w; qyz = r3.x;
+            }
+          }
+          else {
+            const double2 r0 = md[5 * k], r1 = md[5 * k + 1];
+            m = r0.x;
+            dx = xa - r0.y;
+            dy = ya - r1.x;
+            dz = za - r1.y;
+            if(order >= 2) {
+              const double2 r2 = md[5 * k + 2], r3 = md[5 * k + 3], r4 = md[5 * k + 4];
+              qxx = r2.x; qyy = r2.y; qzz = r3.x; qxy = r3.y; qxz = r4.x; qyz = r4.y;
+            }
+          }
           const R r2 = dx * dx + dy * dy + dz * dz;
           const R ir = MIXED ? (R)rsqrtf((float)r2) : (R)rsqrt((double)r2);
           const R ir2 = ir * ir;
@@ -269,9 +333,6 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
           R fx = -m * ir3 * dx, fy = -m * ir3 * dy, fz = -m * ir3 * dz;
           if(order >= 2) {
             // phi_Q = -(1/2) d.Q.d / r^5,  a_Q = Q.d / r^5 - (5/2) (d.Q.d) d / r^7
-            const R qxx = mm[4 * GW_MCAP + k], qyy = mm[5 * GW_MCAP + k];
-            const R qzz = mm[6 * GW_MCAP + k], qxy = mm[7 * GW_MCAP + k];
-            const R qxz = mm[8 * GW_MCAP + k], qyz = mm[9 * GW_MCAP + k];
             const R qdx = qxx * dx + qxy * dy + qxz * dz;
             const R qdy = qxy * dx + qyy * dy + qyz * dz;
             const R qdz = qxz * dx + qyz * dy + qzz * dz;
@@ -291,14 +352,24 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
       }
       if(mem && flush_p) {
         for(int k = 0; k < np; ++k) {
-          const int j = pidx[k];
-          R dx = ax - pl[k], dy = ay - pl[GW_PCAP + k], dz = az - pl[2 * GW_PCAP + k];
+          int j;
+          R m, dx, dy, dz;
           if(MIXED) {
-            dx += axl - pl[4 * GW_PCAP + k];
-            dy += ayl - pl[5 * GW_PCAP + k];
-            dz += azl - pl[6 * GW_PCAP + k];
+            const float4 h = pf[2 * k], l = pf[2 * k + 1];
+            j = __float_as_int(l.w);
+            m = h.w;
+            dx = (ah.x - h.x) + (al.x - l.x);
+            dy = (ah.y - h.y) + (al.y - l.y);
+            dz = (ah.z - h.z) + (al.z - l.z);
           }
-          const R m = pl[3 * GW_PCAP + k];
+          else {
+            const double2 p0 = pd[2 * k], p1 = pd[2 * k + 1];
+            j = pidx[k];
+            m = p1.y;
+            dx = xa - p0.x;
+            dy = ya - p0.y;
+            dz = za - p1.x;
+          }
           const R r2 = dx * dx + dy * dy + dz * dz;
           // the particle itself drops out (fmm.h:136-137)
           const R ir = j == a ? (R)0
@@ -320,48 +391,45 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
         break;
     }
     if(mem) {
-      const double fx = ((double)sx - (double)cx) * G;
-      const double fy = ((double)sy - (double)cy) * G;
-      const double fz = ((double)sz - (double)cz) * G;
+      const double fx = ((double)sx - (double)cx) * Gc;
+      const double fy = ((double)sy - (double)cy) * Gc;
+      const double fz = ((double)sz - (double)cz) * Gc;
       P.f[F_GAX][a] += fx;
       P.f[F_GAY][a] += fy;
       if(dim == 3)
         P.f[F_GAZ][a] += fz;
-      P.f[F_GPOT][a] += ((double)sp - (double)cp) * G;
+      P.f[F_GPOT][a] += ((double)sp - (double)cp) * Gc;
     }
   }
 }
 
 cudaError_t launch_gravity(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Tree & T, GravNode * gn, double * gbox,
-  unsigned * counter, double theta, int order, int mixed, DevStatus * st,
-  int nsm) {
+  const PhysParams & pp, const Tree & T, const GravBuffers & G,
+  const unsigned long long * rbits, double theta, int order, int mixed,
+  DevStatus * st, int nsm) {
   const int n = P.n;
   if(n < 2)  // a lone particle feels no force
     return cudaSuccess;
-  cudaMemsetAsync(counter, 0, sizeof(unsigned) * (size_t)n, L.stream);
-  k_multipoles<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, gn, gbox,
-    counter, order);
-  auto smem_of = [](size_t rs, int prows) {
-    return ((size_t)GW_STACK * 4 + (size_t)GW_MCAP * 10 * rs +
-            (size_t)GW_PCAP * prows * rs + (size_t)GW_PCAP * 4) * GW_WARPS;
-  };
-  const size_t smem = mixed ? smem_of(sizeof(float), 7) : smem_of(sizeof(double), 4);
+  k_grav_nodes<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, G, rbits, order);
+  const size_t smem = (mixed ? gw_warp_bytes<true>() : gw_warp_bytes<false>()) * GW_WARPS;
   static bool attr = false;
   if(!attr) {
     cudaFuncSetAttribute(k_gravity_walk<true>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_of(sizeof(float), 7));
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<true>() * GW_WARPS));
     cudaFuncSetAttribute(k_gravity_walk<false>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_of(sizeof(double), 4));
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<false>() * GW_WARPS));
     attr = true;
   }
-  const int blocks = nsm * 4;
+  int blocks = nsm * 4;
+  const int maxb = (n + GW_WARPS * 32 - 1) / (GW_WARPS * 32) * 4;
+  if(blocks > maxb)
+    blocks = maxb > 0 ? maxb : 1;
   if(mixed)
-    k_gravity_walk<true><<<blocks, GW_WARPS * 32, smem, L.stream>>>(P, T, gn,
-      theta, pp.G, order, pp.dim, st);
+    k_gravity_walk<true><<<blocks, GW_WARPS * 32, smem, L.stream>>>(P, T, G,
+      (float)theta, pp.G, order, pp.dim, st);
   else
-    k_gravity_walk<false><<<blocks, GW_WARPS * 32, smem, L.stream>>>(P, T, gn,
-      theta, pp.G, order, pp.dim, st);
+    k_gravity_walk<false><<<blocks, GW_WARPS * 32, smem, L.stream>>>(P, T, G,
+      (float)theta, pp.G, order, pp.dim, st);
   *L.counter += 2;
   return cudaGetLastError();
 }

@@ -77,6 +77,10 @@ struct Tree {
   int * group_first;
   int * group_last;
   int * ngroups;           // device scalar
+  double * gmom;           // with gravity only (else null): per node the raw
+                           // moments of mass about the range centre,
+                           // {m, m y_xyz, m y_x^2, m y_y^2, m y_z^2,
+                           //  m y_x y_y, m y_x y_z, m y_y y_z}
 };
 
 // Packed FP32 records of the mixed-precision path (rebuilt every step).
@@ -98,6 +102,17 @@ struct GravNode {
   double q[6];
   double rmax;
   double pad;
+};
+
+// Device buffers of the gravity pass.  gnf holds every node again in FP32
+// for the walk: {c_hi, rmax (rounded up)}, {m, c_lo}, {q0..q3}, {q4, q5},
+// c_hi + c_lo being the centre of mass relative to the range's lower corner
+// as an unevaluated FP32 sum; gpk holds every particle as {x_hi, m},
+// {x_lo} in the same frame.
+struct GravBuffers {
+  GravNode * gn;       // n nodes
+  float4 * gnf;        // 4 n
+  float4 * gpk;        // 2 n
 };
 
 struct Lists {
@@ -155,9 +170,9 @@ cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
 
 // ---- fsph_gravity.cu ----
 cudaError_t launch_gravity(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Tree & T, GravNode * gn, double * gbox,
-  unsigned * counter, double theta, int order, int mixed, DevStatus * st,
-  int nsm);
+  const PhysParams & pp, const Tree & T, const GravBuffers & G,
+  const unsigned long long * rbits, double theta, int order, int mixed,
+  DevStatus * st, int nsm);
 
 // ---- fsph_periodic.cu ----
 struct PeriodicScratch {

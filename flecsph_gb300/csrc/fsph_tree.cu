@@ -431,20 +431,59 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
 }
 
 // Bottom-up node data: the fixed-point position box and the largest h of
-// every node (what the neighbour walk prunes with), and, only when h
-// varies, the reference's FP64 box of x -/+ h/2 (compute_cofm,
-// default_physics.h:79-82,90-93) used by ref_node_tests.
+// every node (what the neighbour walk prunes with); only when h varies, the
+// reference's FP64 box of x -/+ h/2 (compute_cofm, default_physics.h:
+// 79-82,90-93) used by the reference node tests; only with gravity, the
+// node's raw mass moments (ten FP64 sums: children add, so every level
+// costs ten additions whatever the order of the multipoles built from
+// them).
 __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
   const unsigned long long * rbits) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
   const bool nonuni = rbits[6] != rbits[7];
+  double rc[3] = {0.0, 0.0, 0.0};
+  if(T.gmom)
+    for(int d = 0; d < dim; ++d)
+      rc[d] = 0.5 * (ord_dec(rbits[d]) + ord_dec(rbits[3 + d]));
   int p = T.leaf_parent[i];
   while(p >= 0) {
     __threadfence();
     if(atomicAdd(&T.counter[p], 1u) == 0)
       return;  // the sibling subtree is not finished yet
+    if(T.gmom) {
+      double S[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      const int cg[2] = {T.left[p], T.right[p]};
+      for(int c = 0; c < 2; ++c) {
+        if(cg[c] < 0) {
+          const int j = ~cg[c];
+          const double m = P.f[F_M][j];
+          double y[3] = {0.0, 0.0, 0.0};
+          for(int d = 0; d < dim; ++d)
+            y[d] = P.f[F_X + d][j] - rc[d];
+          const double my[3] = {m * y[0], m * y[1], m * y[2]};
+          S[0] += m;
+          S[1] += my[0];
+          S[2] += my[1];
+          S[3] += my[2];
+          S[4] += my[0] * y[0];
+          S[5] += my[1] * y[1];
+          S[6] += my[2] * y[2];
+          S[7] += my[0] * y[1];
+          S[8] += my[0] * y[2];
+          S[9] += my[1] * y[2];
+        }
+        else {
+          const double * cs = T.gmom + 10 * (size_t)cg[c];
+          for(int k = 0; k < 10; ++k)
+            S[k] += __ldcg(cs + k);
+        }
+      }
+      double * out = T.gmom + 10 * (size_t)p;
+      for(int k = 0; k < 10; ++k)
+        out[k] = S[k];
+    }
     int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
     int hi[3] = {-1, -1, -1};
     float hm = 0.f;
