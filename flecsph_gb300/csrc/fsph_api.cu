@@ -319,7 +319,7 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->Ls.cnt, N) == cudaSuccess;
   ok &= dalloc(c, &c->d_time, 1) == cudaSuccess;
   ok &= dalloc(c, &c->d_status, 1) == cudaSuccess;
-  ok &= dalloc(c, &c->d_cons, 8) == cudaSuccess;
+  ok &= dalloc(c, &c->d_cons, 8 * (1 + CONS_BLOCKS)) == cudaSuccess;
   if(!ok) {
     cudaGetLastError();
     return fail(FSPH_ERR_OOM);

@@ -388,13 +388,14 @@ cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t) {
 }
 
 // Conserved totals (analysis.h:56-214): mass, energy, momentum (3),
-// angular momentum (3); one block, fixed order (deterministic).
-__global__ void __launch_bounds__(512) k_conserved(Particles P, PhysParams pp,
-  double * out, long long nreal) {
-  __shared__ double part[8][512];
+// angular momentum (3).  Two passes in a fixed order (deterministic):
+// CONS_BLOCKS block partials, then one block adds them up.
+__global__ void __launch_bounds__(256) k_conserved_part(Particles P,
+  PhysParams pp, double * part_out, long long nreal) {
+  __shared__ double part[8][256];
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int D = pp.dim;
-  for(int i = threadIdx.x; i < P.n; i += 512) {
+  for(int i = blockIdx.x * 256 + threadIdx.x; i < P.n; i += gridDim.x * 256) {
     if(P.id[i] >= nreal)  // periodic copies (WALL) are not counted
       continue;
     double m = P.f[F_M][i];
@@ -415,20 +416,42 @@ __global__ void __launch_bounds__(512) k_conserved(Particles P, PhysParams pp,
   for(int k = 0; k < 8; ++k)
     part[k][threadIdx.x] = s[k];
   __syncthreads();
-  for(int o = 256; o; o >>= 1) {
+  for(int o = 128; o; o >>= 1) {
     if(threadIdx.x < o)
       for(int k = 0; k < 8; ++k)
         part[k][threadIdx.x] += part[k][threadIdx.x + o];
     __syncthreads();
   }
   if(threadIdx.x < 8)
-    out[threadIdx.x] = part[threadIdx.x][0];
+    part_out[8 + 8 * blockIdx.x + threadIdx.x] = part[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) k_conserved_final(double * buf, int nb) {
+  __shared__ double part[8][256];
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for(int b = threadIdx.x; b < nb; b += 256)
+    for(int k = 0; k < 8; ++k)
+      s[k] += buf[8 + 8 * b + k];
+  for(int k = 0; k < 8; ++k)
+    part[k][threadIdx.x] = s[k];
+  __syncthreads();
+  for(int o = 128; o; o >>= 1) {
+    if(threadIdx.x < o)
+      for(int k = 0; k < 8; ++k)
+        part[k][threadIdx.x] += part[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x < 8)
+    buf[threadIdx.x] = part[threadIdx.x][0];
 }
 
 cudaError_t launch_conserved(const Launch & L, const Particles & P,
   const PhysParams & pp, double * out8, long long nreal) {
-  k_conserved<<<1, 512, 0, L.stream>>>(P, pp, out8, nreal);
-  *L.counter += 1;
+  // out8 holds 8 totals followed by 8 * CONS_BLOCKS partials
+  const int nb = P.n < 256 * CONS_BLOCKS ? (P.n + 255) / 256 : CONS_BLOCKS;
+  k_conserved_part<<<nb > 0 ? nb : 1, 256, 0, L.stream>>>(P, pp, out8, nreal);
+  k_conserved_final<<<1, 256, 0, L.stream>>>(out8, nb > 0 ? nb : 1);
+  *L.counter += 2;
   return cudaGetLastError();
 }
 

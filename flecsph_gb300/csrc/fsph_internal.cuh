@@ -223,6 +223,8 @@ cudaError_t launch_set_adaptive_timestep(const Launch & L,
 cudaError_t launch_advance_time(const Launch & L, const PhysParams & pp,
   DevTime * t);
 cudaError_t launch_hsum(const Launch & L, const Particles & P, DevTime * t);
+#define CONS_BLOCKS 1024
+// out8: 8 * (1 + CONS_BLOCKS) doubles; the totals land in the first 8
 cudaError_t launch_conserved(const Launch & L, const Particles & P,
   const PhysParams & pp, double * out8, long long nreal);
 

@@ -148,3 +148,28 @@ def test_variable_h_lists_vs_oracle(oracle_port, dim, seed, spread, base, mode):
             assert np.array_equal(np.sort(gi[go[a]:go[a + 1]]),
                                   np.sort(ri[ro[a]:ro[a + 1]])), a
     bs.close()
+
+
+def test_conserved_sums_vs_numpy():
+    """analysis.h:56-214 totals (mass, energy, momentum, angular momentum)
+    against numpy sums of the downloaded state."""
+    from flecsph_gb300 import setups
+    s, p, meta = setups.sedov3d(24)
+    bs = _bs(p, meta["n"])
+    bs.read_bodies(s)
+    for _ in range(2):
+        bs.step()
+    st = bs.download()
+    c = bs.conserved()
+    bs.close()
+    m = st["m"]
+    v = np.stack([st["vx"], st["vy"], st["vz"]], 1)
+    x = np.stack([st["x"], st["y"], st["z"]], 1)
+    e = (m * st["e"]).sum() + 0.5 * (m * st["gpot"]).sum()
+    mom = (m[:, None] * v).sum(0)
+    L = (m[:, None] * np.cross(x, v)).sum(0)
+    assert abs(c["mass"] - m.sum()) <= 1e-13 * m.sum()
+    assert abs(c["energy"] - e) <= 1e-12 * abs(e)
+    scale = (m[:, None] * np.abs(v)).sum()
+    assert np.abs(np.array(c["momentum"]) - mom).max() <= 1e-12 * scale
+    assert np.abs(np.array(c["angular_momentum"]) - L).max() <= 1e-12 * scale
