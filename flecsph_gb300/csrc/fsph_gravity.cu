@@ -156,12 +156,13 @@ __device__ __forceinline__ void kahan_g(R & s, R & c, R t) {
 }
 
 // Shared-memory list records, one broadcast 16-byte load per quarter:
-//   mixed cell     {m, c_hi} {c_lo, q0} {q1..q4} {q5, -, -, -}   64 B
+//   mixed cell     {m, c - g} {q0..q3} {q4, q5, -, -}             48 B
+//                  (g: the group's reference point, see the walk)
 //   mixed particle {x_hi, m} {x_lo, index}                        32 B
 //   FP64 cell      {m, c} {q0..q5}  as five double2              80 B
 //   FP64 particle  {x, m} as two double2, index beside            32 B + 4
 template<bool MIXED>
-__host__ __device__ constexpr size_t gw_cell_bytes() { return MIXED ? 64 : 80; }
+__host__ __device__ constexpr size_t gw_cell_bytes() { return MIXED ? 48 : 80; }
 
 template<bool MIXED>
 __host__ __device__ constexpr size_t gw_warp_bytes() {
@@ -205,6 +206,16 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
         lo[d] = fminf(lo[d], __shfl_xor_sync(GFULL, lo[d], o));
         hi[d] = fmaxf(hi[d], __shfl_xor_sync(GFULL, hi[d], o));
       }
+    // mixed: positions relative to the first member (the group's reference
+    // point), from the hi + lo words; cells entering the list get the same
+    // frame once per group, so a cell term needs one subtraction per axis
+    const float rh[3] = {__shfl_sync(GFULL, ah.x, 0), __shfl_sync(GFULL, ah.y, 0),
+      __shfl_sync(GFULL, ah.z, 0)};
+    const float rl[3] = {__shfl_sync(GFULL, al.x, 0), __shfl_sync(GFULL, al.y, 0),
+      __shfl_sync(GFULL, al.z, 0)};
+    const float rx = (ah.x - rh[0]) + (al.x - rl[0]);
+    const float ry = (ah.y - rh[1]) + (al.y - rl[1]);
+    const float rz = (ah.z - rh[2]) + (al.z - rl[2]);
     double xa = 0.0, ya = 0.0, za = 0.0;
     if(!MIXED && mem) {
       xa = P.f[F_X][a];
@@ -259,13 +270,14 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
         if(acc) {
           const int pos = nm + __popc(ba & lt);
           if(MIXED) {
-            // gnf: {c_hi, rmax} {m, c_lo} {q0..q3} {q4, q5}
+            // gnf: {c_hi, rmax} {m, c_lo} {q0..q3} {q4, q5}; stored as
+            // {m, centre - group reference} {q0..q3} {q4, q5}
             const float4 c0 = G.gnf[4 * node], c1 = G.gnf[4 * node + 1];
             const float4 q0 = G.gnf[4 * node + 2], q1 = G.gnf[4 * node + 3];
-            mf[4 * pos] = make_float4(c1.x, c0.x, c0.y, c0.z);
-            mf[4 * pos + 1] = make_float4(c1.y, c1.z, c1.w, q0.x);
-            mf[4 * pos + 2] = make_float4(q0.y, q0.z, q0.w, q1.x);
-            mf[4 * pos + 3] = make_float4(q1.y, 0.f, 0.f, 0.f);
+            mf[3 * pos] = make_float4(c1.x, (c0.x - rh[0]) + (c1.y - rl[0]),
+              (c0.y - rh[1]) + (c1.z - rl[1]), (c0.z - rh[2]) + (c1.w - rl[2]));
+            mf[3 * pos + 1] = q0;
+            mf[3 * pos + 2] = make_float4(q1.x, q1.y, 0.f, 0.f);
           }
           else {
             const GravNode & gnd = G.gn[node];
@@ -297,21 +309,20 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
       const bool flush_m = nm > GW_MCAP - 32 || (done && nm > 0);
       const bool flush_p = np > GW_PCAP - 32 || (done && np > 0);
       if(mem && flush_m) {
+        // plain sums over one flush (<= GW_MCAP terms), compensated into the
+        // totals at its end
+        R px = 0, py = 0, pz = 0, pp = 0;
         for(int k = 0; k < nm; ++k) {
           R m, dx, dy, dz, qxx, qyy, qzz, qxy, qxz, qyz;
           if(MIXED) {
-            // (a_hi - c_hi) + (a_lo - c_lo): the hi difference keeps the
-            // digits that matter when the two are close, the lo words the
-            // rest
-            const float4 r0 = mf[4 * k], r1 = mf[4 * k + 1];
+            const float4 r0 = mf[3 * k];
             m = r0.x;
-            dx = (ah.x - r0.y) + (al.x - r1.x);
-            dy = (ah.y - r0.z) + (al.y - r1.y);
-            dz = (ah.z - r0.w) + (al.z - r1.z);
-            qxx = r1.w;
+            dx = rx - r0.y;
+            dy = ry - r0.z;
+            dz = rz - r0.w;
             if(order >= 2) {
-              const float4 r2 = mf[4 * k + 2], r3 = mf[4 * k + 3];
-              qyy = r2.x; qzz = r2.y; qxy = r2.z; qxz = r2.w; qyz = r3.x;
+              const float4 r1 = mf[3 * k + 1], r2 = mf[3 * k + 2];
+              qxx = r1.x; qyy = r1.y; qzz = r1.z; qxy = r1.w; qxz = r2.x; qyz = r2.y;
             }
           }
           else {
@@ -344,13 +355,18 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
             fy += qdy * ir5 - (R)2.5 * dqd * ir7 * dy;
             fz += qdz * ir5 - (R)2.5 * dqd * ir7 * dz;
           }
-          kahan_g(sx, cx, fx);
-          kahan_g(sy, cy, fy);
-          kahan_g(sz, cz, fz);
-          kahan_g(sp, cp, phi);
+          px += fx;
+          py += fy;
+          pz += fz;
+          pp += phi;
         }
+        kahan_g(sx, cx, px);
+        kahan_g(sy, cy, py);
+        kahan_g(sz, cz, pz);
+        kahan_g(sp, cp, pp);
       }
       if(mem && flush_p) {
+        R px = 0, py = 0, pz = 0, pp = 0;
         for(int k = 0; k < np; ++k) {
           int j;
           R m, dx, dy, dz;
@@ -376,11 +392,15 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
                               : (MIXED ? (R)rsqrtf((float)r2) : (R)rsqrt((double)r2));
           const R w = m * ir;
           const R w3 = w * ir * ir;
-          kahan_g(sx, cx, -w3 * dx);
-          kahan_g(sy, cy, -w3 * dy);
-          kahan_g(sz, cz, -w3 * dz);
-          kahan_g(sp, cp, -w);
+          px -= w3 * dx;
+          py -= w3 * dy;
+          pz -= w3 * dz;
+          pp -= w;
         }
+        kahan_g(sx, cx, px);
+        kahan_g(sy, cy, py);
+        kahan_g(sz, cz, pz);
+        kahan_g(sp, cp, pp);
       }
       __syncwarp();
       if(flush_m)

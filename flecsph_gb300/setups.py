@@ -109,7 +109,8 @@ def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0, rho_floor=1e
     (bisection in FP64), isotropic directions, m = M/n, rho_c = pi M/(4 R^3)
     (so the enclosed mass is M), polytropic EOS with gamma = 2 and
     K = 2 G R^2 / pi (hydrostatic equilibrium), v = 0, h from the local
-    density.  The density is the analytic profile (the SPH sum recomputes it
+    density; internal energy evolved by du/dt (thermokinetic off, as the
+    reference's self-gravity parfile data/collapse_nx10.par has it).  The density is the analytic profile (the SPH sum recomputes it
     in the first density pass).  The density that sets h is floored at
     rho_floor * rho_c: near the surface the profile goes to zero and h with
     it to the star's size (1e-3 leaves the outermost few particles with
@@ -150,7 +151,7 @@ def polytrope3d(n=1 << 22, seed=2024, eta=1.2, G=1.0, R=1.0, M=1.0, rho_floor=1e
                              eos_type=EOS_POLYTROPIC, poly_gamma=2.0, sph_eta=eta,
                              enable_fmm=1, fmm_macangle=0.5, gravitational_constant=G,
                              gravity_order=2, adaptive_timestep=1,
-                             initial_dt=1.0e-6)
+                             initial_dt=1.0e-6, thermokinetic_formulation=0)
     meta = dict(problem="polytrope3d", n=n, seed=seed, K=K, rho_c=rho_c, eta=eta)
     return s, params, meta
 

@@ -39,6 +39,7 @@ def cases():
     s, p, m = setups.polytrope3d(3000)
     p.enable_fmm = 0
     p.sph_variable_h = 1
+    p.thermokinetic_formulation = 1
     yield "polytrope3d_varh_3000", s, p, 2
     s, p, m = setups.sod3d(40, 10, 10)
     p.sph_kernel = KERNEL_WENDLAND_C4
