@@ -49,6 +49,10 @@ sys.path.insert(0, ROOT)
 # per neighbour pair for the pair passes, compulsory HBM bytes for the rest.
 FLOPS_PAIR = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
 HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
+# DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) for kernels whose traffic grows with the particle
+# count: profiles/k_neighbors_mixed_sedov3d_64.md (148.2 MB / 262,144)
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 565.0}
 
 
 def work_model(phase, nb, mixed):
@@ -496,7 +500,11 @@ def gpu_arm(args):
     roof = dict(per_phase.get(top, {"bound": "hbm", "achieved": None,
                                     "peak": HBM_PEAK, "unit": "GB/s", "frac": None}))
     roof["kernel"] = top
-    roof["traffic"] = None
+    tpp = MEASURED_TRAFFIC_PER_PARTICLE.get(top)
+    roof["traffic"] = tpp * head["ntot"] if (tpp and mixed_run) else None
+    if roof["traffic"] is not None:
+        roof["traffic_source"] = ("ncu dram bytes of a 64^3 capture, per particle, "
+                                  "scaled to this launch")
     roof["peak_source"] = ("MEASURED_PEAKS.json hbm_gbs" if roof.get("bound") == "hbm" else
                            "in-repo FMA-chain probe (fsph_measure_peak), measured this run")
     line = {
