@@ -314,8 +314,8 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
     ok &= dalloc(c, &c->T.gmom, 10 * N) == cudaSuccess;
   }
   c->mixed = p->precision_mode == FSPH_PRECISION_MIXED;
-  c->Ls.maxnb = p->max_neighbors;
-  ok &= dalloc(c, &c->Ls.idx, Npad * (size_t)p->max_neighbors) == cudaSuccess;
+  c->Ls.maxnb = (p->max_neighbors + 3) & ~3;  // whole chunks of four slots
+  ok &= dalloc(c, &c->Ls.idx, Npad * (size_t)c->Ls.maxnb) == cudaSuccess;
   ok &= dalloc(c, &c->Ls.cnt, N) == cudaSuccess;
   ok &= dalloc(c, &c->d_time, 1) == cudaSuccess;
   ok &= dalloc(c, &c->d_status, 1) == cudaSuccess;

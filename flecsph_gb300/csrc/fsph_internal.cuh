@@ -115,15 +115,25 @@ struct GravBuffers {
   float4 * gpk;        // 2 n
 };
 
+// Neighbour lists, interleaved by warp in chunks of four slots:
+// [(i>>5)][slot/4][i&31][slot%4], so a lane reads four slots with one
+// 16-byte load and a warp reads 512 contiguous bytes.  maxnb is a multiple
+// of 4; the slots past a list's end in its last chunk hold the particle
+// itself (a zero-weight pair for every pass but the density, which masks
+// them).
 struct Lists {
-  int * idx;   // interleaved: [(i>>5)][slot][i&31]
+  int * idx;
   int * cnt;
   int maxnb;
 };
 
 __host__ __device__ inline size_t list_slot(int i, int j, int maxnb) {
-  return ((size_t)(i >> 5) * (size_t)maxnb + (size_t)j) * 32u + (size_t)(i & 31);
+  return ((size_t)(i >> 5) * (size_t)maxnb + (size_t)(j & ~3)) * 32u +
+         (size_t)(i & 31) * 4u + (size_t)(j & 3);
 }
+
+// offset of slot j from slot 0 of the same particle
+__host__ __device__ inline int slot_off(int j) { return ((j & ~3) << 5) | (j & 3); }
 
 // Kernel launch helpers (host).  Each translation unit exports plain host
 // functions; the API layer strings them together on the context stream.

@@ -184,15 +184,20 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
   const int cnt = Ls.cnt[a];
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   float sum = 0.f, comp = 0.f;
-#pragma unroll 4
-  for(int j = 0; j < cnt; ++j) {
-    const int b = lp[32 * j];
-    const int4 qb = Kp.qpos[b];
-    const float mb = Kp.vhm[b].w;
-    const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = 1.0f / hab;
-    kahan(sum, comp, mb * wfun<D, K>(sqrtf(g.r2), hab, ih));
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    // four slots per 16-byte load; padding slots hold a itself
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const int4 qb = Kp.qpos[b];
+      const float mb = Kp.vhm[b].w;
+      const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
+      const float hab = 0.5f * (ha + __int_as_float(qb.w));
+      const float ih = 1.0f / hab;
+      const float w = mb * wfun<D, K>(sqrtf(g.r2), hab, ih);
+      kahan(sum, comp, j0 + u < cnt ? w : 0.f);
+    }
   }
   const double rho = (double)sum - (double)comp;
   if(!(rho > 0)) {
@@ -246,18 +251,22 @@ __global__ void __launch_bounds__(MIX_THREADS) k_vsig_mixed(Particles P,
   const int cnt = Ls.cnt[a];
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   float vsig = 0.f;
-#pragma unroll 4
-  for(int j = 0; j < cnt; ++j) {
-    const int b = lp[32 * j];
-    const PairGeom g = geom<D>(qa, Kp.qpos[b], s0, s1, s2);
-    const float4 vb = Kp.vel[b];
-    const float4 tb = Kp.thermo[b];
-    const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
-                         (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
-    const float cb = b > a ? tb.z : tb.w;
-    // the self pair and coincident pairs are NaN in the reference and drop out
-    const float cand = fmaxf(ca, cb) - fminf(dotv, 0.f);
-    vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    // four slots per 16-byte load; padding slots hold a itself
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const PairGeom g = geom<D>(qa, Kp.qpos[b], s0, s1, s2);
+      const float4 vb = Kp.vel[b];
+      const float4 tb = Kp.thermo[b];
+      const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
+                           (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
+      const float cb = b > a ? tb.z : tb.w;
+      // the self pair and coincident pairs are NaN in the reference and drop out
+      const float cand = fmaxf(ca, cb) - fminf(dotv, 0.f);
+      vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
+    }
   }
   P.f[F_VSIG][a] = (double)vsig;
 }
@@ -288,36 +297,40 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   // The self pair and coincident pairs add exactly zero (x_ab = 0, mu = 0),
   // as the reference's m_b = 0 makes them; the loop needs no branch.
-#pragma unroll 2
-  for(int j = 0; j < cnt; ++j) {
-    const int b = lp[32 * j];
-    const int4 qb = Kp.qpos[b];
-    const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = 1.0f / hab;
-    const float r = sqrtf(g.r2);
-    const float f = gfac<D, K>(r, hab, ih);
-    const float4 vhb = Kp.vhm[b];
-    const float4 tb = Kp.thermo[b];
-    const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
-                       (vha.z - vhb.z) * g.dz;
-    const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-    const float rho_ab = 0.5f * (ta.x + tb.x);
-    const float c_ab = 0.5f * (ta.z + tb.z);
-    const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
-    const float sc = -vhb.w * (ta.y + tb.y + Pi) * f;
-    if(VSIG) {
-      const float4 vb = Kp.vel[b];
-      const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
-                           (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
-      const float cb = b > a ? tb.z : tb.w;
-      const float cand = fmaxf(ta.z, cb) - fminf(dotv, 0.f);
-      vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    // four slots per 16-byte load; padding slots hold a itself
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const int4 qb = Kp.qpos[b];
+      const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
+      const float hab = 0.5f * (ha + __int_as_float(qb.w));
+      const float ih = 1.0f / hab;
+      const float r = sqrtf(g.r2);
+      const float f = gfac<D, K>(r, hab, ih);
+      const float4 vhb = Kp.vhm[b];
+      const float4 tb = Kp.thermo[b];
+      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
+                         (vha.z - vhb.z) * g.dz;
+      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float rho_ab = 0.5f * (ta.x + tb.x);
+      const float c_ab = 0.5f * (ta.z + tb.z);
+      const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
+      const float sc = -vhb.w * (ta.y + tb.y + Pi) * f;
+      if(VSIG) {
+        const float4 vb = Kp.vel[b];
+        const float dotv = ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
+                             (va.z - vb.z) * g.dz) * rsqrtf(g.r2);
+        const float cb = b > a ? tb.z : tb.w;
+        const float cand = fmaxf(ta.z, cb) - fminf(dotv, 0.f);
+        vsig = fmaxf(vsig, (b != a && g.r2 > 0.f) ? cand : 0.f);
+      }
+      kahan(ax, cx, g.dx * sc);
+      kahan(ay, cy, g.dy * sc);
+      if(D == 3)
+        kahan(az, cz, g.dz * sc);
     }
-    kahan(ax, cx, g.dx * sc);
-    kahan(ay, cy, g.dy * sc);
-    if(D == 3)
-      kahan(az, cz, g.dz * sc);
   }
   const double acc[3] = {(double)ax - (double)cx, (double)ay - (double)cy,
     D == 3 ? (double)az - (double)cz : 0.0};
@@ -354,27 +367,31 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
   const int cnt = Ls.cnt[a];
   float dp = 0.f, cp = 0.f, dv = 0.f, cv = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
-#pragma unroll 2
-  for(int j = 0; j < cnt; ++j) {
-    const int b = lp[32 * j];
-    const int4 qb = Kp.qpos[b];
-    const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = 1.0f / hab;
-    const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
-    const float4 vhb = Kp.vhm[b];
-    const float4 vb = Kp.vel[b];
-    const float4 tb = Kp.thermo[b];
-    const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
-                       (vha.z - vhb.z) * g.dz;
-    const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-    const float rho_ab = 0.5f * (ta.x + tb.x);
-    const float c_ab = 0.5f * (ta.z + tb.z);
-    const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
-    const float vdw = f * ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
-                           (va.z - vb.z) * g.dz);
-    kahan(dp, cp, vhb.w * vdw);
-    kahan(dv, cv, vhb.w * vdw * Pi);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    // four slots per 16-byte load; padding slots hold a itself
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const int4 qb = Kp.qpos[b];
+      const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
+      const float hab = 0.5f * (ha + __int_as_float(qb.w));
+      const float ih = 1.0f / hab;
+      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
+      const float4 vhb = Kp.vhm[b];
+      const float4 vb = Kp.vel[b];
+      const float4 tb = Kp.thermo[b];
+      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
+                         (vha.z - vhb.z) * g.dz;
+      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float rho_ab = 0.5f * (ta.x + tb.x);
+      const float c_ab = 0.5f * (ta.z + tb.z);
+      const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
+      const float vdw = f * ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
+                             (va.z - vb.z) * g.dz);
+      kahan(dp, cp, vhb.w * vdw);
+      kahan(dv, cv, vhb.w * vdw * Pi);
+    }
   }
   const double sp = (double)dp - (double)cp, sv = (double)dv - (double)cv;
   const double rho_a = P.f[F_RHO][a];
@@ -398,26 +415,30 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
   const int cnt = Ls.cnt[a];
   float sum = 0.f, comp = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
-#pragma unroll 2
-  for(int j = 0; j < cnt; ++j) {
-    const int b = lp[32 * j];
-    const int4 qb = Kp.qpos[b];
-    const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
-    const float hab = 0.5f * (ha + __int_as_float(qb.w));
-    const float ih = 1.0f / hab;
-    const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
-    const float4 vhb = Kp.vhm[b];
-    const float4 vb = Kp.vel[b];
-    const float4 tb = Kp.thermo[b];
-    const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
-                       (vha.z - vhb.z) * g.dz;
-    const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-    const float rho_ab = 0.5f * (ta.x + tb.x);
-    const float c_ab = 0.5f * (ta.z + tb.z);
-    const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
-    const float vad = f * (va.x * g.dx + va.y * g.dy + va.z * g.dz);
-    const float vbd = f * (vb.x * g.dx + vb.y * g.dy + vb.z * g.dz);
-    kahan(sum, comp, vhb.w * (ta.y * vbd + vad * tb.y + 0.5f * Pi * (vbd + vad)));
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    // four slots per 16-byte load; padding slots hold a itself
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const int4 qb = Kp.qpos[b];
+      const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
+      const float hab = 0.5f * (ha + __int_as_float(qb.w));
+      const float ih = 1.0f / hab;
+      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
+      const float4 vhb = Kp.vhm[b];
+      const float4 vb = Kp.vel[b];
+      const float4 tb = Kp.thermo[b];
+      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
+                         (vha.z - vhb.z) * g.dz;
+      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float rho_ab = 0.5f * (ta.x + tb.x);
+      const float c_ab = 0.5f * (ta.z + tb.z);
+      const float Pi = (-alpha * c_ab + beta * mu) * mu / rho_ab;
+      const float vad = f * (va.x * g.dx + va.y * g.dy + va.z * g.dz);
+      const float vbd = f * (vb.x * g.dx + vb.y * g.dy + vb.z * g.dz);
+      kahan(sum, comp, vhb.w * (ta.y * vbd + vad * tb.y + 0.5f * Pi * (vbd + vad)));
+    }
   }
   double gv = 0;
   for(int d = 0; d < D; ++d)

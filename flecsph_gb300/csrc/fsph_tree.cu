@@ -642,7 +642,9 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 #ifndef NB_WARPS
 #define NB_WARPS 8
 #endif
+#ifndef NB_STACK
 #define NB_STACK 1024
+#endif
 #define NB_CAND_ORDERED 2048
 #ifndef NB_CAND
 #define NB_CAND 512
@@ -1027,7 +1029,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
                             za, ha, cax, cay, caz, haf, gnode, g2, fglo, fghi,
                             rlo, ftol)) {
               if(cnt < maxnb)
-                out[32 * cnt] = b;
+                out[slot_off(cnt)] = b;
               ++cnt;
             }
           };
@@ -1074,12 +1076,12 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
                 in1 = decide(t.y, mg, id.y);
               if(in0) {
                 if(cnt < maxnb)
-                  out[32 * cnt] = id.x;
+                  out[slot_off(cnt)] = id.x;
                 ++cnt;
               }
               if(in1) {
                 if(cnt < maxnb)
-                  out[32 * cnt] = id.y;
+                  out[slot_off(cnt)] = id.y;
                 ++cnt;
               }
             }
@@ -1124,6 +1126,12 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         cnt = maxnb;
       }
       Ls.cnt[a] = cnt;
+      {
+        // pad the last chunk of four with the particle itself
+        int * o = Ls.idx + list_slot(a, 0, maxnb);
+        for(int k = cnt; k < ((cnt + 3) & ~3); ++k)
+          o[slot_off(k)] = a;
+      }
       if(ORDERED && chunked) {
         // the candidates came in several sorted chunks: put the whole list
         // in (reference octree depth, index) order (Shell sort, Ciura gaps)
@@ -1135,14 +1143,14 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         for(int gi = 0; gi < 8; ++gi) {
           const int gap = gaps[gi];
           for(int i = gap; i < cnt; ++i) {
-            const int v = out[32 * i];
+            const int v = out[slot_off(i)];
             const unsigned long long kv = key(v);
             int j = i;
-            while(j >= gap && key(out[32 * (j - gap)]) > kv) {
-              out[32 * j] = out[32 * (j - gap)];
+            while(j >= gap && key(out[slot_off(j - gap)]) > kv) {
+              out[slot_off(j)] = out[slot_off(j - gap)];
               j -= gap;
             }
-            out[32 * j] = v;
+            out[slot_off(j)] = v;
           }
         }
       }
