@@ -24,6 +24,8 @@ KERNEL_WENDLAND_C2 = 2
 KERNEL_WENDLAND_C4 = 3
 KERNEL_WENDLAND_C6 = 4
 EOS_IDEAL = 0
+VISC_CONSTANT = 0
+VISC_CULLEN = 1
 EOS_POLYTROPIC = 1
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -82,6 +84,10 @@ class Params(C.Structure):
         ("precision_mode", C.c_int32),
         ("max_neighbors", C.c_int32),
         ("gravity_order", C.c_int32),
+        ("reserved_pad", C.c_int32),
+        ("sph_viscosity_alpha_max", C.c_double),
+        ("sph_viscosity_l", C.c_double),
+        ("sph_viscosity_delta", C.c_double),
         ("reserved", C.c_int32 * 8),
     ]
 
@@ -117,6 +123,9 @@ class Params(C.Structure):
         p.precision_mode = PRECISION_FP64
         p.max_neighbors = 256
         p.gravity_order = 2
+        p.sph_viscosity_alpha_max = 1.0
+        p.sph_viscosity_l = 0.05
+        p.sph_viscosity_delta = 1.0
         for k, v in kw.items():
             if not hasattr(p, k):
                 raise AttributeError(k)
@@ -126,7 +135,7 @@ class Params(C.Structure):
     def as_dict(self):
         out = {}
         for name, _ in self._fields_:
-            if name == "reserved":
+            if name in ("reserved", "reserved_pad"):
                 continue
             out[name] = getattr(self, name)
         return out
@@ -147,6 +156,7 @@ class SoAView(C.Structure):
         ("gpot", _DP), ("m", _DP), ("h", _DP), ("rho", _DP), ("P", _DP),
         ("cs", _DP), ("u", _DP), ("e", _DP), ("dudt", _DP), ("dedt", _DP),
         ("K", _DP), ("alpha", _DP), ("vsig", _DP), ("dt", _DP),
+        ("divv", _DP), ("ddivvdt", _DP),
         ("id", C.POINTER(C.c_int64)),
         ("key", C.POINTER(C.c_uint64)),
     ]
@@ -162,7 +172,7 @@ class Conserved(C.Structure):
 DOUBLE_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "vhx", "vhy", "vhz",
                  "ax", "ay", "az", "gax", "gay", "gaz", "gpot", "m", "h",
                  "rho", "P", "cs", "u", "e", "dudt", "dedt", "K", "alpha",
-                 "vsig", "dt"]
+                 "vsig", "dt", "divv", "ddivvdt"]
 
 
 def new_state(n):

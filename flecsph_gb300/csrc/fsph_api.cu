@@ -91,6 +91,10 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->alpha = p->sph_viscosity_alpha;
   pp->beta = p->sph_viscosity_beta;
   pp->eps = p->sph_viscosity_epsilon;
+  pp->cullen = p->sph_viscosity == FSPH_VISC_CULLEN;
+  pp->alpha_max = p->sph_viscosity_alpha_max;
+  pp->visc_l = p->sph_viscosity_l;
+  pp->visc_delta = p->sph_viscosity_delta;
   pp->cfl = p->timestep_cfl_factor;
   pp->out_screen_dt = p->out_screen_dt;
   pp->out_scalar_dt = p->out_scalar_dt;
@@ -132,8 +136,12 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "eos_type not implemented";
     return false;
   }
-  if(p->sph_viscosity != FSPH_VISC_CONSTANT) {
-    *why = "only visc_constant";
+  if(p->sph_viscosity != FSPH_VISC_CONSTANT && p->sph_viscosity != FSPH_VISC_CULLEN) {
+    *why = "sph_viscosity must be visc_constant or visc_cullen";
+    return false;
+  }
+  if(p->sph_viscosity == FSPH_VISC_CULLEN && p->precision_mode != FSPH_PRECISION_FP64) {
+    *why = "visc_cullen runs in the FP64 mode";
     return false;
   }
   if(p->relaxation_steps != 0) {
@@ -199,6 +207,9 @@ void fsph_params_default(fsph_params * p) {
   p->precision_mode = FSPH_PRECISION_FP64;
   p->max_neighbors = 256;
   p->gravity_order = 2;
+  p->sph_viscosity_alpha_max = 1.0;
+  p->sph_viscosity_l = 0.05;
+  p->sph_viscosity_delta = 1.0;
 }
 
 int32_t fsph_abi_version(void) { return FSPH_ABI_VERSION; }
@@ -377,7 +388,7 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
     v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
     v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
-    v->vsig, v->dt};
+    v->vsig, v->dt, v->divv, v->ddivvdt};
   for(int k = 0; k < NF; ++k) {
     if(src[k])
       CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
@@ -409,7 +420,7 @@ fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
   const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
     v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
     v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
-    v->vsig, v->dt};
+    v->vsig, v->dt, v->divv, v->ddivvdt};
   for(int k = 0; k < NF; ++k)
     if(src[k])
       CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
@@ -491,7 +502,7 @@ fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
   double * dst[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx, v->vhy,
     v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m, v->h,
     v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha, v->vsig,
-    v->dt};
+    v->dt, v->divv, v->ddivvdt};
   for(int k = 0; k < NF; ++k) {
     if(k == F_Z || k == F_VZ || k == F_VHZ || k == F_AZ || k == F_GAZ)
       if(c->p.dimension == 2)
@@ -627,6 +638,30 @@ fsph_status fsph_reset_ghosts(fsph_ctx * c) {
   return FSPH_OK;
 }
 
+static fsph_status elem(fsph_ctx * c, int op, int phase);
+
+// viscosity::initialize_alpha over all particles (viscosity.h:171-177).
+fsph_status fsph_initialize_alpha(fsph_ctx * c) {
+  return elem(c, OP_INIT_ALPHA, FSPH_TIMER_INTEGRATE);
+}
+
+// apply_in_smoothinglength(viscosity::compute_alpha) (viscosity.h:310-363).
+fsph_status fsph_compute_alpha(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  if(!c->pp.cullen) {
+    c->last_error = "compute_alpha needs sph_viscosity = visc_cullen";
+    return FSPH_ERR_STATE;
+  }
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_DENSITY);
+  CK(launch_alpha_cullen(L, c->P, c->pp, c->Ls, c->d_time));
+  return FSPH_OK;
+}
+
 static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
@@ -647,7 +682,7 @@ static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   else {
     {
       Phase ph(c, FSPH_TIMER_DENSITY);
-      CK(launch_density_fp64(L, c->P, c->pp, c->Ls, c->cs_new, c->d_status));
+      CK(launch_density_fp64(L, c->P, c->pp, c->Ls, c->cs_new, c->d_status, c->d_time));
     }
     Phase ph(c, FSPH_TIMER_VSIG);
     CK(launch_vsig_fp64(L, c->P, c->pp, c->Ls, c->cs_new));
@@ -834,14 +869,19 @@ fsph_status fsph_step(fsph_ctx * c) {
   const bool thermo = p.thermokinetic_formulation;
   const bool evolve = p.evolve_internal_energy;
   const bool grav = p.enable_fmm;
+  const bool cullen = c->pp.cullen;
   if(c->iteration == p.initial_iteration) {
     TRY(fsph_update_iteration(c));
     TRY(fsph_eos_init(c));
     if(thermo)
       TRY(fsph_set_total_energy(c));
+    if(cullen)
+      TRY(fsph_initialize_alpha(c));
     // mixed: the signal speed rides in the acceleration loop
     TRY(density_impl(c, !c->mixed));
     TRY(fsph_save_velocityhalf(c));
+    if(cullen)
+      TRY(fsph_compute_alpha(c));
     TRY(accel_impl(c, 0, c->mixed));
     if(grav) {
       // newtonian/main_driver.cc:137-151: gravity, then total energy again
@@ -871,6 +911,8 @@ fsph_status fsph_step(fsph_ctx * c) {
       FSPH_TIMER_INTEGRATE));
     TRY(fsph_update_iteration(c));
     TRY(density_impl(c, !c->mixed));
+    if(cullen)
+      TRY(fsph_compute_alpha(c));
     if(grav) {
       // newtonian/main_driver.cc:217-227: gravity between the hydro
       // acceleration and the velocity kick

@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
       f[F_H][i] = r * pp.eta * pp.kw;
       break;
     }
+    case OP_INIT_ALPHA:  // viscosity::initialize_alpha (viscosity.h:171-177)
+      f[F_ALPHA][i] = pp.cullen ? 0.0 : pp.alpha;
+      break;
     case OP_SET_H:  // second half of compute_average_smoothinglength
       f[F_H][i] = 1. / (double)P.n * tm->hsum;
       break;

@@ -19,7 +19,7 @@ namespace fsph {
 // pass still needs the old one (see k_vsig).
 template<int D, int K>
 __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
-  PhysParams pp, Lists Ls, double * cs_new, DevStatus * st) {
+  PhysParams pp, Lists Ls, double * cs_new, DevStatus * st, const DevTime * tm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
     return;
@@ -66,6 +66,123 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
   eos_p_cs(pp, rho_a, u, P.f[F_K][a], Pa, cs);
   P.f[F_P][a] = Pa;
   cs_new[a] = cs;
+  if(pp.cullen) {
+    // compute_divv (default_physics.h:273-299), same traversal
+    double va[3] = {P.f[F_VX][a], P.f[F_VY][a], D == 3 ? P.f[F_VZ][a] : 0.0};
+    double pa[3] = {pa0, pa1, pa2};
+    double div_v = 0.0;
+    for(int j = 0; j < cnt; ++j) {
+      const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
+      double pos_ab[3] = {pa[0] - X[b], pa[1] - Y[b], D == 3 ? pa[2] - Z[b] : 0.0};
+      const double h_ab = .5 * (h_a + H[b]);
+      double DiWab[3];
+      kgrad<D, K>(pos_ab, h_ab, DiWab);
+      double dot = 0.0;
+      for(int d = 0; d < D; ++d)
+        dot += va[d] * DiWab[d];
+      div_v += M[b] * dot;
+    }
+    div_v /= rho_a;
+    const double div_v_p = P.f[F_DIVV][a];
+    P.f[F_DDIVVDT][a] = (div_v - div_v_p) / tm->dt;
+    P.f[F_DIVV][a] = div_v;
+  }
+}
+
+// viscosity::compute_alpha with A_trigger and compute_xi (viscosity.h:
+// 185-363): Cullen & Dehnen's adaptive alpha from the velocity divergence,
+// its rate and the traceless shear, in the reference's operand order.
+template<int D, int K>
+__global__ void __launch_bounds__(PAIR_THREADS) k_alpha_cullen(Particles P,
+  PhysParams pp, Lists Ls, const DevTime * tm) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const double * X = P.f[F_X];
+  const double * Y = P.f[F_Y];
+  const double * Z = P.f[F_Z];
+  const double * H = P.f[F_H];
+  const double * M = P.f[F_M];
+  const double * CS = P.f[F_CS];
+  const double * DV = P.f[F_DIVV];
+  const double * V[3] = {P.f[F_VX], P.f[F_VY], P.f[F_VZ]};
+  const double c_a = CS[a], h_a = H[a], alpha_a = P.f[F_ALPHA][a];
+  const double rho_a = P.f[F_RHO][a];
+  const double pa[3] = {X[a], Y[a], D == 3 ? Z[a] : 0.0};
+  double va[3] = {0, 0, 0};
+  for(int d = 0; d < D; ++d)
+    va[d] = V[d][a];
+  const int cnt = Ls.cnt[a];
+  // signal speed of this pass: all sound speeds are the new ones here
+  double vsig = 0.0;
+  // compute_xi accumulations
+  double R_a = 0.0;
+  double gradV[D * D];
+  for(int k = 0; k < D * D; ++k)
+    gradV[k] = 0.0;
+  for(int j = 0; j < cnt; ++j) {
+    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
+    const double pb[3] = {X[b], Y[b], D == 3 ? Z[b] : 0.0};
+    double pos_ab[3] = {0, 0, 0}, vab[3] = {0, 0, 0};
+    double dist = 0.0;
+    for(int d = 0; d < D; ++d) {
+      pos_ab[d] = pa[d] - pb[d];
+      vab[d] = va[d] - V[d][b];
+      dist += pos_ab[d] * pos_ab[d];
+    }
+    dist = sqrt(dist);
+    // vsig = max(vsig, max(c_a, c_b) - min(v_ab . n_ab, 0)); the self pair
+    // (0/0) is a NaN that std::max drops
+    double vn = 0.0;
+    for(int d = 0; d < D; ++d)
+      vn += vab[d] * (pos_ab[d] / dist);
+    const double cmax = c_a < CS[b] ? CS[b] : c_a;
+    const double mn = 0.0 < vn ? 0.0 : vn;   // std::min(vn, 0.0)
+    const double cand = cmax - mn;
+    vsig = vsig < cand ? cand : vsig;        // std::max(vsig, cand)
+    const double h_ab = .5 * (h_a + H[b]);
+    double DiWa[3];
+    kgrad<D, K>(pos_ab, h_ab, DiWa);
+    const double Wab = kfun<D, K>(dist, h_ab);
+    const double dvb = DV[b];
+    const double sgn = dvb > 0.0 ? 1.0 : (dvb < 0.0 ? -1.0 : dvb);
+    R_a += sgn * M[b] * Wab;
+    for(int i = 0; i < D; ++i)
+      for(int k = 0; k < D; ++k)
+        gradV[D * i + k] += M[b] * (-vab[i]) * DiWa[k];
+  }
+  R_a /= rho_a;
+  for(int k = 0; k < D * D; ++k)
+    gradV[k] /= rho_a;
+  const double divV_a = DV[a];
+  double traceSS = 0.0;
+  for(int i = 0; i < D; ++i) {
+    double row[3];
+    for(int k = 0; k < D; ++k)
+      row[k] = 0.5 * (gradV[D * i + k] + gradV[D * k + i]);
+    row[i] -= divV_a / D;
+    for(int k = 0; k < D; ++k)
+      traceSS += row[k] * row[k];
+  }
+  const double om = 1.0 - R_a;
+  const double q4 = om * om * om * om;
+  const double t = 2.0 * q4 * divV_a;
+  const double res = t * t;
+  const double xi = (res < 1e-16) ? 0.0 : res / (res + traceSS);
+  const double ddv = P.f[F_DDIVVDT][a];
+  const double trig = -ddv < 0.0 ? 0.0 : -ddv;   // std::max(-dDivVdt, 0.0)
+  const double Atrig = xi * trig;
+  const double vh = vsig / h_a;
+  const double alpha_loc = pp.alpha_max * Atrig / (pp.visc_delta * (vh * vh) + Atrig);
+  double alpha;
+  if(alpha_a <= alpha_loc)
+    alpha = alpha_loc;
+  else {
+    const double decayt = h_a / (2.0 * pp.visc_l * vsig);
+    const double dalphadt = (alpha_a - alpha_loc) / decayt;
+    alpha = alpha_a * exp(-dalphadt * tm->dt);
+  }
+  P.f[F_ALPHA][a] = alpha;
 }
 
 // compute_signalspeed (default_physics.h:236-265).  The reference visits
@@ -156,7 +273,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_accel(Particles P,
     const double mu_ab = visc_mu<D>(pp.eps, h_ab, v12_ab, pos_ab);
     const double rho_ab = .5 * (rho_a + rho_b);
     const double c_ab = .5 * (c_a + CS[b]);
-    const double Pi = visc_pi(pp.alpha, pp.beta, rho_ab, c_ab, mu_ab);
+    const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
     kgrad<D, K>(pos_ab, h_ab, DiWa);
     const double Prho2_b = PR[b] / (rho_b * rho_b);
     const double s = -m_b * (Prho2_a + Prho2_b + Pi);
@@ -216,7 +333,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dudt(Particles P,
     const double mu_ab = visc_mu<D>(pp.eps, h_ab, v12_ab, pos_ab);
     const double rho_ab = .5 * (rho_a + RHO[b]);
     const double c_ab = .5 * (c_a + CS[b]);
-    const double Pi = visc_pi(pp.alpha, pp.beta, rho_ab, c_ab, mu_ab);
+    const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
     kgrad<D, K>(pos_ab, h_ab, DiWab);
     double vdw = 0;
     for(int d = 0; d < D; ++d)
@@ -273,7 +390,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
     const double mu_ab = visc_mu<D>(pp.eps, h_ab, v12_ab, pos_ab);
     const double rho_ab = .5 * (rho_a + rho_b);
     const double c_ab = .5 * (c_a + CS[b]);
-    const double Pi = visc_pi(pp.alpha, pp.beta, rho_ab, c_ab, mu_ab);
+    const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
     kgrad<D, K>(pos_ab, h_ab, DiWab);
     double vad = 0, vbd = 0;
     for(int d = 0; d < D; ++d)
@@ -319,8 +436,15 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
   } while(0)
 
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st) {
-  DISPATCH_DK(k_density, P, pp, Ls, cs_new, st);
+  const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st,
+  const DevTime * t) {
+  DISPATCH_DK(k_density, P, pp, Ls, cs_new, st, t);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_cullen(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const DevTime * t) {
+  DISPATCH_DK(k_alpha_cullen, P, pp, Ls, t);
   return cudaGetLastError();
 }
 

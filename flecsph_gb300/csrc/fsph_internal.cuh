@@ -14,7 +14,7 @@ namespace fsph {
 enum Field {
   F_X, F_Y, F_Z, F_VX, F_VY, F_VZ, F_VHX, F_VHY, F_VHZ, F_AX, F_AY, F_AZ,
   F_GAX, F_GAY, F_GAZ, F_GPOT, F_M, F_H, F_RHO, F_P, F_CS, F_U, F_E, F_DUDT,
-  F_DEDT, F_K, F_ALPHA, F_VSIG, F_DT, NF
+  F_DEDT, F_K, F_ALPHA, F_VSIG, F_DT, F_DIVV, F_DDIVVDT, NF
 };
 
 // physics:: time globals of the reference (default_physics.h:32-39), kept in
@@ -44,7 +44,9 @@ struct Particles {
 
 struct PhysParams {
   int dim, kernel, eos, thermokinetic, evolve_u, adaptive;
+  int cullen;  // sph_viscosity == visc_cullen
   double gamma, eta, kw, alpha, beta, eps, cfl;
+  double alpha_max, visc_l, visc_delta;  // visc_cullen parameters
   double out_screen_dt, out_scalar_dt, out_h5data_dt;
   double G;
 };
@@ -206,7 +208,10 @@ cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
 
 // ---- fsph_fp64.cu ----
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st);
+  const PhysParams & pp, const Lists & Ls, double * cs_new, DevStatus * st,
+  const DevTime * t);
+cudaError_t launch_alpha_cullen(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const DevTime * t);
 cudaError_t launch_vsig_fp64(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const double * cs_new);
 cudaError_t launch_accel_fp64(const Launch & L, const Particles & P,
@@ -221,7 +226,8 @@ enum ElemOp {
   OP_EOS_INIT, OP_SET_TOTAL_ENERGY, OP_SAVE_VHALF, OP_KICK_V, OP_KICK_U,
   OP_KICK_E, OP_DRIFT, OP_RECOMPUTE, OP_RECOMPUTE_THERMO, OP_SMOOTHING_LENGTH,
   OP_CHECK_NANS, OP_CHECK_NEGATIVITY, OP_KICK_DRIFT_E, OP_KICK_DRIFT_U,
-  OP_KICK_DRIFT_NONE, OP_SET_H, OP_RECOMPUTE_KICK_E, OP_RECOMPUTE_KICK_U
+  OP_KICK_DRIFT_NONE, OP_SET_H, OP_RECOMPUTE_KICK_E, OP_RECOMPUTE_KICK_U,
+  OP_INIT_ALPHA
 };
 cudaError_t launch_elementwise(const Launch & L, const Particles & P,
   const PhysParams & pp, int op, DevTime * t, DevStatus * st);

@@ -146,6 +146,19 @@ __device__ __forceinline__ double visc_pi(double alpha, double beta,
   return (-alpha * c_ab + beta * mu_ab) * mu_ab / rho_ab;
 }
 
+// sph_artificial_viscosity for the configured viscosity: visc_constant
+// ignores alpha_ab (viscosity.h:128-137); visc_cullen is
+// viscosity_function<visc_cullen> (viscosity.h:150-158) with
+// alpha_ab = (alpha_a + alpha_b) / 2 (default_physics.h:388).
+__device__ __forceinline__ double visc_pi_pp(const PhysParams & pp,
+  const double * ALPHA, int a, int b, double rho_ab, double c_ab, double mu_ab) {
+  if(pp.cullen) {
+    const double alpha_ab = .5 * (ALPHA[a] + ALPHA[b]);
+    return -alpha_ab * (c_ab - 2.0 * mu_ab) * mu_ab / rho_ab;
+  }
+  return visc_pi(pp.alpha, pp.beta, rho_ab, c_ab, mu_ab);
+}
+
 // eos_t<ideal>/<polytropic> compute_pressure + compute_soundspeed
 // (eos/eos.h:102-119, 166-183)
 __device__ __forceinline__ void eos_p_cs(const PhysParams & pp, double rho,

@@ -6,8 +6,9 @@
 //   hydro_driver <in.bin> <out.bin> <iterations> [key=value ...]
 //
 // in/out: raw particle snapshots, little endian:
-//   char magic[8] = "FSPHSOA1"; int64 n; int32 dim; int32 nfields(=29);
-//   29 double arrays of length n in fsph_soa_view order (x..dt); int64 id[n]
+//   char magic[8] = "FSPHSOA1"; int64 n; int32 dim; int32 nfields(=31);
+//   31 double arrays of length n in fsph_soa_view order (x..ddivvdt);
+//   int64 id[n]
 // Parameters not given as key=value keep their reference defaults.
 #include <cstdint>
 #include <cstdio>
@@ -20,7 +21,7 @@
 
 namespace {
 
-constexpr int NFIELDS = 29;
+constexpr int NFIELDS = 31;
 
 struct Snapshot {
   int64_t n = 0;
@@ -36,7 +37,7 @@ struct Snapshot {
     double ** slots[NFIELDS] = {&v.x, &v.y, &v.z, &v.vx, &v.vy, &v.vz, &v.vhx,
       &v.vhy, &v.vhz, &v.ax, &v.ay, &v.az, &v.gax, &v.gay, &v.gaz, &v.gpot,
       &v.m, &v.h, &v.rho, &v.P, &v.cs, &v.u, &v.e, &v.dudt, &v.dedt, &v.K,
-      &v.alpha, &v.vsig, &v.dt};
+      &v.alpha, &v.vsig, &v.dt, &v.divv, &v.ddivvdt};
     for(int k = 0; k < NFIELDS; ++k)
       *slots[k] = f[k].data();
     v.id = id.data();
@@ -141,8 +142,12 @@ int main(int argc, char ** argv) {
         bs.apply_all(eos::init);
         if(p.thermokinetic_formulation)
           bs.apply_all(physics::set_total_energy);
+        if(p.sph_viscosity != FSPH_VISC_CONSTANT)
+          bs.apply_all(viscosity::initialize_alpha);
         bs.apply_in_smoothinglength(physics::compute_density_pressure_soundspeed);
         bs.apply_all(integration::save_velocityhalf);
+        if(p.sph_viscosity != FSPH_VISC_CONSTANT)
+          bs.apply_in_smoothinglength(viscosity::compute_alpha);
         bs.reset_ghosts();
         bs.apply_in_smoothinglength(physics::compute_acceleration);
         if(p.adaptive_timestep) {
@@ -168,6 +173,8 @@ int main(int argc, char ** argv) {
         bs.apply_all(integration::leapfrog_drift);
         bs.update_iteration();
         bs.apply_in_smoothinglength(physics::compute_density_pressure_soundspeed);
+        if(p.sph_viscosity != FSPH_VISC_CONSTANT)
+          bs.apply_in_smoothinglength(viscosity::compute_alpha);
         bs.reset_ghosts();
         bs.apply_in_smoothinglength(physics::compute_acceleration);
         bs.apply_all(integration::leapfrog_kick_v);

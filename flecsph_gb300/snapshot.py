@@ -1,7 +1,7 @@
 """Raw particle snapshots read and written by the C++ hydro driver.
 
-Layout (little endian): b"FSPHSOA1", int64 n, int32 dim, int32 nfields (29),
-then the 29 FP64 arrays of fsph_soa_view in header order, then int64 id[n].
+Layout (little endian): b"FSPHSOA1", int64 n, int32 dim, int32 nfields (31),
+then the 31 FP64 arrays of fsph_soa_view in header order, then int64 id[n].
 The reference writes H5part files (mpisph/io.h:874-1088); HDF5 is not part
 of this build, so snapshots are raw SoA.
 """
@@ -31,7 +31,12 @@ def read(path):
         n = int(np.frombuffer(f.read(8), np.int64)[0])
         dim = int(np.frombuffer(f.read(4), np.int32)[0])
         nf = int(np.frombuffer(f.read(4), np.int32)[0])
-        assert nf == len(DOUBLE_FIELDS)
-        out = {k: np.frombuffer(f.read(8 * n), np.float64).copy() for k in DOUBLE_FIELDS}
+        if not 0 < nf <= len(DOUBLE_FIELDS):
+            raise ValueError(f"snapshot holds {nf} fields")
+        # files written before the divergence fields existed hold the first 29
+        out = {k: np.frombuffer(f.read(8 * n), np.float64).copy()
+               for k in DOUBLE_FIELDS[:nf]}
+        for k in DOUBLE_FIELDS[nf:]:
+            out[k] = np.zeros(n)
         out["id"] = np.frombuffer(f.read(8 * n), np.int64).copy()
     return out, dim

@@ -32,7 +32,7 @@ _STEP_FUNCS = [
     "recompute_pressure_soundspeed_thermokinetic", "compute_dt", "check_nans",
     "check_negativity", "set_adaptive_timestep", "compute_smoothinglength",
     "compute_average_smoothinglength", "gravitation", "advance_time", "step", "sync",
-    "timers_reset",
+    "timers_reset", "compute_alpha", "initialize_alpha",
 ]
 
 

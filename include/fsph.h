@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FSPH_ABI_VERSION 1
+#define FSPH_ABI_VERSION 2
 
 /* Status codes.  They replace the reference's assert()/mpi_assert() aborts
  * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
@@ -77,8 +77,8 @@ enum fsph_kernel {
 };
 /* Same numbering as param::eos_type_keyword (include/params.h:139-145). */
 enum fsph_eos { FSPH_EOS_IDEAL = 0, FSPH_EOS_POLYTROPIC = 1 };
-/* param::sph_viscosity_keyword (include/params.h:148-152): only visc_constant. */
-enum fsph_viscosity { FSPH_VISC_CONSTANT = 0 };
+/* param::sph_viscosity_keyword (include/params.h:148-152). */
+enum fsph_viscosity { FSPH_VISC_CONSTANT = 0, FSPH_VISC_CULLEN = 1 };
 enum fsph_precision {
   FSPH_PRECISION_FP64 = 0,  /* every pair term in FP64 (plain method) */
   FSPH_PRECISION_MIXED = 1  /* FP32 pair math with compensated sums; FP64 state */
@@ -126,6 +126,11 @@ typedef struct fsph_params {
   int32_t precision_mode;            /* enum fsph_precision, default FP64 */
   int32_t max_neighbors;             /* neighbour-list capacity per particle, default 256 */
   int32_t gravity_order;             /* multipole order of fsph_gravitation: 1 or 2 (default 2) */
+  int32_t reserved_pad;
+  /* Cullen & Dehnen adaptive viscosity (visc_cullen), param:: names */
+  double sph_viscosity_alpha_max;    /* [516] 1.0 */
+  double sph_viscosity_l;            /* [523] 0.05 */
+  double sph_viscosity_delta;        /* [529] 1.0 */
   int32_t reserved[8];
 } fsph_params;
 
@@ -155,6 +160,8 @@ typedef struct fsph_soa_view {
   double *alpha;           /* (opt) viscosity alpha (unused by visc_constant) */
   double *vsig;            /* (opt) signal speed */
   double *dt;              /* (opt) per-particle timestep estimate */
+  double *divv;            /* (opt) velocity divergence (visc_cullen) */
+  double *ddivvdt;         /* (opt) its time derivative (visc_cullen) */
   int64_t *id;             /* (in)  particle id (sort tie-break) */
   uint64_t *key;           /* (out) Morton key, download only */
 } fsph_soa_view;
@@ -228,7 +235,13 @@ fsph_status fsph_get_range(fsph_ctx * ctx, double * range);
 fsph_status fsph_update_iteration(fsph_ctx * ctx);
 fsph_status fsph_reset_ghosts(fsph_ctx * ctx);
 /* apply_in_smoothinglength(...) */
+/* physics::compute_density_pressure_soundspeed (default_physics.h:309-320):
+ * density, EOS, signal speed and, with visc_cullen, compute_divv */
 fsph_status fsph_density_pressure_soundspeed(fsph_ctx * ctx);
+/* viscosity::compute_alpha (viscosity.h:310-363), visc_cullen only */
+fsph_status fsph_compute_alpha(fsph_ctx * ctx);
+/* apply_all(viscosity::initialize_alpha) (viscosity.h:171-177) */
+fsph_status fsph_initialize_alpha(fsph_ctx * ctx);
 fsph_status fsph_acceleration(fsph_ctx * ctx);
 fsph_status fsph_dudt(fsph_ctx * ctx);
 fsph_status fsph_dedt(fsph_ctx * ctx);

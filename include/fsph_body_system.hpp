@@ -87,6 +87,13 @@ constexpr leapfrog_kick_e_t leapfrog_kick_e{};
 constexpr leapfrog_drift_t leapfrog_drift{};
 } // namespace integration
 
+namespace viscosity {
+struct compute_alpha_t {};
+struct initialize_alpha_t {};
+constexpr compute_alpha_t compute_alpha{};        // viscosity.h:310-363
+constexpr initialize_alpha_t initialize_alpha{};  // viscosity.h:171-177
+} // namespace viscosity
+
 template<int D>
 class body_system {
 public:
@@ -124,6 +131,12 @@ public:
   void apply_in_smoothinglength(physics::dudt_t) { check(fsph_dudt(ctx_), "compute_dudt"); }
   void apply_in_smoothinglength(physics::dedt_t) { check(fsph_dedt(ctx_), "compute_dedt"); }
 
+  void apply_in_smoothinglength(viscosity::compute_alpha_t) {
+    check(fsph_compute_alpha(ctx_), "viscosity::compute_alpha");
+  }
+  void apply_all(viscosity::initialize_alpha_t) {
+    check(fsph_initialize_alpha(ctx_), "viscosity::initialize_alpha");
+  }
   void apply_all(eos::init_t) { check(fsph_eos_init(ctx_), "eos::init"); }
   void apply_all(physics::set_total_energy_t) {
     check(fsph_set_total_energy(ctx_), "set_total_energy");

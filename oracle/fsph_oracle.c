@@ -77,7 +77,7 @@ struct orc_ctx {
   int64_t nreal; /* real particles hold ids [0, nreal); WALL copies above */
   double *x[3], *v[3], *vh[3], *a[3], *ga[3];
   double *gpot, *m, *h, *rho, *P, *cs, *u, *e, *dudt, *dedt, *K, *alpha, *vsig,
-    *dtp;
+    *dtp, *divv, *ddivvdt;
   int64_t * id;
   uint64_t * key;
   double * csnew;
@@ -263,8 +263,15 @@ static double visc_mu(const orc_ctx * c, double h_ab, const double * vel_ab,
   return result * (dotp < 0.0);
 }
 
-/* viscosity_function<visc_constant> (viscosity.h:128-137) */
-static double visc_pi(const orc_ctx * c, double rho_ab, double c_ab, double mu_ab) {
+/* sph_artificial_viscosity: viscosity_function<visc_constant>
+ * (viscosity.h:128-137) ignores alpha_ab; <visc_cullen> (:150-158) uses
+ * alpha_ab = (alpha_a + alpha_b) / 2 (default_physics.h:388). */
+static double visc_pi(const orc_ctx * c, int64_t a, int64_t b, double rho_ab,
+  double c_ab, double mu_ab) {
+  if(c->p.sph_viscosity == FSPH_VISC_CULLEN) {
+    const double alpha_ab = .5 * (c->alpha[a] + c->alpha[b]);
+    return -alpha_ab * (c_ab - 2.0 * mu_ab) * mu_ab / rho_ab;
+  }
   return (-c->p.sph_viscosity_alpha * c_ab + c->p.sph_viscosity_beta * mu_ab) *
          mu_ab / rho_ab;
 }
@@ -320,6 +327,7 @@ static void free_state(orc_ctx * c) {
   free(c->gpot); free(c->m); free(c->h); free(c->rho); free(c->P); free(c->cs);
   free(c->u); free(c->e); free(c->dudt); free(c->dedt); free(c->K);
   free(c->alpha); free(c->vsig); free(c->dtp); free(c->id); free(c->key);
+  free(c->divv); free(c->ddivvdt);
   free(c->csnew);
 }
 
@@ -387,6 +395,7 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
   c->u = xalloc(8 * n); c->e = xalloc(8 * n); c->dudt = xalloc(8 * n);
   c->dedt = xalloc(8 * n); c->K = xalloc(8 * n); c->alpha = xalloc(8 * n);
   c->vsig = xalloc(8 * n); c->dtp = xalloc(8 * n); c->id = xalloc(8 * n);
+  c->divv = xalloc(8 * n); c->ddivvdt = xalloc(8 * n);
   c->key = xalloc(8 * n); c->csnew = xalloc(8 * n);
   double * const xs[3] = {v->x, v->y, v->z};
   double * const vs[3] = {v->vx, v->vy, v->vz};
@@ -402,6 +411,7 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
   CPY_IN(c->u, v->u); CPY_IN(c->e, v->e); CPY_IN(c->dudt, v->dudt);
   CPY_IN(c->dedt, v->dedt); CPY_IN(c->K, v->K); CPY_IN(c->alpha, v->alpha);
   CPY_IN(c->vsig, v->vsig); CPY_IN(c->dtp, v->dt);
+  CPY_IN(c->divv, v->divv); CPY_IN(c->ddivvdt, v->ddivvdt);
   memcpy(c->id, v->id, 8 * n);
   c->nreal = n;
   if(is_periodic(c)) {
@@ -449,6 +459,7 @@ int orc_download(orc_ctx * c, fsph_soa_view * v) {
   CPY_OUT(v->u, c->u); CPY_OUT(v->e, c->e); CPY_OUT(v->dudt, c->dudt);
   CPY_OUT(v->dedt, c->dedt); CPY_OUT(v->K, c->K); CPY_OUT(v->alpha, c->alpha);
   CPY_OUT(v->vsig, c->vsig); CPY_OUT(v->dt, c->dtp);
+  CPY_OUT(v->divv, c->divv); CPY_OUT(v->ddivvdt, c->ddivvdt);
   if(v->id) memcpy(v->id, c->id, 8 * n);
   if(v->key) memcpy(v->key, c->key, 8 * n);
   return FSPH_OK;
@@ -644,7 +655,7 @@ static void collect_groups(orc_ctx * c, int64_t node) {
 }
 
 /* Every per-particle array, for moves of whole particles. */
-#define ORC_NFIELDS 27
+#define ORC_NFIELDS 29
 static void field_list(orc_ctx * c, double *** out) {
   int k = 0;
   for(int d = 0; d < 3; ++d) {
@@ -655,6 +666,7 @@ static void field_list(orc_ctx * c, double *** out) {
   out[k++] = &c->P; out[k++] = &c->cs; out[k++] = &c->u; out[k++] = &c->e;
   out[k++] = &c->dudt; out[k++] = &c->dedt; out[k++] = &c->K;
   out[k++] = &c->alpha;
+  out[k++] = &c->divv; out[k++] = &c->ddivvdt;
 }
 
 static void ensure_cap(orc_ctx * c, int64_t need) {
@@ -850,7 +862,8 @@ int orc_update_iteration(orc_ctx * c) {
     permute_d(&c->ga[d], rec, n, tmp);
   }
   double ** fs[] = {&c->gpot, &c->m, &c->h, &c->rho, &c->P, &c->cs, &c->u,
-    &c->e, &c->dudt, &c->dedt, &c->K, &c->alpha, &c->vsig, &c->dtp};
+    &c->e, &c->dudt, &c->dedt, &c->K, &c->alpha, &c->vsig, &c->dtp, &c->divv,
+    &c->ddivvdt};
   for(size_t k = 0; k < sizeof(fs) / sizeof(fs[0]); ++k)
     permute_d(fs[k], rec, n, tmp);
   for(int64_t i = 0; i < n; ++i) {
@@ -1096,7 +1109,99 @@ static int density_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
   eos_pressure(c, a, c->u[a], &P, &cs);
   c->P[a] = P;
   c->csnew[a] = cs;
+  if(c->p.sph_viscosity == FSPH_VISC_CULLEN) {
+    /* compute_divv (default_physics.h:273-299) */
+    double div_v = 0.0;
+    for(int64_t j = 0; j < nn; ++j) {
+      int64_t b = nb[j];
+      double pos_ab[3], DiWab[3];
+      for(int d = 0; d < D; ++d)
+        pos_ab[d] = pa[d] - c->x[d][b];
+      kgrad(c, pos_ab, .5 * (h_a + c->h[b]), DiWab);
+      double dot = 0.0;
+      for(int d = 0; d < D; ++d)
+        dot += c->v[d][a] * DiWab[d];
+      div_v += c->m[b] * dot;
+    }
+    div_v /= c->rho[a];
+    const double div_v_p = c->divv[a];
+    c->ddivvdt[a] = (div_v - div_v_p) / c->dt;
+    c->divv[a] = div_v;
+  }
   return FSPH_OK;
+}
+
+/* viscosity::compute_alpha with A_trigger and compute_xi (viscosity.h:
+ * 185-363). */
+static void alpha_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double c_a = c->cs[a], h_a = c->h[a], alpha_a = c->alpha[a];
+  const double rho_a = c->rho[a];
+  double pa[3];
+  getx(c, a, pa);
+  /* signal speed (:324-333) */
+  double vsig = 0.0;
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pb[3];
+    getx(c, b, pb);
+    double dist = dist_pts(D, pa, pb);
+    double dotv = 0.0;
+    for(int d = 0; d < D; ++d)
+      dotv += (c->v[d][a] - c->v[d][b]) * ((pa[d] - pb[d]) / dist);
+    double cab = dmax_(c_a, c->cs[b]);
+    vsig = dmax_(vsig, cab - dmin_(dotv, 0.0));
+  }
+  /* compute_xi (:200-285) */
+  const double divV_a = c->divv[a];
+  double R_a = 0.0;
+  double gradV[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    double pb[3], pos_ab[3], vab[3], DiWa[3];
+    getx(c, b, pb);
+    for(int d = 0; d < D; ++d) {
+      pos_ab[d] = pa[d] - pb[d];
+      vab[d] = c->v[d][a] - c->v[d][b];
+    }
+    const double h_ab = .5 * (h_a + c->h[b]);
+    kgrad(c, pos_ab, h_ab, DiWa);
+    const double Wab = kfun(c, dist_pts(D, pa, pb), h_ab);
+    const double dvb = c->divv[b];
+    const double sgn = dvb > 0.0 ? 1.0 : (dvb < 0.0 ? -1.0 : dvb);
+    R_a += sgn * c->m[b] * Wab;
+    for(int i = 0; i < D; ++i)
+      for(int k = 0; k < D; ++k)
+        gradV[D * i + k] += c->m[b] * (-vab[i]) * DiWa[k];
+  }
+  R_a /= rho_a;
+  for(int k = 0; k < D * D; ++k)
+    gradV[k] /= rho_a;
+  double traceSS = 0.0;
+  for(int i = 0; i < D; ++i) {
+    double row[3];
+    for(int k = 0; k < D; ++k)
+      row[k] = 0.5 * (gradV[D * i + k] + gradV[D * k + i]);
+    row[i] -= divV_a / D;
+    for(int k = 0; k < D; ++k)
+      traceSS += row[k] * row[k];
+  }
+  const double om = 1.0 - R_a;
+  const double t = 2.0 * (om * om * om * om) * divV_a;
+  const double res = t * t;
+  const double xi = (res < 1e-16) ? 0.0 : res / (res + traceSS);
+  /* A_trigger (:293-306) */
+  const double Atrig = xi * dmax_(-c->ddivvdt[a], 0.0);
+  const double vh = vsig / h_a;
+  const double alpha_loc = c->p.sph_viscosity_alpha_max * Atrig /
+                           (c->p.sph_viscosity_delta * (vh * vh) + Atrig);
+  if(alpha_a <= alpha_loc)
+    c->alpha[a] = alpha_loc;
+  else {
+    const double decayt = h_a / (2.0 * c->p.sph_viscosity_l * vsig);
+    const double dalphadt = (alpha_a - alpha_loc) / decayt;
+    c->alpha[a] = alpha_a * exp(-dalphadt * c->dt);
+  }
 }
 
 /* compute_signalspeed (default_physics.h:236-265) with the visiting-order
@@ -1149,7 +1254,7 @@ static void accel_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
     double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
     double rho_ab = .5 * (rho_a + c->rho[b]);
     double c_ab = .5 * (c_a + c->cs[b]);
-    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    double Pi = visc_pi(c, a, b, rho_ab, c_ab, mu_ab);
     kgrad(c, pos_ab, h_ab, DiWa);
     double Prho2_b = c->P[b] / (c->rho[b] * c->rho[b]);
     double s = -m_b * (Prho2_a + Prho2_b + Pi);
@@ -1193,7 +1298,7 @@ static void dudt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
     double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
     double rho_ab = .5 * (rho_a + c->rho[b]);
     double c_ab = .5 * (c_a + c->cs[b]);
-    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    double Pi = visc_pi(c, a, b, rho_ab, c_ab, mu_ab);
     kgrad(c, pos_ab, h_ab, DiWab);
     double vdw = 0;
     for(int d = 0; d < D; ++d)
@@ -1232,7 +1337,7 @@ static void dedt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
     double mu_ab = visc_mu(c, h_ab, v12_ab, pos_ab);
     double rho_ab = .5 * (rho_a + c->rho[b]);
     double c_ab = .5 * (c_a + c->cs[b]);
-    double Pi = visc_pi(c, rho_ab, c_ab, mu_ab);
+    double Pi = visc_pi(c, a, b, rho_ab, c_ab, mu_ab);
     kgrad(c, pos_ab, h_ab, DiWab);
     double vad = 0, vbd = 0;
     for(int d = 0; d < D; ++d)
@@ -1246,7 +1351,7 @@ static void dedt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
   c->dedt[a] = dedt;
 }
 
-enum { PASS_DENSITY, PASS_VSIG, PASS_ACCEL, PASS_DUDT, PASS_DEDT };
+enum { PASS_DENSITY, PASS_VSIG, PASS_ACCEL, PASS_DUDT, PASS_DEDT, PASS_ALPHA };
 
 /* apply_in_smoothinglength: walk every group and apply the pass to its
  * members (tree_topology.h:253-409). */
@@ -1280,6 +1385,7 @@ static int run_pass(orc_ctx * c, int pass) {
           case PASS_ACCEL: accel_one(c, a, s.nb[k], s.nbn[k]); break;
           case PASS_DUDT: dudt_one(c, a, s.nb[k], s.nbn[k]); break;
           case PASS_DEDT: dedt_one(c, a, s.nb[k], s.nbn[k]); break;
+          case PASS_ALPHA: alpha_one(c, a, s.nb[k], s.nbn[k]); break;
         }
       }
     }
@@ -1307,6 +1413,18 @@ int orc_density_pressure_soundspeed(orc_ctx * c) {
 }
 
 int orc_acceleration(orc_ctx * c) { return run_pass(c, PASS_ACCEL); }
+int orc_compute_alpha(orc_ctx * c) {
+  if(c->p.sph_viscosity != FSPH_VISC_CULLEN)
+    return FSPH_ERR_STATE;
+  return run_pass(c, PASS_ALPHA);
+}
+int orc_initialize_alpha(orc_ctx * c) {
+  /* viscosity::initialize_alpha (viscosity.h:171-177) */
+  const double v = c->p.sph_viscosity == FSPH_VISC_CULLEN ? 0.0 : c->p.sph_viscosity_alpha;
+  for(int64_t i = 0; i < c->n; ++i)
+    c->alpha[i] = v;
+  return FSPH_OK;
+}
 int orc_dudt(orc_ctx * c) { return run_pass(c, PASS_DUDT); }
 int orc_dedt(orc_ctx * c) { return run_pass(c, PASS_DEDT); }
 
@@ -1593,15 +1711,21 @@ int orc_gravity_direct(orc_ctx * c, int64_t s0, int64_t s1) {
  * gravity standing in for the FMM). */
 int orc_step(orc_ctx * c) {
   const fsph_params * p = &c->p;
-  if(p->relaxation_steps != 0 || p->sph_viscosity != FSPH_VISC_CONSTANT)
+  if(p->relaxation_steps != 0 ||
+     (p->sph_viscosity != FSPH_VISC_CONSTANT && p->sph_viscosity != FSPH_VISC_CULLEN))
     return FSPH_ERR_ARG;
+  const int cullen = p->sph_viscosity == FSPH_VISC_CULLEN;
   if(c->iteration == p->initial_iteration) {
     TRY(orc_update_iteration(c));
     TRY(orc_eos_init(c));
     if(p->thermokinetic_formulation)
       TRY(orc_set_total_energy(c));
+    if(cullen)
+      TRY(orc_initialize_alpha(c));
     TRY(orc_density_pressure_soundspeed(c));
     TRY(orc_save_velocityhalf(c));
+    if(cullen)
+      TRY(orc_compute_alpha(c));
     TRY(orc_reset_ghosts(c));
     TRY(orc_acceleration(c));
     if(p->enable_fmm)
@@ -1639,6 +1763,8 @@ int orc_step(orc_ctx * c) {
     TRY(orc_leapfrog_drift(c));
     TRY(orc_update_iteration(c));
     TRY(orc_density_pressure_soundspeed(c));
+    if(cullen)
+      TRY(orc_compute_alpha(c));
     TRY(orc_reset_ghosts(c));
     TRY(orc_acceleration(c));
     if(p->enable_fmm)

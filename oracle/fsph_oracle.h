@@ -43,6 +43,8 @@ int orc_particle_count(orc_ctx * c, int64_t * total, int64_t * real);
 int orc_update_iteration(orc_ctx * c);
 int orc_reset_ghosts(orc_ctx * c);
 int orc_density_pressure_soundspeed(orc_ctx * c);
+int orc_compute_alpha(orc_ctx * c);
+int orc_initialize_alpha(orc_ctx * c);
 int orc_acceleration(orc_ctx * c);
 int orc_dudt(orc_ctx * c);
 int orc_dedt(orc_ctx * c);

@@ -46,7 +46,7 @@ _FUNCS0 = ["update_iteration", "reset_ghosts", "density_pressure_soundspeed",
            "recompute_pressure_soundspeed_thermokinetic", "compute_dt",
            "set_adaptive_timestep", "compute_smoothinglength",
            "compute_average_smoothinglength", "check_nans", "check_negativity",
-           "advance_time", "step"]
+           "advance_time", "step", "compute_alpha", "initialize_alpha"]
 
 _libs = {}
 

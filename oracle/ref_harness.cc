@@ -41,7 +41,10 @@ static void set_params(const fsph_params * p) {
   _sph_eta = p->sph_eta;
   _sph_kernel = (sph_kernel_keyword)p->sph_kernel;
   _eos_type = (eos_type_keyword)p->eos_type;
-  _sph_viscosity = visc_constant;
+  _sph_viscosity = p->sph_viscosity == FSPH_VISC_CULLEN ? visc_cullen : visc_constant;
+  _sph_viscosity_alpha_max = p->sph_viscosity_alpha_max;
+  _sph_viscosity_l = p->sph_viscosity_l;
+  _sph_viscosity_delta = p->sph_viscosity_delta;
   _sph_viscosity_alpha = p->sph_viscosity_alpha;
   _sph_viscosity_beta = p->sph_viscosity_beta;
   _sph_viscosity_epsilon = p->sph_viscosity_epsilon;
@@ -156,6 +159,8 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
     b.setAlpha(get(v->alpha, i));
     b.setSignalspeed(get(v->vsig, i));
     b.setDt(get(v->dt, i));
+    b.setDivergenceV(get(v->divv, i));
+    b.setDdivvdt(get(v->ddivvdt, i));
     b.setEntropy(0.0);
     b.setTemperature(0.0);
     b.setElectronfraction(0.0);
@@ -199,6 +204,8 @@ int orc_download(orc_ctx * c, fsph_soa_view * v) {
     if(v->alpha) v->alpha[i] = b.getAlpha();
     if(v->vsig) v->vsig[i] = b.getSignalspeed();
     if(v->dt) v->dt[i] = b.getDt();
+    if(v->divv) v->divv[i] = b.getDivergenceV();
+    if(v->ddivvdt) v->ddivvdt[i] = b.getDdivvdt();
     if(v->id) v->id[i] = (int64_t)b.id();
     if(v->key) v->key[i] = b.key().value();
   }
@@ -295,6 +302,11 @@ int orc_density_pressure_soundspeed(orc_ctx * c) {
   c->tree->traversal_sph(physics::compute_density_pressure_soundspeed);
   return FSPH_OK;
 }
+int orc_compute_alpha(orc_ctx * c) {
+  c->tree->traversal_sph(viscosity::compute_alpha);
+  return FSPH_OK;
+}
+int orc_initialize_alpha(orc_ctx * c) { return apply_all(c, viscosity::initialize_alpha); }
 int orc_acceleration(orc_ctx * c) {
   c->tree->traversal_sph(physics::compute_acceleration);
   return FSPH_OK;
@@ -366,8 +378,12 @@ int orc_step(orc_ctx * c) {
     orc_eos_init(c);
     if(thermokinetic_formulation)
       orc_set_total_energy(c);
+    if(sph_viscosity != visc_constant)
+      orc_initialize_alpha(c);
     orc_density_pressure_soundspeed(c);
     orc_save_velocityhalf(c);
+    if(sph_viscosity != visc_constant)
+      orc_compute_alpha(c);
     orc_reset_ghosts(c);
     orc_acceleration(c);
     if(adaptive_timestep) {
@@ -401,6 +417,8 @@ int orc_step(orc_ctx * c) {
     orc_leapfrog_drift(c);
     orc_update_iteration(c);
     orc_density_pressure_soundspeed(c);
+    if(sph_viscosity != visc_constant)
+      orc_compute_alpha(c);
     orc_reset_ghosts(c);
     orc_acceleration(c);
     orc_leapfrog_kick_v(c);

@@ -24,7 +24,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from flecsph_gb300 import setups  # noqa: E402
-from flecsph_gb300.abi import DOUBLE_FIELDS, KERNEL_WENDLAND_C4  # noqa: E402
+from flecsph_gb300.abi import DOUBLE_FIELDS, KERNEL_WENDLAND_C4, VISC_CULLEN  # noqa: E402
 import pyoracle  # noqa: E402
 
 
@@ -48,6 +48,10 @@ def cases():
     yield "sod2d_1000", setups.shuffled(s, 5), p, 2
     s, p, m = setups.noh2d(40)
     yield "noh2d_1264", setups.shuffled(s, 6), p, 2
+    # Cullen & Dehnen adaptive viscosity
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.sph_viscosity = VISC_CULLEN
+    yield "sod3d_cullen_4000", setups.shuffled(s, 9), p, 3
     # periodic boundaries: copies regenerated at every update_iteration;
     # a few particles start outside the box and are teleported back
     s, p, m = setups.kh2d(40)

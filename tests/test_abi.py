@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_abi_version(lib):
     lib.fsph_abi_version.restype = C.c_int32
-    assert lib.fsph_abi_version() == 1
+    assert lib.fsph_abi_version() == 2
 
 
 def test_params_defaults_match_header(lib):
@@ -37,15 +37,39 @@ def test_params_defaults_match_header(lib):
     lib.fsph_params_default(C.byref(p))
     q = abi.Params.defaults()
     for name, _ in abi.Params._fields_:
-        if name == "reserved":
+        if name in ("reserved", "reserved_pad"):
             continue
         assert getattr(p, name) == getattr(q, name), name
 
 
 def test_struct_sizes():
-    # fsph_soa_view: n + 29 double pointers + id + key
-    assert C.sizeof(abi.SoAView) == 8 * 32
+    # fsph_soa_view: n + 31 double pointers + id + key
+    assert C.sizeof(abi.SoAView) == 8 * 34
     assert C.sizeof(abi.Conserved) == 8 * 8
+
+
+def test_struct_layout_matches_c(tmp_path):
+    """sizeof and the offsets of the last fields, as the C compiler lays
+    the header out, equal the ctypes mirror's."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stddef.h>\n#include <stdio.h>\n#include "fsph.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(fsph_params), '
+        'offsetof(fsph_params, sph_viscosity_delta), sizeof(fsph_soa_view), '
+        'offsetof(fsph_soa_view, ddivvdt), offsetof(fsph_soa_view, key)); return 0; }\n')
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = [C.sizeof(abi.Params), abi.Params.sph_viscosity_delta.offset,
+            C.sizeof(abi.SoAView), abi.SoAView.ddivvdt.offset, abi.SoAView.key.offset]
+    assert got == want
 
 
 def test_create_without_device_fails_cleanly(lib):
