@@ -922,6 +922,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
     int sp = 1;
     int ncand = 0;
     bool chunked = false;
+    bool refdone = false;  // varying h: this lane's list is already filtered
     if(lane == 0)
       stack[0] = 0;
     __syncwarp();
@@ -1024,14 +1025,33 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
             double r = ha < hbd ? hbd : ha;
             return d2 <= r * r;
           };
+          // The reference's node tests (varying h) run after the walk over
+          // each lane's whole list, where every lane of the warp has work;
+          // a list that fills up before then is filtered on the spot and
+          // the lane tests the rest as they come, so the capacity counts the
+          // same pairs as the reference's list.
+          auto refok = [&](int b) {
+            return ref_node_tests_mixed(T, X, Y, Z, H, dim, b, a, xa, ya, za, ha,
+              cax, cay, caz, haf, gnode, g2, fglo, fghi, rlo, ftol);
+          };
           auto append = [&](int b) {
-            if(!nonuni || ref_node_tests_mixed(T, X, Y, Z, H, dim, b, a, xa, ya,
-                            za, ha, cax, cay, caz, haf, gnode, g2, fglo, fghi,
-                            rlo, ftol)) {
-              if(cnt < maxnb)
-                out[slot_off(cnt)] = b;
-              ++cnt;
+            if(nonuni && !refdone && cnt == maxnb) {
+              int kept = 0;
+              for(int j = 0; j < cnt; ++j) {
+                const int e = out[slot_off(j)];
+                if(refok(e)) {
+                  out[slot_off(kept)] = e;
+                  ++kept;
+                }
+              }
+              cnt = kept;
+              refdone = true;
             }
+            if(nonuni && refdone && !refok(b))
+              return;
+            if(cnt < maxnb)
+              out[slot_off(cnt)] = b;
+            ++cnt;
           };
           if(ORDERED) {
             for(int c = 0; c < ncand; ++c) {
@@ -1124,6 +1144,22 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
         if(atomicCAS(&st->code, 0, (int)FSPH_ERR_LIST_OVERFLOW) == 0)
           st->index = a;
         cnt = maxnb;
+      }
+      if(nonuni && !refdone) {
+        // drop the pairs the reference's node tests drop; the list keeps
+        // its order
+        const double xa = X[a], ya = Y[a], za = dim == 3 ? Z[a] : 0.0, ha = H[a];
+        int * o = Ls.idx + list_slot(a, 0, maxnb);
+        int kept = 0;
+        for(int j = 0; j < cnt; ++j) {
+          const int b = o[slot_off(j)];
+          if(ref_node_tests_mixed(T, X, Y, Z, H, dim, b, a, xa, ya, za, ha, cax,
+               cay, caz, haf, gnode, g2, fglo, fghi, rlo, ftol)) {
+            o[slot_off(kept)] = b;
+            ++kept;
+          }
+        }
+        cnt = kept;
       }
       Ls.cnt[a] = cnt;
       {
