@@ -23,6 +23,8 @@ KERNEL_QUINTIC_SPLINE = 1
 KERNEL_WENDLAND_C2 = 2
 KERNEL_WENDLAND_C4 = 3
 KERNEL_WENDLAND_C6 = 4
+KERNEL_GAUSSIAN = 5
+KERNEL_SUPER_GAUSSIAN = 6
 EOS_IDEAL = 0
 VISC_CONSTANT = 0
 VISC_CULLEN = 1

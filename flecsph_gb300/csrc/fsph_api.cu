@@ -87,7 +87,10 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->adaptive = p->adaptive_timestep;
   pp->gamma = p->poly_gamma;
   pp->eta = p->sph_eta;
-  pp->kw = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE) ? 3.0 : 2.0;
+  // kernels::select (kernels.h:753-786)
+  pp->kw = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE ||
+            p->sph_kernel == FSPH_KERNEL_GAUSSIAN ||
+            p->sph_kernel == FSPH_KERNEL_SUPER_GAUSSIAN) ? 3.0 : 2.0;
   pp->alpha = p->sph_viscosity_alpha;
   pp->beta = p->sph_viscosity_beta;
   pp->eps = p->sph_viscosity_epsilon;
@@ -125,11 +128,9 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "dimension must be 2 or 3";
     return false;
   }
-  if(p->sph_kernel != FSPH_KERNEL_CUBIC_SPLINE &&
-     p->sph_kernel != FSPH_KERNEL_WENDLAND_C2 &&
-     p->sph_kernel != FSPH_KERNEL_WENDLAND_C4 &&
-     p->sph_kernel != FSPH_KERNEL_WENDLAND_C6) {
-    *why = "sph_kernel not implemented";
+  if(p->sph_kernel < FSPH_KERNEL_CUBIC_SPLINE ||
+     p->sph_kernel > FSPH_KERNEL_SUPER_GAUSSIAN) {
+    *why = "sph_kernel not implemented (the sinc kernel is not)";
     return false;
   }
   if(p->eos_type != FSPH_EOS_IDEAL && p->eos_type != FSPH_EOS_POLYTROPIC) {

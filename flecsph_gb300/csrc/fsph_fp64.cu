@@ -412,6 +412,12 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
       switch(pp.kernel) {                                                      \
         case FSPH_KERNEL_CUBIC_SPLINE:                                         \
           KERNEL_T<3, FSPH_KERNEL_CUBIC_SPLINE><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_QUINTIC_SPLINE:                                       \
+          KERNEL_T<3, FSPH_KERNEL_QUINTIC_SPLINE><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_GAUSSIAN:                                             \
+          KERNEL_T<3, FSPH_KERNEL_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
+          KERNEL_T<3, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<3, FSPH_KERNEL_WENDLAND_C2><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -424,6 +430,12 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
       switch(pp.kernel) {                                                      \
         case FSPH_KERNEL_CUBIC_SPLINE:                                         \
           KERNEL_T<2, FSPH_KERNEL_CUBIC_SPLINE><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_QUINTIC_SPLINE:                                       \
+          KERNEL_T<2, FSPH_KERNEL_QUINTIC_SPLINE><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_GAUSSIAN:                                             \
+          KERNEL_T<2, FSPH_KERNEL_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
+          KERNEL_T<2, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<2, FSPH_KERNEL_WENDLAND_C2><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \

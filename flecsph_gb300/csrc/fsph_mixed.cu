@@ -101,11 +101,41 @@ __device__ __forceinline__ float sig_c4(int D) {
 __device__ __forceinline__ float sig_c6(int D) {
   return D == 2 ? 78.f / (7.f * FPI) : 1365.f / (64.f * FPI);
 }
+__device__ __forceinline__ float sig_quintic(int D) {
+  return D == 2 ? 63.f / (478.f * FPI) : 81.f / (359.f * FPI);
+}
+__device__ __forceinline__ float sig_gauss(int D) {
+  return D == 2 ? 2.86514256f : 4.85098600f;
+}
+__device__ __forceinline__ float sig_sgauss(int D) {
+  return D == 2 ? 2.86196342f : 4.83280746f;
+}
 
 // W(r, h) for the kernel families of kernels.h (FP32).
 template<int D, int K>
 __device__ __forceinline__ float wfun(float r, float h, float inv_h) {
   const float ihD = D == 3 ? inv_h * inv_h * inv_h : inv_h * inv_h;
+  if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN ||
+     K == FSPH_KERNEL_SUPER_GAUSSIAN) {
+    const float q = 3.f * r * inv_h;
+    if(K == FSPH_KERNEL_GAUSSIAN)
+      return q <= 3.f ? sig_gauss(D) * ihD * expf(-q * q) : 0.f;
+    if(q >= 3.f)
+      return 0.f;
+    if(K == FSPH_KERNEL_SUPER_GAUSSIAN)
+      return sig_sgauss(D) * ihD * expf(-q * q) * ((float)D * 0.5f + 1.f - q * q);
+    const float t3 = 3.f - q, t3s = t3 * t3;
+    float w = t3s * t3s * t3;
+    if(q < 2.f) {
+      const float t2 = 2.f - q, t2s = t2 * t2;
+      w -= 6.f * t2s * t2s * t2;
+    }
+    if(q < 1.f) {
+      const float t1 = 1.f - q, t1s = t1 * t1;
+      w += 15.f * t1s * t1s * t1;
+    }
+    return w * sig_quintic(D) * ihD;
+  }
   if(K == FSPH_KERNEL_CUBIC_SPLINE) {
     float q = 2.f * r * inv_h;
     if(q >= 2.f)
@@ -131,6 +161,35 @@ __device__ __forceinline__ float wfun(float r, float h, float inv_h) {
 template<int D, int K>
 __device__ __forceinline__ float gfac(float r, float h, float inv_h) {
   const float ihD1 = D == 3 ? inv_h * inv_h * inv_h * inv_h : inv_h * inv_h * inv_h;
+  if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN ||
+     K == FSPH_KERNEL_SUPER_GAUSSIAN) {
+    // q = 3 r / h: (dW/dr) / r = 3 sigma / h^(D+1) * g(q) * (3 / h) / q,
+    // with g(q) / q written out so that r = 0 gives a finite factor
+    const float q = 3.f * r * inv_h;
+    if(q >= 3.f)
+      return 0.f;
+    const float e = (K == FSPH_KERNEL_QUINTIC_SPLINE) ? 0.f : expf(-q * q);
+    float gq;
+    if(K == FSPH_KERNEL_GAUSSIAN)
+      gq = -2.f * e * sig_gauss(D);
+    else if(K == FSPH_KERNEL_SUPER_GAUSSIAN)
+      gq = e * (2.f * q * q - ((float)D + 4.f)) * sig_sgauss(D);
+    else {
+      if(q < 1.f)  // -5(3-q)^4 + 30(2-q)^4 - 75(1-q)^4 = q (-120 + 120 q^2 - 50 q^3)
+        gq = -120.f + q * q * (120.f - 50.f * q);
+      else {
+        const float t3 = 3.f - q, t3s = t3 * t3;
+        float g = -5.f * t3s * t3s;
+        if(q < 2.f) {
+          const float t2 = 2.f - q, t2s = t2 * t2;
+          g += 30.f * t2s * t2s;
+        }
+        gq = g / q;
+      }
+      gq *= sig_quintic(D);
+    }
+    return 9.f * ihD1 * inv_h * gq;
+  }
   if(K == FSPH_KERNEL_CUBIC_SPLINE) {
     float q = 2.f * r * inv_h;
     if(q >= 2.f)
@@ -454,6 +513,12 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
       switch(pp.kernel) {                                                      \
         case FSPH_KERNEL_CUBIC_SPLINE:                                         \
           KERNEL_T<3, FSPH_KERNEL_CUBIC_SPLINE><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_QUINTIC_SPLINE:                                       \
+          KERNEL_T<3, FSPH_KERNEL_QUINTIC_SPLINE><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_GAUSSIAN:                                             \
+          KERNEL_T<3, FSPH_KERNEL_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
+          KERNEL_T<3, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<3, FSPH_KERNEL_WENDLAND_C2><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -466,6 +531,12 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
       switch(pp.kernel) {                                                      \
         case FSPH_KERNEL_CUBIC_SPLINE:                                         \
           KERNEL_T<2, FSPH_KERNEL_CUBIC_SPLINE><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_QUINTIC_SPLINE:                                       \
+          KERNEL_T<2, FSPH_KERNEL_QUINTIC_SPLINE><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_GAUSSIAN:                                             \
+          KERNEL_T<2, FSPH_KERNEL_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
+          KERNEL_T<2, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<2, FSPH_KERNEL_WENDLAND_C2><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -516,6 +587,9 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   if(pp.dim == 3) {
     switch(pp.kernel) {
       case FSPH_KERNEL_CUBIC_SPLINE: PICK(3, FSPH_KERNEL_CUBIC_SPLINE); break;
+      case FSPH_KERNEL_QUINTIC_SPLINE: PICK(3, FSPH_KERNEL_QUINTIC_SPLINE); break;
+      case FSPH_KERNEL_GAUSSIAN: PICK(3, FSPH_KERNEL_GAUSSIAN); break;
+      case FSPH_KERNEL_SUPER_GAUSSIAN: PICK(3, FSPH_KERNEL_SUPER_GAUSSIAN); break;
       case FSPH_KERNEL_WENDLAND_C2: PICK(3, FSPH_KERNEL_WENDLAND_C2); break;
       case FSPH_KERNEL_WENDLAND_C4: PICK(3, FSPH_KERNEL_WENDLAND_C4); break;
       default: PICK(3, FSPH_KERNEL_WENDLAND_C6); break;
@@ -524,6 +598,9 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   else {
     switch(pp.kernel) {
       case FSPH_KERNEL_CUBIC_SPLINE: PICK(2, FSPH_KERNEL_CUBIC_SPLINE); break;
+      case FSPH_KERNEL_QUINTIC_SPLINE: PICK(2, FSPH_KERNEL_QUINTIC_SPLINE); break;
+      case FSPH_KERNEL_GAUSSIAN: PICK(2, FSPH_KERNEL_GAUSSIAN); break;
+      case FSPH_KERNEL_SUPER_GAUSSIAN: PICK(2, FSPH_KERNEL_SUPER_GAUSSIAN); break;
       case FSPH_KERNEL_WENDLAND_C2: PICK(2, FSPH_KERNEL_WENDLAND_C2); break;
       case FSPH_KERNEL_WENDLAND_C4: PICK(2, FSPH_KERNEL_WENDLAND_C4); break;
       default: PICK(2, FSPH_KERNEL_WENDLAND_C6); break;

@@ -27,10 +27,54 @@ __device__ __forceinline__ double wc6_sigma(int D) {
   return D == 1 ? 55. / 32.
                 : (D == 2 ? 78. / (7. * FSPH_PI) : 1365. / (64. * FSPH_PI));
 }
+__device__ __forceinline__ double quintic_sigma(int D) {
+  return D == 1 ? 1. / 40.
+                : (D == 2 ? 63. / (478. * FSPH_PI) : 81. / (359. * FSPH_PI));
+}
+// kernels.h:47-55 gives these as long-double literals; the doubles they
+// round to, exactly
+__device__ __forceinline__ double gaussian_sigma(int D) {
+  return D == 1 ? 0x1.b14ea2d5440dap+0
+                : (D == 2 ? 0x1.6ebcfdd1ce67cp+1 : 0x1.36768dfdddb6bp+2);
+}
+__device__ __forceinline__ double super_gaussian_sigma(int D) {
+  return D == 1 ? 0x1.b13778577c0efp+0
+                : (D == 2 ? 0x1.6e54d13f8aff2p+1 : 0x1.354cb7a91e8ccp+2);
+}
 
-// kernel<K,D>(r, h) -- kernels.h:106-121, 282-312, 375-410, 477-512
+// kernel<K,D>(r, h) -- kernels.h:106-121, 167-179, 217-235, 282-312,
+// 375-410, 477-512, 581-590
 template<int D, int K>
 __device__ __forceinline__ double kfun(double r, double h) {
+  if(K == FSPH_KERNEL_QUINTIC_SPLINE) {
+    double rh = 3. * r / h;
+    double result = 0.;
+    if(rh < 3.) {
+      result = pow(3 - rh, 5);
+      if(rh < 2.)
+        result += -6 * pow(2 - rh, 5);
+      if(rh < 1.)
+        result += 15 * pow(1 - rh, 5);
+      double sigma = quintic_sigma(D) / pow(h, (double)D);
+      result *= sigma;
+    }
+    return result;
+  }
+  if(K == FSPH_KERNEL_GAUSSIAN) {
+    double rh = 3. * r / h;
+    double result = 0.;
+    if(rh <= 3.) {
+      double sigma = gaussian_sigma(D) / pow(h, (double)D);
+      result = sigma * exp(-rh * rh);
+    }
+    return result;
+  }
+  if(K == FSPH_KERNEL_SUPER_GAUSSIAN) {
+    double rh = 3. * r / h, rh2 = rh * rh;
+    double sigma = super_gaussian_sigma(D) / pow(h, (double)D);
+    double result = sigma * exp(-rh2) * (D / 2.0 + 1 - rh2);
+    return result * (fabs(rh) < 3.);
+  }
   if(K == FSPH_KERNEL_CUBIC_SPLINE) {
     double rh = 2. * r / h;
     double result = 0.;
@@ -72,13 +116,46 @@ __device__ __forceinline__ double kfun(double r, double h) {
   }
 }
 
-// kernel_gradient<K,D>(vecP, h) -- kernels.h:132-153, 322-361, 435-463, 536-566
+// kernel_gradient<K,D>(vecP, h) -- kernels.h:132-153, 189-205, 246-270,
+// 322-361, 435-463, 536-566, 600-613
 template<int D, int K>
 __device__ __forceinline__ void kgrad(const double * p, double h, double * out) {
   double r = 0;
   for(int d = 0; d < D; ++d)
     r += p[d] * p[d];
   r = sqrt(r);
+  if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN) {
+    double rh = 3. * r / h;
+    for(int d = 0; d < D; ++d)
+      out[d] = 0.0;
+    if(rh < 3.) {
+      double sigma, dWdr;
+      if(K == FSPH_KERNEL_QUINTIC_SPLINE) {
+        sigma = 3. * quintic_sigma(D) / pow(h, (double)(D + 1));
+        dWdr = -5. * pow(3 - rh, 4);
+        if(rh < 2.)
+          dWdr += 30. * pow(2 - rh, 4);
+        if(rh < 1.)
+          dWdr += -75. * pow(1 - rh, 4);
+      }
+      else {
+        sigma = 3. * gaussian_sigma(D) / pow(h, (double)(D + 1));
+        dWdr = -2. * rh * exp(-rh * rh);
+      }
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * sigma * dWdr / (r + FSPH_TINY);
+    }
+    return;
+  }
+  if(K == FSPH_KERNEL_SUPER_GAUSSIAN) {
+    double rh = 3. * r / h;
+    double sigma = 3. * super_gaussian_sigma(D) / pow(h, (double)(D + 1));
+    double dWdr = exp(-rh * rh) * (2. * pow(rh, 3.) - (D + 4.) * rh);
+    double f = (rh < 3.0) * (sigma * dWdr / (r + FSPH_TINY));
+    for(int d = 0; d < D; ++d)
+      out[d] = p[d] * f;
+    return;
+  }
   if(K == FSPH_KERNEL_CUBIC_SPLINE) {
     double rh = 2. * r / h;
     for(int d = 0; d < D; ++d)

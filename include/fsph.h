@@ -73,7 +73,9 @@ enum fsph_kernel {
   FSPH_KERNEL_QUINTIC_SPLINE = 1,
   FSPH_KERNEL_WENDLAND_C2 = 2,
   FSPH_KERNEL_WENDLAND_C4 = 3,
-  FSPH_KERNEL_WENDLAND_C6 = 4
+  FSPH_KERNEL_WENDLAND_C6 = 4,
+  FSPH_KERNEL_GAUSSIAN = 5,
+  FSPH_KERNEL_SUPER_GAUSSIAN = 6
 };
 /* Same numbering as param::eos_type_keyword (include/params.h:139-145). */
 enum fsph_eos { FSPH_EOS_IDEAL = 0, FSPH_EOS_POLYTROPIC = 1 };

@@ -136,12 +136,49 @@ static const double wc2_sigma[3] = {1.25, 7. / M_PI, 21. / (2. * M_PI)};
 static const double wc4_sigma[3] = {1.5, 9. / M_PI, 495. / (32. * M_PI)};
 static const double wc6_sigma[3] = {55. / 32., 78. / (7. * M_PI),
   1365. / (64. * M_PI)};
+static const double quintic_sigma[3] = {1. / 40., 63. / (478. * M_PI),
+  81. / (359. * M_PI)};
+/* kernels.h:47-55 writes these as long-double literals; the doubles they
+ * round to */
+static const double gaussian_sigma[3] = {0x1.b14ea2d5440dap+0,
+  0x1.6ebcfdd1ce67cp+1, 0x1.36768dfdddb6bp+2};
+static const double super_gaussian_sigma[3] = {0x1.b13778577c0efp+0,
+  0x1.6e54d13f8aff2p+1, 0x1.354cb7a91e8ccp+2};
 
 /* kernel<K,D>(r, h): kernels.h:106-121 (cubic), :282-312 (C2), :375-410
  * (C4), :477-512 (C6). */
 static double kfun(const orc_ctx * c, double r, double h) {
   const int D = c->D;
   switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_QUINTIC_SPLINE: { /* kernels.h:217-235 */
+      double rh = 3. * r / h;
+      double result = 0.;
+      if(rh < 3.) {
+        result = pow(3 - rh, 5);
+        if(rh < 2.)
+          result += -6 * pow(2 - rh, 5);
+        if(rh < 1.)
+          result += 15 * pow(1 - rh, 5);
+        double sigma = quintic_sigma[D - 1] / pow(h, D);
+        result *= sigma;
+      }
+      return result;
+    }
+    case FSPH_KERNEL_GAUSSIAN: { /* kernels.h:167-179 */
+      double rh = 3. * r / h;
+      double result = 0.;
+      if(rh <= 3.) {
+        double sigma = gaussian_sigma[D - 1] / pow(h, D);
+        result = sigma * exp(-rh * rh);
+      }
+      return result;
+    }
+    case FSPH_KERNEL_SUPER_GAUSSIAN: { /* kernels.h:581-590 */
+      double rh = 3. * r / h, rh2 = rh * rh;
+      double sigma = super_gaussian_sigma[D - 1] / pow(h, D);
+      double result = sigma * exp(-rh2) * (D / 2.0 + 1 - rh2);
+      return result * (fabs(rh) < 3.);
+    }
     case FSPH_KERNEL_CUBIC_SPLINE: {
       double rh = 2. * r / h;
       double result = 0.;
@@ -194,6 +231,39 @@ static void kgrad(const orc_ctx * c, const double * p, double h, double * out) {
     r += p[d] * p[d];
   r = sqrt(r); /* flecsi::magnitude */
   switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_QUINTIC_SPLINE:   /* kernels.h:246-270 */
+    case FSPH_KERNEL_GAUSSIAN: {       /* kernels.h:189-205 */
+      double rh = 3. * r / h;
+      for(int d = 0; d < D; ++d)
+        out[d] = 0.0;
+      if(rh < 3.) {
+        double sigma, dWdr;
+        if(c->p.sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE) {
+          sigma = 3. * quintic_sigma[D - 1] / pow(h, D + 1);
+          dWdr = -5. * pow(3 - rh, 4);
+          if(rh < 2.)
+            dWdr += 30. * pow(2 - rh, 4);
+          if(rh < 1.)
+            dWdr += -75. * pow(1 - rh, 4);
+        }
+        else {
+          sigma = 3. * gaussian_sigma[D - 1] / pow(h, D + 1);
+          dWdr = -2. * rh * exp(-rh * rh);
+        }
+        for(int d = 0; d < D; ++d)
+          out[d] = p[d] * sigma * dWdr / (r + TINY);
+      }
+      return;
+    }
+    case FSPH_KERNEL_SUPER_GAUSSIAN: { /* kernels.h:600-613 */
+      double rh = 3. * r / h;
+      double sigma = 3. * super_gaussian_sigma[D - 1] / pow(h, D + 1);
+      double dWdr = exp(-rh * rh) * (2. * pow(rh, 3.) - (D + 4.) * rh);
+      double f = (rh < 3.0) * (sigma * dWdr / (r + TINY));
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * f;
+      return;
+    }
     case FSPH_KERNEL_CUBIC_SPLINE: {
       double rh = 2. * r / h;
       for(int d = 0; d < D; ++d)
@@ -305,7 +375,9 @@ orc_ctx * orc_create(const fsph_params * p) {
   c->D = p->dimension;
   c->nthreads = 1;
   /* kernels::select (kernels.h:753-767) */
-  c->kernel_width = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE) ? 3.0 : 2.0;
+  c->kernel_width = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE ||
+                     p->sph_kernel == FSPH_KERNEL_GAUSSIAN ||
+                     p->sph_kernel == FSPH_KERNEL_SUPER_GAUSSIAN) ? 3.0 : 2.0;
   return c;
 }
 

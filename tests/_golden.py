@@ -21,7 +21,12 @@ def load(name):
     # room for the longest list of this fixture (the variable-h polytrope
     # has particles with several hundred neighbours)
     longest = int(np.diff(d["nb_offsets"]).max())
-    params.max_neighbors = max(params.max_neighbors, longest + longest // 4 + 32)
+    want = longest + longest // 4 + 32
+    if params.sph_variable_h:
+        # h is recomputed every step (a kernel of width 3 makes it grow at
+        # the first one): room for the lists of later iterations
+        want = max(want, 8 * longest)
+    params.max_neighbors = min(4096, max(params.max_neighbors, want))
     state = {f: np.ascontiguousarray(d["in_" + f]) for f in DOUBLE_FIELDS}
     state["id"] = np.ascontiguousarray(d["in_id"])
     state["key"] = np.zeros(len(state["x"]), np.uint64)

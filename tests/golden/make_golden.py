@@ -24,7 +24,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from flecsph_gb300 import setups  # noqa: E402
-from flecsph_gb300.abi import DOUBLE_FIELDS, KERNEL_WENDLAND_C4, VISC_CULLEN  # noqa: E402
+from flecsph_gb300.abi import (DOUBLE_FIELDS, KERNEL_QUINTIC_SPLINE,  # noqa: E402
+                               KERNEL_SUPER_GAUSSIAN, KERNEL_WENDLAND_C4, VISC_CULLEN)
 import pyoracle  # noqa: E402
 
 
@@ -52,6 +53,14 @@ def cases():
     s, p, m = setups.sod3d(40, 10, 10)
     p.sph_viscosity = VISC_CULLEN
     yield "sod3d_cullen_4000", setups.shuffled(s, 9), p, 3
+    # the kernels of kernel width 3
+    s, p, m = setups.sod2d(100, 10)
+    p.sph_kernel = KERNEL_SUPER_GAUSSIAN
+    yield "sod2d_supergauss_1000", setups.shuffled(s, 10), p, 2
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.sph_kernel = KERNEL_QUINTIC_SPLINE
+    p.sph_variable_h = 1
+    yield "sod3d_quintic_varh_4000", setups.shuffled(s, 11), p, 2
     # periodic boundaries: copies regenerated at every update_iteration;
     # a few particles start outside the box and are teleported back
     s, p, m = setups.kh2d(40)
