@@ -25,6 +25,7 @@ KERNEL_WENDLAND_C4 = 3
 KERNEL_WENDLAND_C6 = 4
 KERNEL_GAUSSIAN = 5
 KERNEL_SUPER_GAUSSIAN = 6
+KERNEL_SINC = 7
 EOS_IDEAL = 0
 VISC_CONSTANT = 0
 VISC_CULLEN = 1
@@ -90,6 +91,7 @@ class Params(C.Structure):
         ("sph_viscosity_alpha_max", C.c_double),
         ("sph_viscosity_l", C.c_double),
         ("sph_viscosity_delta", C.c_double),
+        ("sph_sinc_index", C.c_double),
         ("reserved", C.c_int32 * 8),
     ]
 
@@ -128,6 +130,7 @@ class Params(C.Structure):
         p.sph_viscosity_alpha_max = 1.0
         p.sph_viscosity_l = 0.05
         p.sph_viscosity_delta = 1.0
+        p.sph_sinc_index = 4.0
         for k, v in kw.items():
             if not hasattr(p, k):
                 raise AttributeError(k)

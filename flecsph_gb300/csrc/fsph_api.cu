@@ -2,6 +2,7 @@
 // body_system / physics call surface, sequenced on one CUDA stream.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -91,6 +92,18 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->kw = (p->sph_kernel == FSPH_KERNEL_QUINTIC_SPLINE ||
             p->sph_kernel == FSPH_KERNEL_GAUSSIAN ||
             p->sph_kernel == FSPH_KERNEL_SUPER_GAUSSIAN) ? 3.0 : 2.0;
+  // set_sinc_kernel_normalization (kernels.h:67-77)
+  {
+    const double b0[3] = {-1.5404568e-2, 5.2245027e-2, 2.7012593e-2};
+    const double b1[3] = {3.6632876e-1, 1.3090245e-1, 2.0410827e-2};
+    const double b2[3] = {-4.6519576e-4, 1.9358485e-2, 3.7451957e-3};
+    const double b3[3] = {7.3658324e-2, -6.1642906e-3, 4.7013839e-2};
+    const double si = p->sph_sinc_index, sq = sqrt(si), s2 = si * si;
+    pp->sinc_index = si;
+    pp->sinc_sigma[0] = 2. * (b0[0] + b1[0] * sq + b2[0] * si + b3[0] / sq);
+    pp->sinc_sigma[1] = 4. * (b0[1] + b1[1] * si + b2[1] / si + b3[1] / s2);
+    pp->sinc_sigma[2] = 8. * (b0[2] + b1[2] * sq + b2[2] * si + b3[2] * sq * si);
+  }
   pp->alpha = p->sph_viscosity_alpha;
   pp->beta = p->sph_viscosity_beta;
   pp->eps = p->sph_viscosity_epsilon;
@@ -128,9 +141,12 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "dimension must be 2 or 3";
     return false;
   }
-  if(p->sph_kernel < FSPH_KERNEL_CUBIC_SPLINE ||
-     p->sph_kernel > FSPH_KERNEL_SUPER_GAUSSIAN) {
-    *why = "sph_kernel not implemented (the sinc kernel is not)";
+  if(p->sph_kernel < FSPH_KERNEL_CUBIC_SPLINE || p->sph_kernel > FSPH_KERNEL_SINC) {
+    *why = "unknown sph_kernel";
+    return false;
+  }
+  if(p->sph_kernel == FSPH_KERNEL_SINC && !(p->sph_sinc_index > 1.0)) {
+    *why = "sph_sinc_index must exceed 1";
     return false;
   }
   if(p->eos_type != FSPH_EOS_IDEAL && p->eos_type != FSPH_EOS_POLYTROPIC) {
@@ -211,6 +227,7 @@ void fsph_params_default(fsph_params * p) {
   p->sph_viscosity_alpha_max = 1.0;
   p->sph_viscosity_l = 0.05;
   p->sph_viscosity_delta = 1.0;
+  p->sph_sinc_index = 4.0;
 }
 
 int32_t fsph_abi_version(void) { return FSPH_ABI_VERSION; }

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
       r += d2 * d2;
     }
     r = sqrt(r);
-    double Wab = kfun<D, K>(r, .5 * (h_a + H[b]));
+    double Wab = kfun<D, K>(r, .5 * (h_a + H[b]), pp);
     rho_a += M[b] * Wab;
   }
   if(!(rho_a > 0))
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
       double pos_ab[3] = {pa[0] - X[b], pa[1] - Y[b], D == 3 ? pa[2] - Z[b] : 0.0};
       const double h_ab = .5 * (h_a + H[b]);
       double DiWab[3];
-      kgrad<D, K>(pos_ab, h_ab, DiWab);
+      kgrad<D, K>(pos_ab, h_ab, DiWab, pp);
       double dot = 0.0;
       for(int d = 0; d < D; ++d)
         dot += va[d] * DiWab[d];
@@ -142,8 +142,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_alpha_cullen(Particles P,
     vsig = vsig < cand ? cand : vsig;        // std::max(vsig, cand)
     const double h_ab = .5 * (h_a + H[b]);
     double DiWa[3];
-    kgrad<D, K>(pos_ab, h_ab, DiWa);
-    const double Wab = kfun<D, K>(dist, h_ab);
+    kgrad<D, K>(pos_ab, h_ab, DiWa, pp);
+    const double Wab = kfun<D, K>(dist, h_ab, pp);
     const double dvb = DV[b];
     const double sgn = dvb > 0.0 ? 1.0 : (dvb < 0.0 ? -1.0 : dvb);
     R_a += sgn * M[b] * Wab;
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_accel(Particles P,
     const double rho_ab = .5 * (rho_a + rho_b);
     const double c_ab = .5 * (c_a + CS[b]);
     const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
-    kgrad<D, K>(pos_ab, h_ab, DiWa);
+    kgrad<D, K>(pos_ab, h_ab, DiWa, pp);
     const double Prho2_b = PR[b] / (rho_b * rho_b);
     const double s = -m_b * (Prho2_a + Prho2_b + Pi);
     for(int d = 0; d < D; ++d)
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dudt(Particles P,
     const double rho_ab = .5 * (rho_a + RHO[b]);
     const double c_ab = .5 * (c_a + CS[b]);
     const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
-    kgrad<D, K>(pos_ab, h_ab, DiWab);
+    kgrad<D, K>(pos_ab, h_ab, DiWab, pp);
     double vdw = 0;
     for(int d = 0; d < D; ++d)
       vdw += vel_ab[d] * DiWab[d];
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
     const double rho_ab = .5 * (rho_a + rho_b);
     const double c_ab = .5 * (c_a + CS[b]);
     const double Pi = visc_pi_pp(pp, P.f[F_ALPHA], a, b, rho_ab, c_ab, mu_ab);
-    kgrad<D, K>(pos_ab, h_ab, DiWab);
+    kgrad<D, K>(pos_ab, h_ab, DiWab, pp);
     double vad = 0, vbd = 0;
     for(int d = 0; d < D; ++d)
       vad += va[d] * DiWab[d];
@@ -418,6 +418,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
           KERNEL_T<3, FSPH_KERNEL_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
           KERNEL_T<3, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SINC:                                                 \
+          KERNEL_T<3, FSPH_KERNEL_SINC><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<3, FSPH_KERNEL_WENDLAND_C2><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -436,6 +438,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_dedt(Particles P,
           KERNEL_T<2, FSPH_KERNEL_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
           KERNEL_T<2, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SINC:                                                 \
+          KERNEL_T<2, FSPH_KERNEL_SINC><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<2, FSPH_KERNEL_WENDLAND_C2><<<nb_, PAIR_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \

@@ -47,6 +47,7 @@ struct PhysParams {
   int cullen;  // sph_viscosity == visc_cullen
   double gamma, eta, kw, alpha, beta, eps, cfl;
   double alpha_max, visc_l, visc_delta;  // visc_cullen parameters
+  double sinc_index, sinc_sigma[3];       // sinc kernel power and norms
   double out_screen_dt, out_scalar_dt, out_h5data_dt;
   double G;
 };

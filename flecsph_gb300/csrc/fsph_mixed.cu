@@ -113,8 +113,17 @@ __device__ __forceinline__ float sig_sgauss(int D) {
 
 // W(r, h) for the kernel families of kernels.h (FP32).
 template<int D, int K>
-__device__ __forceinline__ float wfun(float r, float h, float inv_h) {
+__device__ __forceinline__ float wfun(float r, float h, float inv_h,
+  const PhysParams & pp) {
   const float ihD = D == 3 ? inv_h * inv_h * inv_h : inv_h * inv_h;
+  if(K == FSPH_KERNEL_SINC) {
+    const float q = r * inv_h;
+    if(q >= 1.f)
+      return 0.f;
+    const float x = FPI * q;
+    const float sinc = x > 1e-4f ? sinf(x) / x : 1.f - x * x * (1.f / 6.f);
+    return (float)pp.sinc_sigma[D - 1] * ihD * powf(sinc, (float)pp.sinc_index);
+  }
   if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN ||
      K == FSPH_KERNEL_SUPER_GAUSSIAN) {
     const float q = 3.f * r * inv_h;
@@ -159,8 +168,30 @@ __device__ __forceinline__ float wfun(float r, float h, float inv_h) {
 
 // grad_a W = x_ab * F(r, h); returns F = (dW/dr) / r.
 template<int D, int K>
-__device__ __forceinline__ float gfac(float r, float h, float inv_h) {
+__device__ __forceinline__ float gfac(float r, float h, float inv_h,
+  const PhysParams & pp) {
   const float ihD1 = D == 3 ? inv_h * inv_h * inv_h * inv_h : inv_h * inv_h * inv_h;
+  if(K == FSPH_KERNEL_SINC) {
+    // (dW/dr) / r = sigma / h^(D+2) (-n pi^2 sinc^(n-1)) (sin x - x cos x) / x^3
+    const float q = r * inv_h;
+    if(q >= 1.f)
+      return 0.f;
+    const float x = FPI * q, x2 = x * x;
+    const float n = (float)pp.sinc_index;
+    float sinc, g3;
+    if(x > 0.05f) {
+      float sx, cx;
+      sincosf(x, &sx, &cx);
+      sinc = sx / x;
+      g3 = (sx - x * cx) / (x2 * x);
+    }
+    else {
+      sinc = 1.f - x2 * (1.f / 6.f);
+      g3 = 1.f / 3.f - x2 * (1.f / 30.f - x2 * (1.f / 840.f));
+    }
+    return (float)pp.sinc_sigma[D - 1] * ihD1 * inv_h * (-n * FPI * FPI) *
+           powf(sinc, n - 1.f) * g3;
+  }
   if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN ||
      K == FSPH_KERNEL_SUPER_GAUSSIAN) {
     // q = 3 r / h: (dW/dr) / r = 3 sigma / h^(D+1) * g(q) * (3 / h) / q,
@@ -254,7 +285,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
       const float ih = 1.0f / hab;
-      const float w = mb * wfun<D, K>(sqrtf(g.r2), hab, ih);
+      const float w = mb * wfun<D, K>(sqrtf(g.r2), hab, ih, pp);
       kahan(sum, comp, j0 + u < cnt ? w : 0.f);
     }
   }
@@ -367,7 +398,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
       const float ih = 1.0f / hab;
       const float r = sqrtf(g.r2);
-      const float f = gfac<D, K>(r, hab, ih);
+      const float f = gfac<D, K>(r, hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
       const float4 tb = Kp.thermo[b];
       const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
@@ -436,7 +467,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
       const float ih = 1.0f / hab;
-      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
+      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
       const float4 vb = Kp.vel[b];
       const float4 tb = Kp.thermo[b];
@@ -484,7 +515,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
       const float ih = 1.0f / hab;
-      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih);
+      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
       const float4 vb = Kp.vel[b];
       const float4 tb = Kp.thermo[b];
@@ -519,6 +550,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
           KERNEL_T<3, FSPH_KERNEL_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
           KERNEL_T<3, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SINC:                                                 \
+          KERNEL_T<3, FSPH_KERNEL_SINC><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<3, FSPH_KERNEL_WENDLAND_C2><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -537,6 +570,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
           KERNEL_T<2, FSPH_KERNEL_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_SUPER_GAUSSIAN:                                       \
           KERNEL_T<2, FSPH_KERNEL_SUPER_GAUSSIAN><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
+        case FSPH_KERNEL_SINC:                                                 \
+          KERNEL_T<2, FSPH_KERNEL_SINC><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C2:                                          \
           KERNEL_T<2, FSPH_KERNEL_WENDLAND_C2><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); break; \
         case FSPH_KERNEL_WENDLAND_C4:                                          \
@@ -590,6 +625,7 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
       case FSPH_KERNEL_QUINTIC_SPLINE: PICK(3, FSPH_KERNEL_QUINTIC_SPLINE); break;
       case FSPH_KERNEL_GAUSSIAN: PICK(3, FSPH_KERNEL_GAUSSIAN); break;
       case FSPH_KERNEL_SUPER_GAUSSIAN: PICK(3, FSPH_KERNEL_SUPER_GAUSSIAN); break;
+      case FSPH_KERNEL_SINC: PICK(3, FSPH_KERNEL_SINC); break;
       case FSPH_KERNEL_WENDLAND_C2: PICK(3, FSPH_KERNEL_WENDLAND_C2); break;
       case FSPH_KERNEL_WENDLAND_C4: PICK(3, FSPH_KERNEL_WENDLAND_C4); break;
       default: PICK(3, FSPH_KERNEL_WENDLAND_C6); break;
@@ -601,6 +637,7 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
       case FSPH_KERNEL_QUINTIC_SPLINE: PICK(2, FSPH_KERNEL_QUINTIC_SPLINE); break;
       case FSPH_KERNEL_GAUSSIAN: PICK(2, FSPH_KERNEL_GAUSSIAN); break;
       case FSPH_KERNEL_SUPER_GAUSSIAN: PICK(2, FSPH_KERNEL_SUPER_GAUSSIAN); break;
+      case FSPH_KERNEL_SINC: PICK(2, FSPH_KERNEL_SINC); break;
       case FSPH_KERNEL_WENDLAND_C2: PICK(2, FSPH_KERNEL_WENDLAND_C2); break;
       case FSPH_KERNEL_WENDLAND_C4: PICK(2, FSPH_KERNEL_WENDLAND_C4); break;
       default: PICK(2, FSPH_KERNEL_WENDLAND_C6); break;

@@ -45,7 +45,29 @@ __device__ __forceinline__ double super_gaussian_sigma(int D) {
 // kernel<K,D>(r, h) -- kernels.h:106-121, 167-179, 217-235, 282-312,
 // 375-410, 477-512, 581-590
 template<int D, int K>
-__device__ __forceinline__ double kfun(double r, double h) {
+__device__ __forceinline__ double kfun(double r, double h, const PhysParams & pp) {
+  if(K == FSPH_KERNEL_SINC) {  // kernels.h:633-661
+    double rh = fabs(r / h), rh2;
+    const double eps = 1e-24;
+    const double eps_root = sqrt(eps);
+    const double eps_root4 = sqrt(eps_root);
+    double result = 0.;
+    if(rh < 1.) {
+      double hd = h;
+      for(int i = 1; i < D; i++)
+        hd *= h;
+      double sinc = 1.0;
+      rh *= FSPH_PI;
+      if(rh > eps_root4)
+        sinc = sin(rh) / rh;
+      else if(rh > eps) {
+        rh2 = rh * rh;
+        sinc += rh2 * (.05 * rh2 - 1.) / 6.;
+      }
+      result = pp.sinc_sigma[D - 1] / hd * pow(sinc, pp.sinc_index);
+    }
+    return result;
+  }
   if(K == FSPH_KERNEL_QUINTIC_SPLINE) {
     double rh = 3. * r / h;
     double result = 0.;
@@ -119,11 +141,40 @@ __device__ __forceinline__ double kfun(double r, double h) {
 // kernel_gradient<K,D>(vecP, h) -- kernels.h:132-153, 189-205, 246-270,
 // 322-361, 435-463, 536-566, 600-613
 template<int D, int K>
-__device__ __forceinline__ void kgrad(const double * p, double h, double * out) {
+__device__ __forceinline__ void kgrad(const double * p, double h, double * out,
+  const PhysParams & pp) {
   double r = 0;
   for(int d = 0; d < D; ++d)
     r += p[d] * p[d];
   r = sqrt(r);
+  if(K == FSPH_KERNEL_SINC) {  // kernels.h:671-698
+    double rh = fabs(r / h), rh2;
+    const double eps = 1e-24;
+    const double eps_root = sqrt(eps);
+    const double eps_root4 = sqrt(eps_root);
+    const double n = pp.sinc_index;
+    for(int d = 0; d < D; ++d)
+      out[d] = 0.0;
+    if(rh < 1.) {
+      double hd = h * h;
+      for(int i = 1; i < D; i++)
+        hd *= h;
+      double sigma = pp.sinc_sigma[D - 1] / hd;
+      rh *= FSPH_PI;
+      double dWdr = 0.0;
+      if(rh > eps_root4) {
+        double sinc = sin(rh) / rh, cosx = cos(rh) / rh;
+        dWdr = -n * pow(sinc, n - 1) * FSPH_PI * (sinc / rh - cosx);
+      }
+      else if(rh > eps) {
+        rh2 = rh * rh;
+        dWdr = -n * rh / 3. * FSPH_PI * (1 - .5 * rh2 * (.2 - (n - 1) / 18));
+      }
+      for(int d = 0; d < D; ++d)
+        out[d] = p[d] * sigma * dWdr / (r + FSPH_TINY);
+    }
+    return;
+  }
   if(K == FSPH_KERNEL_QUINTIC_SPLINE || K == FSPH_KERNEL_GAUSSIAN) {
     double rh = 3. * r / h;
     for(int d = 0; d < D; ++d)

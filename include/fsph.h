@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FSPH_ABI_VERSION 2
+#define FSPH_ABI_VERSION 3
 
 /* Status codes.  They replace the reference's assert()/mpi_assert() aborts
  * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
@@ -75,7 +75,8 @@ enum fsph_kernel {
   FSPH_KERNEL_WENDLAND_C4 = 3,
   FSPH_KERNEL_WENDLAND_C6 = 4,
   FSPH_KERNEL_GAUSSIAN = 5,
-  FSPH_KERNEL_SUPER_GAUSSIAN = 6
+  FSPH_KERNEL_SUPER_GAUSSIAN = 6,
+  FSPH_KERNEL_SINC = 7
 };
 /* Same numbering as param::eos_type_keyword (include/params.h:139-145). */
 enum fsph_eos { FSPH_EOS_IDEAL = 0, FSPH_EOS_POLYTROPIC = 1 };
@@ -133,6 +134,7 @@ typedef struct fsph_params {
   double sph_viscosity_alpha_max;    /* [516] 1.0 */
   double sph_viscosity_l;            /* [523] 0.05 */
   double sph_viscosity_delta;        /* [529] 1.0 */
+  double sph_sinc_index;             /* [232] 4.0, sinc kernel power */
   int32_t reserved[8];
 } fsph_params;
 

@@ -147,9 +147,45 @@ static const double super_gaussian_sigma[3] = {0x1.b13778577c0efp+0,
 
 /* kernel<K,D>(r, h): kernels.h:106-121 (cubic), :282-312 (C2), :375-410
  * (C4), :477-512 (C6). */
+/* set_sinc_kernel_normalization (kernels.h:67-77) */
+static double sinc_sigma(const orc_ctx * c) {
+  static const double b0[3] = {-1.5404568e-2, 5.2245027e-2, 2.7012593e-2};
+  static const double b1[3] = {3.6632876e-1, 1.3090245e-1, 2.0410827e-2};
+  static const double b2[3] = {-4.6519576e-4, 1.9358485e-2, 3.7451957e-3};
+  static const double b3[3] = {7.3658324e-2, -6.1642906e-3, 4.7013839e-2};
+  const double si = c->p.sph_sinc_index, sq = sqrt(si), s2 = si * si;
+  if(c->D == 1)
+    return 2. * (b0[0] + b1[0] * sq + b2[0] * si + b3[0] / sq);
+  if(c->D == 2)
+    return 4. * (b0[1] + b1[1] * si + b2[1] / si + b3[1] / s2);
+  return 8. * (b0[2] + b1[2] * sq + b2[2] * si + b3[2] * sq * si);
+}
+
 static double kfun(const orc_ctx * c, double r, double h) {
   const int D = c->D;
   switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_SINC: { /* kernels.h:633-661 */
+      double rh = fabs(r / h), rh2;
+      const double eps = 1e-24;
+      const double eps_root = sqrt(eps);
+      const double eps_root4 = sqrt(eps_root);
+      double result = 0.;
+      if(rh < 1.) {
+        double hd = h;
+        for(int i = 1; i < D; i++)
+          hd *= h;
+        double sinc = 1.0;
+        rh *= M_PI;
+        if(rh > eps_root4)
+          sinc = sin(rh) / rh;
+        else if(rh > eps) {
+          rh2 = rh * rh;
+          sinc += rh2 * (.05 * rh2 - 1.) / 6.;
+        }
+        result = sinc_sigma(c) / hd * pow(sinc, c->p.sph_sinc_index);
+      }
+      return result;
+    }
     case FSPH_KERNEL_QUINTIC_SPLINE: { /* kernels.h:217-235 */
       double rh = 3. * r / h;
       double result = 0.;
@@ -231,6 +267,34 @@ static void kgrad(const orc_ctx * c, const double * p, double h, double * out) {
     r += p[d] * p[d];
   r = sqrt(r); /* flecsi::magnitude */
   switch(c->p.sph_kernel) {
+    case FSPH_KERNEL_SINC: { /* kernels.h:671-698 */
+      double rh = fabs(r / h), rh2;
+      const double eps = 1e-24;
+      const double eps_root = sqrt(eps);
+      const double eps_root4 = sqrt(eps_root);
+      const double n = c->p.sph_sinc_index;
+      for(int d = 0; d < D; ++d)
+        out[d] = 0.0;
+      if(rh < 1.) {
+        double hd = h * h;
+        for(int i = 1; i < D; i++)
+          hd *= h;
+        double sigma = sinc_sigma(c) / hd;
+        rh *= M_PI;
+        double dWdr = 0.0;
+        if(rh > eps_root4) {
+          double sinc = sin(rh) / rh, cosx = cos(rh) / rh;
+          dWdr = -n * pow(sinc, n - 1) * M_PI * (sinc / rh - cosx);
+        }
+        else if(rh > eps) {
+          rh2 = rh * rh;
+          dWdr = -n * rh / 3. * M_PI * (1 - .5 * rh2 * (.2 - (n - 1) / 18));
+        }
+        for(int d = 0; d < D; ++d)
+          out[d] = p[d] * sigma * dWdr / (r + TINY);
+      }
+      return;
+    }
     case FSPH_KERNEL_QUINTIC_SPLINE:   /* kernels.h:246-270 */
     case FSPH_KERNEL_GAUSSIAN: {       /* kernels.h:189-205 */
       double rh = 3. * r / h;

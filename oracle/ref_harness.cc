@@ -45,6 +45,7 @@ static void set_params(const fsph_params * p) {
   _sph_viscosity_alpha_max = p->sph_viscosity_alpha_max;
   _sph_viscosity_l = p->sph_viscosity_l;
   _sph_viscosity_delta = p->sph_viscosity_delta;
+  _sph_sinc_index = p->sph_sinc_index;
   _sph_viscosity_alpha = p->sph_viscosity_alpha;
   _sph_viscosity_beta = p->sph_viscosity_beta;
   _sph_viscosity_epsilon = p->sph_viscosity_epsilon;

@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_abi_version(lib):
     lib.fsph_abi_version.restype = C.c_int32
-    assert lib.fsph_abi_version() == 2
+    assert lib.fsph_abi_version() == 3
 
 
 def test_params_defaults_match_header(lib):

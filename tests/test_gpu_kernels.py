@@ -1,4 +1,4 @@
-"""The quintic spline, Gaussian and super-Gaussian kernels on the GPU: FP64
+"""The quintic spline, Gaussian, super-Gaussian and sinc kernels on the GPU: FP64
 mode against the CPU oracle to 1e-12 over full driver iterations, and the
 mixed path's one-pass accelerations against FP64 from the same state."""
 import numpy as np
@@ -6,10 +6,11 @@ import pytest
 
 from flecsph_gb300 import setups
 from flecsph_gb300.abi import (DOUBLE_FIELDS, KERNEL_GAUSSIAN, KERNEL_QUINTIC_SPLINE,
-                               KERNEL_SUPER_GAUSSIAN, PRECISION_FP64, PRECISION_MIXED)
+                               KERNEL_SINC, KERNEL_SUPER_GAUSSIAN, PRECISION_FP64,
+                               PRECISION_MIXED)
 
 pytestmark = pytest.mark.gpu
-KERNELS = [KERNEL_QUINTIC_SPLINE, KERNEL_GAUSSIAN, KERNEL_SUPER_GAUSSIAN]
+KERNELS = [KERNEL_QUINTIC_SPLINE, KERNEL_GAUSSIAN, KERNEL_SUPER_GAUSSIAN, KERNEL_SINC]
 
 
 def normwise(a, b):

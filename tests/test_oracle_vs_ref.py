@@ -143,15 +143,17 @@ def test_cullen_dehnen_viscosity(oracle_port, case):
         assert last["alpha"].max() > 0     # the trigger fired at the shock
 
 
-@pytest.mark.parametrize("kernel", [1, 5, 6])
-def test_quintic_and_gaussian_kernels(oracle_port, kernel):
-    """The quintic spline, Gaussian and super-Gaussian kernels
-    (kernels.h:167-270, 581-613) with their kernel width of 3 through the
-    smoothing-length update, bit-exact against the compiled reference."""
+@pytest.mark.parametrize("kernel", [1, 5, 6, 7])
+def test_quintic_gaussian_sinc_kernels(oracle_port, kernel):
+    """The quintic spline, Gaussian, super-Gaussian (kernel width 3) and sinc
+    kernels (kernels.h:167-270, 581-698) through the smoothing-length
+    update, bit-exact against the compiled reference."""
     from flecsph_gb300 import setups
     s, p, m = setups.sod3d(40, 10, 10)
     p.sph_kernel = kernel
     p.sph_variable_h = 1
+    if kernel == 7:
+        p.sph_sinc_index = 5.0
     s = setups.shuffled(s, 51)
     if not oracle_port.have_ref(3):
         if not oracle_port.build_ref():
