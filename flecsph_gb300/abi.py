@@ -30,6 +30,9 @@ EOS_IDEAL = 0
 VISC_CONSTANT = 0
 VISC_CULLEN = 1
 EOS_POLYTROPIC = 1
+EOS_WD = 2
+EOS_PPT = 3
+EOS_NO_EOS = 4
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
@@ -92,6 +95,8 @@ class Params(C.Structure):
         ("sph_viscosity_l", C.c_double),
         ("sph_viscosity_delta", C.c_double),
         ("sph_sinc_index", C.c_double),
+        ("poly_gamma2", C.c_double),
+        ("ppt_density_thr", C.c_double),
         ("reserved", C.c_int32 * 8),
     ]
 
@@ -131,6 +136,8 @@ class Params(C.Structure):
         p.sph_viscosity_l = 0.05
         p.sph_viscosity_delta = 1.0
         p.sph_sinc_index = 4.0
+        p.poly_gamma2 = 2.5
+        p.ppt_density_thr = 5e14
         for k, v in kw.items():
             if not hasattr(p, k):
                 raise AttributeError(k)
@@ -161,7 +168,7 @@ class SoAView(C.Structure):
         ("gpot", _DP), ("m", _DP), ("h", _DP), ("rho", _DP), ("P", _DP),
         ("cs", _DP), ("u", _DP), ("e", _DP), ("dudt", _DP), ("dedt", _DP),
         ("K", _DP), ("alpha", _DP), ("vsig", _DP), ("dt", _DP),
-        ("divv", _DP), ("ddivvdt", _DP),
+        ("divv", _DP), ("ddivvdt", _DP), ("Ye", _DP),
         ("id", C.POINTER(C.c_int64)),
         ("key", C.POINTER(C.c_uint64)),
     ]
@@ -177,7 +184,7 @@ class Conserved(C.Structure):
 DOUBLE_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "vhx", "vhy", "vhz",
                  "ax", "ay", "az", "gax", "gay", "gaz", "gpot", "m", "h",
                  "rho", "P", "cs", "u", "e", "dudt", "dedt", "K", "alpha",
-                 "vsig", "dt", "divv", "ddivvdt"]
+                 "vsig", "dt", "divv", "ddivvdt", "Ye"]
 
 
 def new_state(n):

@@ -112,6 +112,8 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->visc_l = p->sph_viscosity_l;
   pp->visc_delta = p->sph_viscosity_delta;
   pp->cfl = p->timestep_cfl_factor;
+  pp->gamma2 = p->poly_gamma2;
+  pp->rho_thr = p->ppt_density_thr;
   pp->out_screen_dt = p->out_screen_dt;
   pp->out_scalar_dt = p->out_scalar_dt;
   pp->out_h5data_dt = p->out_h5data_dt;
@@ -149,8 +151,8 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "sph_sinc_index must exceed 1";
     return false;
   }
-  if(p->eos_type != FSPH_EOS_IDEAL && p->eos_type != FSPH_EOS_POLYTROPIC) {
-    *why = "eos_type not implemented";
+  if(p->eos_type < FSPH_EOS_IDEAL || p->eos_type > FSPH_EOS_NO_EOS) {
+    *why = "unknown eos_type";
     return false;
   }
   if(p->sph_viscosity != FSPH_VISC_CONSTANT && p->sph_viscosity != FSPH_VISC_CULLEN) {
@@ -228,6 +230,8 @@ void fsph_params_default(fsph_params * p) {
   p->sph_viscosity_l = 0.05;
   p->sph_viscosity_delta = 1.0;
   p->sph_sinc_index = 4.0;
+  p->poly_gamma2 = 2.5;
+  p->ppt_density_thr = 5e14;
 }
 
 int32_t fsph_abi_version(void) { return FSPH_ABI_VERSION; }
@@ -406,7 +410,7 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
     v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
     v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
-    v->vsig, v->dt, v->divv, v->ddivvdt};
+    v->vsig, v->dt, v->divv, v->ddivvdt, v->Ye};
   for(int k = 0; k < NF; ++k) {
     if(src[k])
       CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
@@ -438,7 +442,7 @@ fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
   const double * src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
     v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
     v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
-    v->vsig, v->dt, v->divv, v->ddivvdt};
+    v->vsig, v->dt, v->divv, v->ddivvdt, v->Ye};
   for(int k = 0; k < NF; ++k)
     if(src[k])
       CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
@@ -520,7 +524,7 @@ fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
   double * dst[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx, v->vhy,
     v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m, v->h,
     v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha, v->vsig,
-    v->dt, v->divv, v->ddivvdt};
+    v->dt, v->divv, v->ddivvdt, v->Ye};
   for(int k = 0; k < NF; ++k) {
     if(k == F_Z || k == F_VZ || k == F_VHZ || k == F_AZ || k == F_GAZ)
       if(c->p.dimension == 2)

@@ -44,8 +44,22 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
   double ** f = P.f;
   const double dt = tm->dt;
   switch(op) {
-    case OP_EOS_INIT:  // eos.h:67-92,157-159
-      f[F_K][i] = f[F_P][i] / pow(f[F_RHO][i], pp.gamma);
+    case OP_EOS_INIT:  // eos_t<>::init (eos.h:67-92, 157-159, 240-243, 345-364)
+      if(pp.eos == FSPH_EOS_WD)
+        f[F_U][i] = wd_internal_energy(f[F_RHO][i], f[F_YE][i]);
+      else if(pp.eos == FSPH_EOS_PPT) {
+        const double rho = f[F_RHO][i], P_ = f[F_P][i], thr = pp.rho_thr;
+        double K1 = 0.0;
+        if(rho < thr)
+          K1 = P_ / pow(rho, pp.gamma);
+        else {
+          double K2 = P_ / pow(rho, pp.gamma2);
+          K1 = K2 * pow(thr, pp.gamma2 - pp.gamma);
+        }
+        f[F_K][i] = K1;
+      }
+      else if(pp.eos != FSPH_EOS_NO_EOS)
+        f[F_K][i] = f[F_P][i] / pow(f[F_RHO][i], pp.gamma);
       break;
     case OP_SET_TOTAL_ENERGY: {  // default_physics.h:327-335
       double vv = 0;
@@ -97,7 +111,8 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
     case OP_RECOMPUTE_KICK_U: {  // default_physics.h:153-161 (+ kick_u)
       double uint = f[F_U][i];
       double P_, cs;
-      eos_p_cs(pp, f[F_RHO][i], uint + 0.5 * dt * f[F_DUDT][i], f[F_K][i], P_, cs);
+      eos_p_cs(pp, f[F_RHO][i], uint + 0.5 * dt * f[F_DUDT][i], f[F_K][i],
+        f[F_YE][i], f[F_P][i], f[F_CS][i], P_, cs);
       f[F_P][i] = P_;
       f[F_CS][i] = cs;
       if(op == OP_RECOMPUTE_KICK_U)
@@ -113,7 +128,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
         vda += f[F_VX + d][i] * f[F_AX + d][i];
       double P_, cs;
       eos_p_cs(pp, f[F_RHO][i], eint + 0.5 * dt * (f[F_DEDT][i] - vda),
-        f[F_K][i], P_, cs);
+        f[F_K][i], f[F_YE][i], f[F_P][i], f[F_CS][i], P_, cs);
       f[F_P][i] = P_;
       f[F_CS][i] = cs;
       if(op == OP_RECOMPUTE_KICK_E)

@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
     P.f[F_U][a] = u;
   }
   double Pa, cs;
-  eos_p_cs(pp, rho_a, u, P.f[F_K][a], Pa, cs);
+  eos_p_cs(pp, rho_a, u, P.f[F_K][a], P.f[F_YE][a], P.f[F_P][a], P.f[F_CS][a], Pa,
+    cs);
   P.f[F_P][a] = Pa;
   cs_new[a] = cs;
   if(pp.cullen) {

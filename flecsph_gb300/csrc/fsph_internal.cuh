@@ -14,7 +14,7 @@ namespace fsph {
 enum Field {
   F_X, F_Y, F_Z, F_VX, F_VY, F_VZ, F_VHX, F_VHY, F_VHZ, F_AX, F_AY, F_AZ,
   F_GAX, F_GAY, F_GAZ, F_GPOT, F_M, F_H, F_RHO, F_P, F_CS, F_U, F_E, F_DUDT,
-  F_DEDT, F_K, F_ALPHA, F_VSIG, F_DT, F_DIVV, F_DDIVVDT, NF
+  F_DEDT, F_K, F_ALPHA, F_VSIG, F_DT, F_DIVV, F_DDIVVDT, F_YE, NF
 };
 
 // physics:: time globals of the reference (default_physics.h:32-39), kept in
@@ -48,6 +48,7 @@ struct PhysParams {
   double gamma, eta, kw, alpha, beta, eps, cfl;
   double alpha_max, visc_l, visc_delta;  // visc_cullen parameters
   double sinc_index, sinc_sigma[3];       // sinc kernel power and norms
+  double gamma2, rho_thr;                 // eos_ppt upper segment
   double out_screen_dt, out_scalar_dt, out_h5data_dt;
   double G;
 };

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "fsph_internal.cuh"
+#include "fsph_sphmath.cuh"  // the FP64 EOS the density pass applies
 
 namespace fsph {
 
@@ -309,15 +310,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
     P.f[F_U][a] = u;
   }
   double Pa, cs;
-  const double g = pp.gamma;
-  if(pp.eos == FSPH_EOS_POLYTROPIC) {
-    Pa = P.f[F_K][a] * pow(rho, g);
-    cs = sqrt(P.f[F_K][a] * g * pow(rho, g - 1.));
-  }
-  else {
-    Pa = (g - 1.) * rho * u;
-    cs = sqrt(g * (g - 1.) * u);
-  }
+  eos_p_cs(pp, rho, u, P.f[F_K][a], P.f[F_YE][a], P.f[F_P][a], P.f[F_CS][a], Pa, cs);
   P.f[F_P][a] = Pa;
   cs_new[a] = cs;
   Kp.thermo[a] = make_float4((float)rho, (float)(Pa / (rho * rho)), (float)cs,

@@ -287,14 +287,63 @@ __device__ __forceinline__ double visc_pi_pp(const PhysParams & pp,
   return visc_pi(pp.alpha, pp.beta, rho_ab, c_ab, mu_ab);
 }
 
-// eos_t<ideal>/<polytropic> compute_pressure + compute_soundspeed
-// (eos/eos.h:102-119, 166-183)
+// eos_t<wd> (eos/eos.h:225-315): pressure function constants and the
+// pressure, sound speed and internal energy of cold degenerate matter
+#define FSPH_WD_A 6.00233181e22       // [dynes/cm^2]
+#define FSPH_WD_B 9.73932099e5        // [moles/cm^3]
+#define FSPH_C_LIGHT_CGS 2.99792458e10
+
+__device__ __forceinline__ double wd_pressure(double rho, double Ye) {
+  double x = cbrt(rho * Ye / FSPH_WD_B);
+  double x2 = x * x;
+  return FSPH_WD_A * (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x));
+}
+__device__ __forceinline__ double wd_soundspeed(double rho, double Ye) {
+  double x = cbrt(rho * Ye / FSPH_WD_B);
+  double x2 = x * x;
+  double numer = (1. + x2) * (6. * x2 - 3.) + 3. + x2 * (2. * x2 - 3.);
+  double denom = (1. + x2) * (6. * x2 + 1.) - 1. + x2 * (2. * x2 + 1.);
+  return sqrt(numer / (3. * denom)) * FSPH_C_LIGHT_CGS;
+}
+__device__ __forceinline__ double wd_internal_energy(double rho, double Ye) {
+  const double x = cbrt(rho * Ye / FSPH_WD_B), x2 = x * x, x3 = x * x * x;
+  return FSPH_WD_A / rho * (8. * x3 * (sqrt(x2 + 1.) - 1.) -
+                            (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x)));
+}
+
+// eos_t<>::compute_pressure + compute_soundspeed for every eos_type
+// (eos/eos.h:102-119 polytropic, 166-183 ideal, 262-289 wd, 362-392 ppt,
+// 425-431 no_eos).  P_old and cs_old are returned by eos_no_eos.
 __device__ __forceinline__ void eos_p_cs(const PhysParams & pp, double rho,
-  double u, double K, double & P, double & cs) {
+  double u, double K, double Ye, double P_old, double cs_old, double & P,
+  double & cs) {
   const double g = pp.gamma;
   if(pp.eos == FSPH_EOS_POLYTROPIC) {
     P = K * pow(rho, g);
     cs = sqrt(K * g * pow(rho, g - 1.));
+  }
+  else if(pp.eos == FSPH_EOS_WD) {
+    P = wd_pressure(rho, Ye);
+    cs = wd_soundspeed(rho, Ye);
+  }
+  else if(pp.eos == FSPH_EOS_PPT) {
+    const double g2 = pp.gamma2, thr = pp.rho_thr;
+    if(rho < thr)
+      P = K * pow(rho, g);
+    else {
+      double K2 = K * pow(thr, g - g2);
+      P = K2 * pow(rho, g2);
+    }
+    if(rho < thr)
+      cs = sqrt(K * g * pow(rho, g - 1.));
+    else {
+      double K2 = K * pow(thr, g - g2);
+      cs = sqrt(K2 * g2 * pow(rho, g2 - 1.));
+    }
+  }
+  else if(pp.eos == FSPH_EOS_NO_EOS) {
+    P = P_old;
+    cs = cs_old;
   }
   else {
     P = (g - 1.) * rho * u;

@@ -6,9 +6,10 @@
 //   hydro_driver <in.bin> <out.bin> <iterations> [key=value ...]
 //
 // in/out: raw particle snapshots, little endian:
-//   char magic[8] = "FSPHSOA1"; int64 n; int32 dim; int32 nfields(=31);
-//   31 double arrays of length n in fsph_soa_view order (x..ddivvdt);
+//   char magic[8] = "FSPHSOA1"; int64 n; int32 dim; int32 nfields(=32);
+//   32 double arrays of length n in fsph_soa_view order (x..Ye);
 //   int64 id[n]
+// Older files with 29 to 31 arrays are read with the missing ones zero.
 // Parameters not given as key=value keep their reference defaults.
 #include <cstdint>
 #include <cstdio>
@@ -21,7 +22,8 @@
 
 namespace {
 
-constexpr int NFIELDS = 31;
+constexpr int NFIELDS = 32;
+constexpr int NFIELDS_MIN = 29;
 
 struct Snapshot {
   int64_t n = 0;
@@ -37,7 +39,7 @@ struct Snapshot {
     double ** slots[NFIELDS] = {&v.x, &v.y, &v.z, &v.vx, &v.vy, &v.vz, &v.vhx,
       &v.vhy, &v.vhz, &v.ax, &v.ay, &v.az, &v.gax, &v.gay, &v.gaz, &v.gpot,
       &v.m, &v.h, &v.rho, &v.P, &v.cs, &v.u, &v.e, &v.dudt, &v.dedt, &v.K,
-      &v.alpha, &v.vsig, &v.dt, &v.divv, &v.ddivvdt};
+      &v.alpha, &v.vsig, &v.dt, &v.divv, &v.ddivvdt, &v.Ye};
     for(int k = 0; k < NFIELDS; ++k)
       *slots[k] = f[k].data();
     v.id = id.data();
@@ -54,10 +56,12 @@ bool read_snapshot(const char * path, Snapshot & s) {
   int32_t nf = 0;
   bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, "FSPHSOA1", 8) == 0 &&
             std::fread(&s.n, 8, 1, fp) == 1 && std::fread(&s.dim, 4, 1, fp) == 1 &&
-            std::fread(&nf, 4, 1, fp) == 1 && nf == NFIELDS && s.n > 1;
+            std::fread(&nf, 4, 1, fp) == 1 && nf >= NFIELDS_MIN && nf <= NFIELDS &&
+            s.n > 1;
   for(int k = 0; ok && k < NFIELDS; ++k) {
-    s.f[k].resize(s.n);
-    ok = std::fread(s.f[k].data(), 8, s.n, fp) == (size_t)s.n;
+    s.f[k].assign(s.n, 0.0);
+    if(k < nf)
+      ok = std::fread(s.f[k].data(), 8, s.n, fp) == (size_t)s.n;
   }
   if(ok) {
     s.id.resize(s.n);

@@ -1,7 +1,9 @@
 """Raw particle snapshots read and written by the C++ hydro driver.
 
-Layout (little endian): b"FSPHSOA1", int64 n, int32 dim, int32 nfields (31),
-then the 31 FP64 arrays of fsph_soa_view in header order, then int64 id[n].
+Layout (little endian): b"FSPHSOA1", int64 n, int32 dim, int32 nfields (32),
+then the 32 FP64 arrays of fsph_soa_view in header order, then int64 id[n].
+Files with fewer arrays (29 to 31, written before the divergence and
+electron-fraction fields existed) read with the missing arrays zero.
 The reference writes H5part files (mpisph/io.h:874-1088); HDF5 is not part
 of this build, so snapshots are raw SoA.
 """
@@ -33,7 +35,6 @@ def read(path):
         nf = int(np.frombuffer(f.read(4), np.int32)[0])
         if not 0 < nf <= len(DOUBLE_FIELDS):
             raise ValueError(f"snapshot holds {nf} fields")
-        # files written before the divergence fields existed hold the first 29
         out = {k: np.frombuffer(f.read(8 * n), np.float64).copy()
                for k in DOUBLE_FIELDS[:nf]}
         for k in DOUBLE_FIELDS[nf:]:

@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FSPH_ABI_VERSION 3
+#define FSPH_ABI_VERSION 4
 
 /* Status codes.  They replace the reference's assert()/mpi_assert() aborts
  * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
@@ -79,7 +79,14 @@ enum fsph_kernel {
   FSPH_KERNEL_SINC = 7
 };
 /* Same numbering as param::eos_type_keyword (include/params.h:139-145). */
-enum fsph_eos { FSPH_EOS_IDEAL = 0, FSPH_EOS_POLYTROPIC = 1 };
+/* param::eos_type_keyword (include/params.h:138-144) */
+enum fsph_eos {
+  FSPH_EOS_IDEAL = 0,
+  FSPH_EOS_POLYTROPIC = 1,
+  FSPH_EOS_WD = 2,      /* cold white-dwarf matter (CGS units) */
+  FSPH_EOS_PPT = 3,     /* piecewise polytrope */
+  FSPH_EOS_NO_EOS = 4   /* pressure and sound speed left as they are */
+};
 /* param::sph_viscosity_keyword (include/params.h:148-152). */
 enum fsph_viscosity { FSPH_VISC_CONSTANT = 0, FSPH_VISC_CULLEN = 1 };
 enum fsph_precision {
@@ -135,6 +142,8 @@ typedef struct fsph_params {
   double sph_viscosity_l;            /* [523] 0.05 */
   double sph_viscosity_delta;        /* [529] 1.0 */
   double sph_sinc_index;             /* [232] 4.0, sinc kernel power */
+  double poly_gamma2;                /* [483] 2.5, eos_ppt upper segment */
+  double ppt_density_thr;            /* [488] 5e14, eos_ppt threshold */
   int32_t reserved[8];
 } fsph_params;
 
@@ -166,6 +175,7 @@ typedef struct fsph_soa_view {
   double *dt;              /* (opt) per-particle timestep estimate */
   double *divv;            /* (opt) velocity divergence (visc_cullen) */
   double *ddivvdt;         /* (opt) its time derivative (visc_cullen) */
+  double *Ye;              /* (opt) electron fraction (eos_wd) */
   int64_t *id;             /* (in)  particle id (sort tie-break) */
   uint64_t *key;           /* (out) Morton key, download only */
 } fsph_soa_view;

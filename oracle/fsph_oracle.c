@@ -77,7 +77,7 @@ struct orc_ctx {
   int64_t nreal; /* real particles hold ids [0, nreal); WALL copies above */
   double *x[3], *v[3], *vh[3], *a[3], *ga[3];
   double *gpot, *m, *h, *rho, *P, *cs, *u, *e, *dudt, *dedt, *K, *alpha, *vsig,
-    *dtp, *divv, *ddivvdt;
+    *dtp, *divv, *ddivvdt, *Ye;
   int64_t * id;
   uint64_t * key;
   double * csnew;
@@ -411,17 +411,64 @@ static double visc_pi(const orc_ctx * c, int64_t a, int64_t b, double rho_ab,
 }
 
 /* ---------------------------------------------------------------- EOS -- */
-/* eos_t<ideal/polytropic> (eos/eos.h:57-209) */
+/* eos_t<wd> constants and functions (eos/eos.h:225-315) */
+#define WD_A 6.00233181e22
+#define WD_B 9.73932099e5
+#define C_LIGHT_CGS 2.99792458e10
+static double wd_x(double rho, double Ye) { return cbrt(rho * Ye / WD_B); }
+static double wd_pressure(double rho, double Ye) {
+  double x = wd_x(rho, Ye), x2 = x * x;
+  return WD_A * (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x));
+}
+static double wd_soundspeed(double rho, double Ye) {
+  double x = wd_x(rho, Ye), x2 = x * x;
+  double numer = (1. + x2) * (6. * x2 - 3.) + 3. + x2 * (2. * x2 - 3.);
+  double denom = (1. + x2) * (6. * x2 + 1.) - 1. + x2 * (2. * x2 + 1.);
+  return sqrt(numer / (3. * denom)) * C_LIGHT_CGS;
+}
+static double wd_internal_energy(double rho, double Ye) {
+  const double x = wd_x(rho, Ye), x2 = x * x, x3 = x * x * x;
+  return WD_A / rho * (8. * x3 * (sqrt(x2 + 1.) - 1.) -
+                       (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x)));
+}
+
+/* eos_t<>::compute_pressure + compute_soundspeed (eos/eos.h:57-431):
+ * ideal, polytropic, wd, ppt; no_eos leaves both as they are. */
 static void eos_pressure(orc_ctx * c, int64_t i, double uval, double * P,
   double * cs) {
   const double g = c->p.poly_gamma;
-  if(c->p.eos_type == FSPH_EOS_POLYTROPIC) {
-    *P = c->K[i] * pow(c->rho[i], g);
-    *cs = sqrt(c->K[i] * g * pow(c->rho[i], g - 1.));
-  }
-  else {
-    *P = (g - 1.) * c->rho[i] * uval;
-    *cs = sqrt(g * (g - 1.) * uval);
+  const double rho = c->rho[i];
+  switch(c->p.eos_type) {
+    case FSPH_EOS_POLYTROPIC:
+      *P = c->K[i] * pow(rho, g);
+      *cs = sqrt(c->K[i] * g * pow(rho, g - 1.));
+      return;
+    case FSPH_EOS_WD:
+      *P = wd_pressure(rho, c->Ye[i]);
+      *cs = wd_soundspeed(rho, c->Ye[i]);
+      return;
+    case FSPH_EOS_PPT: {
+      const double g2 = c->p.poly_gamma2, thr = c->p.ppt_density_thr;
+      const double K1 = c->K[i];
+      if(rho < thr)
+        *P = K1 * pow(rho, g);
+      else
+        *P = K1 * pow(thr, g - g2) * pow(rho, g2);
+      if(rho < thr)
+        *cs = sqrt(K1 * g * pow(rho, g - 1.));
+      else {
+        double K2 = K1 * pow(thr, g - g2);
+        *cs = sqrt(K2 * g2 * pow(rho, g2 - 1.));
+      }
+      return;
+    }
+    case FSPH_EOS_NO_EOS:
+      *P = c->P[i];
+      *cs = c->cs[i];
+      return;
+    default:
+      *P = (g - 1.) * rho * uval;
+      *cs = sqrt(g * (g - 1.) * uval);
   }
 }
 
@@ -463,7 +510,7 @@ static void free_state(orc_ctx * c) {
   free(c->gpot); free(c->m); free(c->h); free(c->rho); free(c->P); free(c->cs);
   free(c->u); free(c->e); free(c->dudt); free(c->dedt); free(c->K);
   free(c->alpha); free(c->vsig); free(c->dtp); free(c->id); free(c->key);
-  free(c->divv); free(c->ddivvdt);
+  free(c->divv); free(c->ddivvdt); free(c->Ye);
   free(c->csnew);
 }
 
@@ -531,7 +578,7 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
   c->u = xalloc(8 * n); c->e = xalloc(8 * n); c->dudt = xalloc(8 * n);
   c->dedt = xalloc(8 * n); c->K = xalloc(8 * n); c->alpha = xalloc(8 * n);
   c->vsig = xalloc(8 * n); c->dtp = xalloc(8 * n); c->id = xalloc(8 * n);
-  c->divv = xalloc(8 * n); c->ddivvdt = xalloc(8 * n);
+  c->divv = xalloc(8 * n); c->ddivvdt = xalloc(8 * n); c->Ye = xalloc(8 * n);
   c->key = xalloc(8 * n); c->csnew = xalloc(8 * n);
   double * const xs[3] = {v->x, v->y, v->z};
   double * const vs[3] = {v->vx, v->vy, v->vz};
@@ -547,7 +594,7 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
   CPY_IN(c->u, v->u); CPY_IN(c->e, v->e); CPY_IN(c->dudt, v->dudt);
   CPY_IN(c->dedt, v->dedt); CPY_IN(c->K, v->K); CPY_IN(c->alpha, v->alpha);
   CPY_IN(c->vsig, v->vsig); CPY_IN(c->dtp, v->dt);
-  CPY_IN(c->divv, v->divv); CPY_IN(c->ddivvdt, v->ddivvdt);
+  CPY_IN(c->divv, v->divv); CPY_IN(c->ddivvdt, v->ddivvdt); CPY_IN(c->Ye, v->Ye);
   memcpy(c->id, v->id, 8 * n);
   c->nreal = n;
   if(is_periodic(c)) {
@@ -595,7 +642,7 @@ int orc_download(orc_ctx * c, fsph_soa_view * v) {
   CPY_OUT(v->u, c->u); CPY_OUT(v->e, c->e); CPY_OUT(v->dudt, c->dudt);
   CPY_OUT(v->dedt, c->dedt); CPY_OUT(v->K, c->K); CPY_OUT(v->alpha, c->alpha);
   CPY_OUT(v->vsig, c->vsig); CPY_OUT(v->dt, c->dtp);
-  CPY_OUT(v->divv, c->divv); CPY_OUT(v->ddivvdt, c->ddivvdt);
+  CPY_OUT(v->divv, c->divv); CPY_OUT(v->ddivvdt, c->ddivvdt); CPY_OUT(v->Ye, c->Ye);
   if(v->id) memcpy(v->id, c->id, 8 * n);
   if(v->key) memcpy(v->key, c->key, 8 * n);
   return FSPH_OK;
@@ -791,7 +838,7 @@ static void collect_groups(orc_ctx * c, int64_t node) {
 }
 
 /* Every per-particle array, for moves of whole particles. */
-#define ORC_NFIELDS 29
+#define ORC_NFIELDS 30
 static void field_list(orc_ctx * c, double *** out) {
   int k = 0;
   for(int d = 0; d < 3; ++d) {
@@ -802,7 +849,7 @@ static void field_list(orc_ctx * c, double *** out) {
   out[k++] = &c->P; out[k++] = &c->cs; out[k++] = &c->u; out[k++] = &c->e;
   out[k++] = &c->dudt; out[k++] = &c->dedt; out[k++] = &c->K;
   out[k++] = &c->alpha;
-  out[k++] = &c->divv; out[k++] = &c->ddivvdt;
+  out[k++] = &c->divv; out[k++] = &c->ddivvdt; out[k++] = &c->Ye;
 }
 
 static void ensure_cap(orc_ctx * c, int64_t need) {
@@ -999,7 +1046,7 @@ int orc_update_iteration(orc_ctx * c) {
   }
   double ** fs[] = {&c->gpot, &c->m, &c->h, &c->rho, &c->P, &c->cs, &c->u,
     &c->e, &c->dudt, &c->dedt, &c->K, &c->alpha, &c->vsig, &c->dtp, &c->divv,
-    &c->ddivvdt};
+    &c->ddivvdt, &c->Ye};
   for(size_t k = 0; k < sizeof(fs) / sizeof(fs[0]); ++k)
     permute_d(fs[k], rec, n, tmp);
   for(int64_t i = 0; i < n; ++i) {
@@ -1566,9 +1613,23 @@ int orc_dedt(orc_ctx * c) { return run_pass(c, PASS_DEDT); }
 
 /* ------------------------------------------------------- apply_all -- */
 int orc_eos_init(orc_ctx * c) {
-  /* eos_t<>::init -> compute_adiabatic (eos.h:67-92,157-159) */
-  for(int64_t i = 0; i < c->n; ++i)
-    c->K[i] = c->P[i] / pow(c->rho[i], c->p.poly_gamma);
+  /* eos_t<>::init (eos.h:67-92, 157-159, 240-243, 345-364) */
+  const double g = c->p.poly_gamma, g2 = c->p.poly_gamma2;
+  const double thr = c->p.ppt_density_thr;
+  for(int64_t i = 0; i < c->n; ++i) {
+    if(c->p.eos_type == FSPH_EOS_WD)
+      c->u[i] = wd_internal_energy(c->rho[i], c->Ye[i]);
+    else if(c->p.eos_type == FSPH_EOS_PPT) {
+      if(c->rho[i] < thr)
+        c->K[i] = c->P[i] / pow(c->rho[i], g);
+      else {
+        double K2 = c->P[i] / pow(c->rho[i], g2);
+        c->K[i] = K2 * pow(thr, g2 - g);
+      }
+    }
+    else if(c->p.eos_type != FSPH_EOS_NO_EOS)
+      c->K[i] = c->P[i] / pow(c->rho[i], g);
+  }
   return FSPH_OK;
 }
 

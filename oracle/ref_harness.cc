@@ -38,6 +38,8 @@ struct orc_ctx {
 static void set_params(const fsph_params * p) {
   using namespace param;
   _poly_gamma = p->poly_gamma;
+  _poly_gamma2 = p->poly_gamma2;
+  _ppt_density_thr = p->ppt_density_thr;
   _sph_eta = p->sph_eta;
   _sph_kernel = (sph_kernel_keyword)p->sph_kernel;
   _eos_type = (eos_type_keyword)p->eos_type;
@@ -164,7 +166,7 @@ int orc_upload(orc_ctx * c, const fsph_soa_view * v) {
     b.setDdivvdt(get(v->ddivvdt, i));
     b.setEntropy(0.0);
     b.setTemperature(0.0);
-    b.setElectronfraction(0.0);
+    b.setElectronfraction(get(v->Ye, i));
     b.setDadt(0.0);
     b.set_id(v->id[i]);
     b.setType(NORMAL);
@@ -207,6 +209,7 @@ int orc_download(orc_ctx * c, fsph_soa_view * v) {
     if(v->dt) v->dt[i] = b.getDt();
     if(v->divv) v->divv[i] = b.getDivergenceV();
     if(v->ddivvdt) v->ddivvdt[i] = b.getDdivvdt();
+    if(v->Ye) v->Ye[i] = b.getElectronfraction();
     if(v->id) v->id[i] = (int64_t)b.id();
     if(v->key) v->key[i] = b.key().value();
   }

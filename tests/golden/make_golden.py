@@ -24,8 +24,9 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from flecsph_gb300 import setups  # noqa: E402
-from flecsph_gb300.abi import (DOUBLE_FIELDS, KERNEL_QUINTIC_SPLINE,  # noqa: E402
-                               KERNEL_SUPER_GAUSSIAN, KERNEL_WENDLAND_C4, VISC_CULLEN)
+from flecsph_gb300.abi import (DOUBLE_FIELDS, EOS_NO_EOS, EOS_PPT, EOS_WD,  # noqa: E402
+                               KERNEL_QUINTIC_SPLINE, KERNEL_SUPER_GAUSSIAN,
+                               KERNEL_WENDLAND_C4, VISC_CULLEN)
 import pyoracle  # noqa: E402
 
 
@@ -61,6 +62,9 @@ def cases():
     p.sph_kernel = KERNEL_QUINTIC_SPLINE
     p.sph_variable_h = 1
     yield "sod3d_quintic_varh_4000", setups.shuffled(s, 11), p, 2
+    # the other equations of state
+    for name, seed, s, p in eos_cases():
+        yield name, setups.shuffled(s, seed), p, 2
     # periodic boundaries: copies regenerated at every update_iteration;
     # a few particles start outside the box and are teleported back
     s, p, m = setups.kh2d(40)
@@ -68,6 +72,27 @@ def cases():
     s, p, m = setups.kh3d(12)
     p.periodic_boundary_y = p.periodic_boundary_z = 0
     yield "kh3d_periodic_x_1728", setups.shuffled(_outside(s), 8), p, 2
+
+
+def eos_cases():
+    """Sod tubes under the piecewise polytrope (threshold between the two
+    states), the white-dwarf EOS (densities 1e7 and 1.25e6 g/cc, Ye = 0.5)
+    and no EOS (pressure and sound speed frozen at their inputs)."""
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.eos_type = EOS_PPT
+    p.poly_gamma2 = 2.5
+    p.ppt_density_thr = 0.5
+    yield "sod3d_ppt_4000", 12, s, p
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.eos_type = EOS_WD
+    s["m"] *= 1.0e7
+    s["rho"] *= 1.0e7
+    s["Ye"][:] = 0.5
+    yield "sod3d_wd_4000", 13, s, p
+    s, p, m = setups.sod2d(100, 10)
+    p.eos_type = EOS_NO_EOS
+    s["cs"][:] = np.sqrt(p.poly_gamma * s["P"] / s["rho"])
+    yield "sod2d_noeos_1000", 14, s, p
 
 
 def _outside(s):

@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_abi_version(lib):
     lib.fsph_abi_version.restype = C.c_int32
-    assert lib.fsph_abi_version() == 3
+    assert lib.fsph_abi_version() == 4
 
 
 def test_params_defaults_match_header(lib):
@@ -43,8 +43,8 @@ def test_params_defaults_match_header(lib):
 
 
 def test_struct_sizes():
-    # fsph_soa_view: n + 31 double pointers + id + key
-    assert C.sizeof(abi.SoAView) == 8 * 34
+    # fsph_soa_view: n + 32 double pointers + id + key
+    assert C.sizeof(abi.SoAView) == 8 * 35
     assert C.sizeof(abi.Conserved) == 8 * 8
 
 
