@@ -24,6 +24,7 @@ SOURCES = {
     "fsph_fp64.cu": ["-fmad=false"],
     "fsph_elementwise.cu": ["-fmad=false"],
     "fsph_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "fsph_mixed_cullen.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "fsph_gravity.cu": [],
     "fsph_periodic.cu": ["-fmad=false"],
     "fsph_peak.cu": [],

@@ -159,10 +159,6 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "sph_viscosity must be visc_constant or visc_cullen";
     return false;
   }
-  if(p->sph_viscosity == FSPH_VISC_CULLEN && p->precision_mode != FSPH_PRECISION_FP64) {
-    *why = "visc_cullen runs in the FP64 mode";
-    return false;
-  }
   if(p->relaxation_steps != 0) {
     *why = "relaxation_steps must be 0";
     return false;
@@ -329,6 +325,8 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.vhm, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.vel, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.thermo, N) == cudaSuccess;
+  if(c->pp.cullen)
+    ok &= dalloc(c, &c->K.visc, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
   c->periodic = p->periodic_boundary_x || p->periodic_boundary_y ||
                 p->periodic_boundary_z;
@@ -680,7 +678,10 @@ fsph_status fsph_compute_alpha(fsph_ctx * c) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_DENSITY);
-  CK(launch_alpha_cullen(L, c->P, c->pp, c->Ls, c->d_time));
+  if(c->mixed)
+    CK(launch_alpha_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time));
+  else
+    CK(launch_alpha_cullen(L, c->P, c->pp, c->Ls, c->d_time));
   return FSPH_OK;
 }
 
@@ -694,7 +695,8 @@ static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(c->mixed) {
     {
       Phase ph(c, FSPH_TIMER_DENSITY);
-      CK(launch_density_mixed(L, c->P, c->pp, c->Ls, c->K, c->cs_new, c->d_status));
+      CK(launch_density_mixed(L, c->P, c->pp, c->Ls, c->K, c->cs_new, c->d_status,
+        c->d_time));
     }
     if(with_vsig) {
       Phase ph(c, FSPH_TIMER_VSIG);

@@ -95,6 +95,8 @@ struct Packed {
   float4 * vhm;     // {vh_x, vh_y, vh_z, m}
   float4 * vel;     // {v_x, v_y, v_z, 0}
   float4 * thermo;  // {rho, P/rho^2, c_s (new), c_s (previous)}
+  float2 * visc;    // Cullen & Dehnen: {c_s, sign(div v)} in the alpha pass,
+                    // {alpha, 0} in the pair passes
   float * qscale;   // device [3]: range extent / 2^31 per axis
 };
 
@@ -171,7 +173,9 @@ cudaError_t launch_pack_positions(const Launch & L, const Particles & P,
   const PhysParams & pp, const unsigned long long * rbits, const Packed & K);
 cudaError_t launch_density_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
-  DevStatus * st);
+  DevStatus * st, const DevTime * tm);
+cudaError_t launch_alpha_mixed(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 cudaError_t launch_vsig_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
 cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
