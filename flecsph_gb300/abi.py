@@ -35,6 +35,21 @@ EOS_PPT = 3
 EOS_NO_EOS = 4
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+# enum fsph_eforce: the terms of external_force::select
+EFORCE_NONE = 0
+EFORCE_WALLS_X = 1
+EFORCE_WALLS_Y = 2
+EFORCE_WALLS_Z = 3
+EFORCE_SPHERICAL_WALL = 4
+EFORCE_SPHERICAL_DENSITY_SUPPORT = 5
+EFORCE_GRAVITY = 6
+EFORCE_AIRFOIL = 7
+EFORCE_ORBIT = 8
+EFORCE_POISON = 9
+MAX_EFORCE = 8
+DENSITY_CONSTANT = 0
+DENSITY_PARABOLIC = 1
+DENSITY_MESA = 2
 
 TIMER_NAMES = ["range_keys", "sort", "tree", "neighbors", "density", "vsig",
                "accel", "energy", "integrate", "dt", "gravity", "periodic"]
@@ -97,6 +112,30 @@ class Params(C.Structure):
         ("sph_sinc_index", C.c_double),
         ("poly_gamma2", C.c_double),
         ("ppt_density_thr", C.c_double),
+        ("external_force", C.c_int32 * MAX_EFORCE),
+        ("density_profile", C.c_int32),
+        ("reserved_pad2", C.c_int32),
+        ("extforce_wall_powerindex", C.c_double),
+        ("extforce_wall_steepness", C.c_double),
+        ("sphere_radius", C.c_double),
+        ("gravity_acceleration_constant", C.c_double),
+        ("orbital_separation", C.c_double),
+        ("mass_neutron_star", C.c_double),
+        ("mass_white_dwarf", C.c_double),
+        ("zero_potential_poison_value", C.c_double),
+        ("airfoil_size", C.c_double),
+        ("airfoil_thickness", C.c_double),
+        ("airfoil_camber", C.c_double),
+        ("airfoil_anchor_x", C.c_double),
+        ("airfoil_anchor_y", C.c_double),
+        ("airfoil_attack_angle", C.c_double),
+        ("rho_initial", C.c_double),
+        ("pressure_initial", C.c_double),
+        ("mesa_rim_width", C.c_double),
+        ("relaxation_beta", C.c_double),
+        ("relaxation_gamma", C.c_double),
+        ("relaxation_repulsion_radius", C.c_double),
+        ("relaxation_repulsion_gamma", C.c_double),
         ("reserved", C.c_int32 * 8),
     ]
 
@@ -138,18 +177,60 @@ class Params(C.Structure):
         p.sph_sinc_index = 4.0
         p.poly_gamma2 = 2.5
         p.ppt_density_thr = 5e14
+        p.density_profile = DENSITY_CONSTANT
+        p.extforce_wall_powerindex = 5.0
+        p.extforce_wall_steepness = 1e12
+        p.sphere_radius = 1.0
+        p.gravity_acceleration_constant = 9.81
+        p.orbital_separation = 2.5e9
+        p.mass_neutron_star = 1.26 * 1.988435e33
+        p.mass_white_dwarf = 1.10 * 1.988435e33
+        p.zero_potential_poison_value = 0.0
+        p.airfoil_size = 2.0
+        p.airfoil_thickness = 0.05
+        p.airfoil_camber = 0.1
+        p.airfoil_anchor_x = -1.0
+        p.airfoil_anchor_y = 0.0
+        p.airfoil_attack_angle = 0.0
+        p.rho_initial = 1.0
+        p.pressure_initial = 1.0
+        p.mesa_rim_width = 0.25
+        p.relaxation_beta = 1e-6
+        p.relaxation_gamma = 0.0
+        p.relaxation_repulsion_radius = 0.25
+        p.relaxation_repulsion_gamma = 0.0
         for k, v in kw.items():
             if not hasattr(p, k):
                 raise AttributeError(k)
-            setattr(p, k, v)
+            if k == "external_force":
+                p.set_forces(v)
+            else:
+                setattr(p, k, v)
         return p
+
+    def set_forces(self, codes):
+        """Set the ordered external-force list (fsph_eforce codes)."""
+        codes = list(codes)
+        if len(codes) > MAX_EFORCE:
+            raise ValueError("at most %d external-force terms" % MAX_EFORCE)
+        self.external_force = (C.c_int32 * MAX_EFORCE)(*(codes + [0] * (MAX_EFORCE - len(codes))))
+
+    def forces(self):
+        """The external-force codes in order, without the terminating zeros."""
+        out = []
+        for c in self.external_force:
+            if c == EFORCE_NONE:
+                break
+            out.append(int(c))
+        return out
 
     def as_dict(self):
         out = {}
         for name, _ in self._fields_:
-            if name in ("reserved", "reserved_pad"):
+            if name in ("reserved", "reserved_pad", "reserved_pad2"):
                 continue
-            out[name] = getattr(self, name)
+            v = getattr(self, name)
+            out[name] = list(v) if name == "external_force" else v
         return out
 
 

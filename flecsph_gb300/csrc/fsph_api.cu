@@ -2,6 +2,7 @@
 // body_system / physics call surface, sequenced on one CUDA stream.
 #include <cuda_runtime.h>
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -10,6 +11,7 @@
 
 #include "fsph_ctx.cuh"
 #include "fsph_internal.cuh"
+#include "fsph_eforce.cuh"
 
 using namespace fsph;
 
@@ -118,6 +120,45 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->out_scalar_dt = p->out_scalar_dt;
   pp->out_h5data_dt = p->out_h5data_dt;
   pp->G = p->gravitational_constant;
+  // external forces (eforce.h) and the constants their functions cache
+  pp->n_eforce = 0;
+  pp->has_eacc = 0;
+  for(int k = 0; k < FSPH_MAX_EFORCE && p->external_force[k] != FSPH_EFORCE_NONE; ++k) {
+    pp->eforce[pp->n_eforce++] = p->external_force[k];
+    if(p->external_force[k] != FSPH_EFORCE_POISON)
+      pp->has_eacc = 1;
+  }
+  for(int k = pp->n_eforce; k < 8; ++k)
+    pp->eforce[k] = FSPH_EFORCE_NONE;
+  pp->ew_n = p->extforce_wall_powerindex;
+  pp->ew_a = p->extforce_wall_steepness;
+  pp->box_half[0] = .5 * p->box_length;
+  pp->box_half[1] = .5 * p->box_width;
+  pp->box_half[2] = .5 * p->box_height;
+  pp->sphere_r = p->sphere_radius;
+  pp->grav_acc = p->gravity_acceleration_constant;
+  pp->poison = p->zero_potential_poison_value;
+  pp->orb_a = p->orbital_separation;
+  pp->orb_mns = p->mass_neutron_star;
+  pp->orb_mwd = p->mass_white_dwarf;
+  pp->af_size = p->airfoil_size;
+  pp->af_thick = p->airfoil_thickness;
+  pp->af_camber = p->airfoil_camber;
+  pp->af_x = p->airfoil_anchor_x;
+  pp->af_y = p->airfoil_anchor_y;
+  pp->af_alpha = p->airfoil_attack_angle * FSPH_PI / 180.0;
+  pp->dprof = p->density_profile;
+  pp->mesa_q = p->mesa_rim_width;
+  pp->mesa_rho0 = mesa_rho0_for(p->dimension, p->mesa_rim_width);
+  pp->rho_init = p->rho_initial;
+  pp->ds_K0 = p->pressure_initial / pow(p->rho_initial, p->poly_gamma);
+  pp->ds_rho0 = dprof_rho(p->dimension, p->density_profile, 0., pp->mesa_q,
+    pp->mesa_rho0);
+  pp->relax_beta = p->relaxation_beta;
+  pp->relax_gamma = p->relaxation_gamma;
+  pp->rep_radius = p->relaxation_repulsion_radius;
+  pp->rep_gamma = p->relaxation_repulsion_gamma;
+  pp->relax_steps = p->relaxation_steps;
 }
 
 // analysis::set_initial_time_iteration (analysis.h:221-249)
@@ -159,9 +200,29 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "sph_viscosity must be visc_constant or visc_cullen";
     return false;
   }
-  if(p->relaxation_steps != 0) {
-    *why = "relaxation_steps must be 0";
+  if(p->relaxation_steps < 0) {
+    *why = "relaxation_steps must be >= 0";
     return false;
+  }
+  for(int k = 0; k < FSPH_MAX_EFORCE && p->external_force[k] != FSPH_EFORCE_NONE; ++k) {
+    const int32_t e = p->external_force[k];
+    if(e < FSPH_EFORCE_WALLS_X || e > FSPH_EFORCE_POISON) {
+      *why = "unknown external_force code";
+      return false;
+    }
+    if(e == FSPH_EFORCE_WALLS_Z && p->dimension < 3) {
+      *why = "walls:z needs three dimensions";
+      return false;
+    }
+    if(e == FSPH_EFORCE_ORBIT && p->dimension != 3) {
+      *why = "the orbit force is three-dimensional (eforce.h:279-298)";
+      return false;
+    }
+    if(e == FSPH_EFORCE_SPHERICAL_DENSITY_SUPPORT &&
+       (p->density_profile < FSPH_DENSITY_CONSTANT || p->density_profile > FSPH_DENSITY_MESA)) {
+      *why = "density_profile must be constant, parabolic or mesa";
+      return false;
+    }
   }
   {
     const int per[3] = {p->periodic_boundary_x, p->periodic_boundary_y,
@@ -228,6 +289,100 @@ void fsph_params_default(fsph_params * p) {
   p->sph_sinc_index = 4.0;
   p->poly_gamma2 = 2.5;
   p->ppt_density_thr = 5e14;
+  p->density_profile = FSPH_DENSITY_CONSTANT;
+  p->extforce_wall_powerindex = 5.0;
+  p->extforce_wall_steepness = 1e12;
+  p->sphere_radius = 1.0;
+  p->gravity_acceleration_constant = 9.81;
+  p->orbital_separation = 2.5e9;
+  p->mass_neutron_star = 1.26 * 1.988435e33;
+  p->mass_white_dwarf = 1.10 * 1.988435e33;
+  p->zero_potential_poison_value = 0.0;
+  p->airfoil_size = 2.0;
+  p->airfoil_thickness = 0.05;
+  p->airfoil_camber = 0.1;
+  p->airfoil_anchor_x = -1.0;
+  p->airfoil_anchor_y = 0.0;
+  p->airfoil_attack_angle = 0.0;
+  p->rho_initial = 1.0;
+  p->pressure_initial = 1.0;
+  p->mesa_rim_width = 0.25;
+  p->relaxation_beta = 1.e-6;
+  p->relaxation_gamma = 0.0;
+  p->relaxation_repulsion_radius = 0.25;
+  p->relaxation_repulsion_gamma = 0.0;
+}
+
+// external_force::select (eforce.h:359-434): split at commas, match each
+// term case-insensitively, "walls:" followed by up to three axis letters.
+static bool ieq(const char * a, size_t na, const char * b) {
+  if(strlen(b) != na)
+    return false;
+  for(size_t i = 0; i < na; ++i)
+    if(tolower((unsigned char)a[i]) != tolower((unsigned char)b[i]))
+      return false;
+  return true;
+}
+
+fsph_status fsph_params_set_external_force(fsph_params * p, const char * spec) {
+  if(!p || !spec)
+    return FSPH_ERR_ARG;
+  int32_t codes[FSPH_MAX_EFORCE];
+  int n = 0;
+  const size_t len = strlen(spec);
+  auto push = [&](int32_t code) {
+    if(n >= FSPH_MAX_EFORCE)
+      return false;
+    codes[n++] = code;
+    return true;
+  };
+  if(!(ieq(spec, len, "zero") || ieq(spec, len, "none"))) {
+    size_t start = 0;
+    while(true) {
+      size_t end = start;
+      while(end < len && spec[end] != ',')
+        ++end;
+      const char * t = spec + start;
+      const size_t tl = end - start;
+      bool ok = true;
+      if(ieq(t, tl, "spherical wall"))
+        ok = push(FSPH_EFORCE_SPHERICAL_WALL);
+      else if(ieq(t, tl, "airfoil"))
+        ok = push(FSPH_EFORCE_AIRFOIL);
+      else if(ieq(t, tl, "spherical density support"))
+        ok = push(FSPH_EFORCE_SPHERICAL_DENSITY_SUPPORT);
+      else if(ieq(t, tl, "gravity"))
+        ok = push(FSPH_EFORCE_GRAVITY);
+      else if(ieq(t, tl, "orbit"))
+        ok = push(FSPH_EFORCE_ORBIT);
+      else if(tl >= 6 && ieq(t, 6, "walls:")) {
+        const size_t imx = tl - 6 < 3 ? tl - 6 : 3;
+        for(size_t i = 0; ok && i < imx; ++i) {
+          const char c = (char)tolower((unsigned char)t[6 + i]);
+          if(c == 'x')
+            ok = push(FSPH_EFORCE_WALLS_X);
+          else if(c == 'y')
+            ok = push(FSPH_EFORCE_WALLS_Y);
+          else if(c == 'z')
+            ok = push(FSPH_EFORCE_WALLS_Z);
+          else
+            ok = false;
+        }
+      }
+      else if(ieq(t, tl, "poison"))
+        ok = push(FSPH_EFORCE_POISON);
+      else
+        ok = false;
+      if(!ok)
+        return FSPH_ERR_ARG;
+      if(end >= len)
+        break;
+      start = end + 1;
+    }
+  }
+  for(int k = 0; k < FSPH_MAX_EFORCE; ++k)
+    p->external_force[k] = k < n ? codes[k] : FSPH_EFORCE_NONE;
+  return FSPH_OK;
 }
 
 int32_t fsph_abi_version(void) { return FSPH_ABI_VERSION; }
@@ -748,7 +903,7 @@ fsph_status fsph_dudt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
-    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K));
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time));
   else
     CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
   return FSPH_OK;
@@ -766,6 +921,30 @@ fsph_status fsph_dedt(fsph_ctx * c) {
     CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K));
   else
     CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
+  return FSPH_OK;
+}
+
+fsph_status fsph_add_drag_acceleration(fsph_ctx * c) {
+  return elem(c, OP_DRAG_ACC, FSPH_TIMER_ACCEL);
+}
+
+fsph_status fsph_add_drag_dedt(fsph_ctx * c) {
+  return elem(c, OP_DRAG_DEDT, FSPH_TIMER_ENERGY);
+}
+
+fsph_status fsph_add_drag_dudt(fsph_ctx * c) {
+  return elem(c, OP_DRAG_DUDT, FSPH_TIMER_ENERGY);
+}
+
+fsph_status fsph_add_short_range_repulsion(fsph_ctx * c) {
+  if(!c || !c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_ACCEL);
+  CK(launch_repulsion(L, c->P, c->pp, c->Ls));
   return FSPH_OK;
 }
 
@@ -894,6 +1073,9 @@ fsph_status fsph_step(fsph_ctx * c) {
   const bool evolve = p.evolve_internal_energy;
   const bool grav = p.enable_fmm;
   const bool cullen = c->pp.cullen;
+  // particle relaxation terms (hydro/main_driver.cc:129-134,150-165,
+  // 204-207,219-234); the newtonian driver has none
+  const bool relax = !grav && c->iteration < p.relaxation_steps;
   if(c->iteration == p.initial_iteration) {
     TRY(fsph_update_iteration(c));
     TRY(fsph_eos_init(c));
@@ -907,6 +1089,10 @@ fsph_status fsph_step(fsph_ctx * c) {
     if(cullen)
       TRY(fsph_compute_alpha(c));
     TRY(accel_impl(c, 0, c->mixed));
+    if(relax) {
+      TRY(fsph_add_drag_acceleration(c));
+      TRY(fsph_add_short_range_repulsion(c));
+    }
     if(grav) {
       // newtonian/main_driver.cc:137-151: gravity, then total energy again
       TRY(fsph_gravitation(c));
@@ -921,10 +1107,14 @@ fsph_status fsph_step(fsph_ctx * c) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         if(thermo) {
           TRY(fsph_dedt(c));
+          if(relax)
+            TRY(fsph_add_drag_dedt(c));
           TRY(elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE));
         }
         else {
           TRY(fsph_dudt(c));
+          if(relax)
+            TRY(fsph_add_drag_dudt(c));
           TRY(elem(c, OP_RECOMPUTE, FSPH_TIMER_INTEGRATE));
         }
       }
@@ -944,6 +1134,12 @@ fsph_status fsph_step(fsph_ctx * c) {
       TRY(fsph_gravitation(c));
       TRY(fsph_leapfrog_kick_v(c));
     }
+    else if(relax) {
+      TRY(accel_impl(c, 0, c->mixed));
+      TRY(fsph_add_drag_acceleration(c));
+      TRY(fsph_add_short_range_repulsion(c));
+      TRY(fsph_leapfrog_kick_v(c));
+    }
     else
       TRY(accel_impl(c, 1, c->mixed));
     if(evolve) {
@@ -951,11 +1147,15 @@ fsph_status fsph_step(fsph_ctx * c) {
         const bool lastp = m == p.pressure_updates_number;
         if(thermo) {
           TRY(fsph_dedt(c));
+          if(relax)
+            TRY(fsph_add_drag_dedt(c));
           TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_E : OP_RECOMPUTE_THERMO,
             FSPH_TIMER_INTEGRATE));
         }
         else {
           TRY(fsph_dudt(c));
+          if(relax)
+            TRY(fsph_add_drag_dudt(c));
           TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_U : OP_RECOMPUTE,
             FSPH_TIMER_INTEGRATE));
         }

@@ -23,13 +23,14 @@ __device__ __forceinline__ double dmin_(double a, double b) { return b < a ? b :
 
 // recover_internal_energy (default_physics.h:126-145)
 template<int D>
-__device__ __forceinline__ double recover_u(const Particles & P, int i,
-  DevStatus * st) {
+__device__ __forceinline__ double recover_u(const Particles & P,
+  const PhysParams & pp, int i, DevStatus * st) {
   double vv = 0;
   for(int d = 0; d < D; ++d)
     vv += P.f[F_VX + d][i] * P.f[F_VX + d][i];
   double ekin = .5 * vv;
-  double eint = P.f[F_E][i] - ekin - 0.0;
+  const double pos[3] = {P.f[F_X][i], P.f[F_Y][i], D == 3 ? P.f[F_Z][i] : 0.0};
+  double eint = P.f[F_E][i] - ekin - ext_potential<D>(pp, pos);
   if(!(eint > 0))
     raise_status(st, FSPH_ERR_NEG_ENERGY, i);
   return eint;
@@ -66,7 +67,8 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
       for(int d = 0; d < D; ++d)
         vv += f[F_VX + d][i] * f[F_VX + d][i];
       double ekin = .5 * vv;
-      f[F_E][i] = ekin + f[F_U][i] + 0.0;
+      const double pos[3] = {f[F_X][i], f[F_Y][i], D == 3 ? f[F_Z][i] : 0.0};
+      f[F_E][i] = ekin + f[F_U][i] + ext_potential<D>(pp, pos);
       break;
     }
     case OP_SAVE_VHALF:  // integration.h:52-55
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
     }
     case OP_RECOMPUTE_THERMO:
     case OP_RECOMPUTE_KICK_E: {  // default_physics.h:169-182 (+ kick_e)
-      double eint = recover_u<D>(P, i, st);
+      double eint = recover_u<D>(P, pp, i, st);
       f[F_U][i] = eint;
       double vda = 0;
       for(int d = 0; d < D; ++d)
@@ -144,6 +146,26 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
     case OP_INIT_ALPHA:  // viscosity::initialize_alpha (viscosity.h:171-177)
       f[F_ALPHA][i] = pp.cullen ? 0.0 : pp.alpha;
       break;
+    case OP_DRAG_ACC:    // add_drag_acceleration (default_physics.h:699-708)
+    case OP_DRAG_DEDT:   // add_drag_dedt (:571-579)
+    case OP_DRAG_DUDT: { // add_drag_dudt (:586-594)
+      double vel[3] = {0.0, 0.0, 0.0}, drag[3];
+      for(int d = 0; d < D; ++d)
+        vel[d] = f[F_VX + d][i];
+      drag_acceleration<D>(pp, vel, drag);
+      if(op == OP_DRAG_ACC) {
+        for(int d = 0; d < D; ++d)
+          f[F_AX + d][i] = f[F_AX + d][i] + drag[d];
+      }
+      else {
+        double v_dot_a = 0.0;
+        for(int d = 0; d < D; ++d)
+          v_dot_a += vel[d] * drag[d];
+        const int F = op == OP_DRAG_DEDT ? F_DEDT : F_DUDT;
+        f[F][i] = f[F][i] + v_dot_a;
+      }
+      break;
+    }
     case OP_SET_H:  // second half of compute_average_smoothinglength
       f[F_H][i] = 1. / (double)P.n * tm->hsum;
       break;
@@ -265,10 +287,16 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
       double gdv = 0;
       for(int d = 0; d < D; ++d)
         gdv += f[F_VX + d][i] * f[F_GAX + d][i];
-      if(gdv != 0.0) {  // -dtmin * 0 < eint/2 holds at once
+      // with no external potential and v . g = 0, the first test passes
+      if(gdv != 0.0 || pp.n_eforce > 0) {
+        const double pos[3] = {f[F_X][i], f[F_Y][i], D == 3 ? f[F_Z][i] : 0.0};
+        const double epot = ext_potential<D>(pp, pos);
         int it;
         for(it = 0; it < 20; ++it) {
-          double delta_epot = 0.0 - 0.0;
+          double p1[3] = {0.0, 0.0, 0.0};
+          for(int d = 0; d < D; ++d)
+            p1[d] = pos[d] + dtmin * f[F_VX + d][i];
+          double delta_epot = ext_potential<D>(pp, p1) - epot;
           double delta_egrv = -dtmin * gdv;
           if(delta_epot + delta_egrv < eint * 0.5)
             break;
@@ -422,8 +450,10 @@ __global__ void __launch_bounds__(256) k_conserved_part(Particles P,
     s[0] += m;
     if(pp.thermokinetic)
       s[1] += m * P.f[F_E][i];
-    else
-      s[1] += m * (P.f[F_U][i] + .5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+    else {
+      const double epot = D == 3 ? ext_potential<3>(pp, x) : ext_potential<2>(pp, x);
+      s[1] += m * (.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) + P.f[F_U][i] + epot);
+    }
     s[1] += .5 * m * P.f[F_GPOT][i];
     for(int d = 0; d < 3; ++d)
       s[2 + d] += m * v[d];

@@ -148,9 +148,12 @@ fsph_status set_lanes(fsph_ensemble * e, int lanes) {
   return FSPH_OK;
 }
 
+// Relaxation iterations run eagerly: their extra passes depend on the
+// iteration number, which a captured graph would freeze.
 bool graph_ready(const fsph_ctx * c) {
   return c->uploaded && !c->periodic && !c->timing &&
-         c->iteration > c->p.initial_iteration + 1;
+         c->iteration > c->p.initial_iteration + 1 &&
+         c->iteration >= c->p.relaxation_steps;
 }
 
 // Capture one regular iteration of every member from its current host view,

@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_density(Particles P,
     for(int d = 0; d < D; ++d)
       vv += P.f[F_VX + d][a] * P.f[F_VX + d][a];
     double ekin = .5 * vv;
-    double eint = P.f[F_E][a] - ekin - 0.0;
+    const double pos_a[3] = {pa0, pa1, pa2};
+    double eint = P.f[F_E][a] - ekin - ext_potential<D>(pp, pos_a);
     if(!(eint > 0))
       raise_status(st, FSPH_ERR_NEG_ENERGY, a);
     u = eint;
@@ -281,9 +282,13 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_accel(Particles P,
     for(int d = 0; d < D; ++d)
       acc[d] += DiWa[d] * s;
   }
+  // acc_a += external_force::acceleration(particle) (:404)
+  double ext[3] = {0.0, 0.0, 0.0};
+  if(pp.has_eacc)
+    ext_acceleration<D>(pp, pa, ext);
   const double half_dt = kick ? 0.5 * tm->dt : 0.0;
   for(int d = 0; d < D; ++d) {
-    const double ad = acc[d] + 0.0;
+    const double ad = acc[d] + ext[d];
     P.f[F_AX + d][a] = ad;
     P.f[F_GAX + d][a] = 0.0;
     if(kick)
@@ -295,10 +300,15 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_accel(Particles P,
 // compute_dudt (default_physics.h:421-487)
 template<int D, int K>
 __global__ void __launch_bounds__(PAIR_THREADS) k_dudt(Particles P,
-  PhysParams pp, Lists Ls) {
+  PhysParams pp, Lists Ls, const DevTime * tm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
     return;
+  // no internal energy change while relaxing (:423-427)
+  if(tm->iteration < pp.relax_steps) {
+    P.f[F_DUDT][a] = 0.0;
+    return;
+  }
   const double * X = P.f[F_X];
   const double * Y = P.f[F_Y];
   const double * Z = P.f[F_Z];
@@ -465,6 +475,59 @@ cudaError_t launch_alpha_cullen(const Launch & L, const Particles & P,
   return cudaGetLastError();
 }
 
+// add_short_range_repulsion (default_physics.h:723-753): neighbours other
+// than the particle itself (by id) within relaxation_repulsion_radius of
+// h_ab push it away with m_b x_ab / r_ab^3, scaled by
+// relaxation_repulsion_gamma.  FP64 on both precision paths (it runs in
+// relaxation iterations only).
+template<int D>
+__global__ void __launch_bounds__(PAIR_THREADS) k_repulsion(Particles P,
+  PhysParams pp, Lists Ls) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const double * H = P.f[F_H];
+  const double * M = P.f[F_M];
+  const double h_a = H[a];
+  const long long id_a = P.id[a];
+  double pa[3] = {0.0, 0.0, 0.0}, acc_r[3] = {0.0, 0.0, 0.0};
+  for(int d = 0; d < D; ++d)
+    pa[d] = P.f[F_X + d][a];
+  const int cnt = Ls.cnt[a];
+  for(int j = 0; j < cnt; ++j) {
+    const int b = Ls.idx[list_slot(a, j, Ls.maxnb)];
+    if(P.id[b] == id_a)
+      continue;
+    double dx[3] = {0.0, 0.0, 0.0};
+    double r2 = 0.0;
+    for(int d = 0; d < D; ++d) {
+      dx[d] = pa[d] - P.f[F_X + d][b];
+      r2 += dx[d] * dx[d];
+    }
+    const double h_ab = .5 * (h_a + H[b]);
+    const double r_ab = sqrt(r2);
+    if(r_ab > h_ab * pp.rep_radius)
+      continue;
+    const double m_b = M[b];
+    const double r3 = r_ab * r_ab * r_ab;
+    for(int d = 0; d < D; ++d)
+      acc_r[d] += m_b * dx[d] / r3;
+  }
+  for(int d = 0; d < D; ++d)
+    P.f[F_AX + d][a] = P.f[F_AX + d][a] + acc_r[d] * pp.rep_gamma;
+}
+
+cudaError_t launch_repulsion(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls) {
+  const int nb = (P.n + PAIR_THREADS - 1) / PAIR_THREADS;
+  if(pp.dim == 3)
+    k_repulsion<3><<<nb, PAIR_THREADS, 0, L.stream>>>(P, pp, Ls);
+  else
+    k_repulsion<2><<<nb, PAIR_THREADS, 0, L.stream>>>(P, pp, Ls);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_vsig_fp64(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const double * cs_new) {
   const int nb = (P.n + PAIR_THREADS - 1) / PAIR_THREADS;
@@ -483,8 +546,8 @@ cudaError_t launch_accel_fp64(const Launch & L, const Particles & P,
 }
 
 cudaError_t launch_dudt_fp64(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const DevTime *) {
-  DISPATCH_DK(k_dudt, P, pp, Ls);
+  const PhysParams & pp, const Lists & Ls, const DevTime * t) {
+  DISPATCH_DK(k_dudt, P, pp, Ls, t);
   return cudaGetLastError();
 }
 

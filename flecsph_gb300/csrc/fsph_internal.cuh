@@ -51,6 +51,20 @@ struct PhysParams {
   double gamma2, rho_thr;                 // eos_ppt upper segment
   double out_screen_dt, out_scalar_dt, out_h5data_dt;
   double G;
+  // external forces (eforce.h) in the order external_force::select lists
+  // them, with the parameters their functions read
+  int n_eforce, eforce[8];
+  int has_eacc;                // a term with an acceleration (all but poison)
+  int dprof;                   // density profile of the density support
+  double ew_n, ew_a;           // extforce_wall_powerindex, _steepness
+  double box_half[3];          // .5 * box_length, _width, _height
+  double sphere_r, grav_acc, poison;
+  double orb_a, orb_mns, orb_mwd;
+  double af_size, af_thick, af_camber, af_x, af_y, af_alpha;  // alpha in radians
+  double ds_K0, ds_rho0, rho_init, mesa_q, mesa_rho0;         // density support
+  // particle relaxation (default_physics.h:571-599,699-753)
+  double relax_beta, relax_gamma, rep_radius, rep_gamma;
+  long long relax_steps;       // relaxation_steps
 };
 
 // Binary radix tree over the sorted keys (n-1 internal nodes, node 0 is the
@@ -182,7 +196,7 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
   const DevTime * t, int fused_vsig);
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
 
@@ -220,6 +234,8 @@ cudaError_t launch_alpha_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const DevTime * t);
 cudaError_t launch_vsig_fp64(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const double * cs_new);
+cudaError_t launch_repulsion(const Launch & L, const Particles & P,
+  const PhysParams & pp, const Lists & Ls);
 cudaError_t launch_accel_fp64(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, int kick, const DevTime * t);
 cudaError_t launch_dudt_fp64(const Launch & L, const Particles & P,
@@ -233,7 +249,7 @@ enum ElemOp {
   OP_KICK_E, OP_DRIFT, OP_RECOMPUTE, OP_RECOMPUTE_THERMO, OP_SMOOTHING_LENGTH,
   OP_CHECK_NANS, OP_CHECK_NEGATIVITY, OP_KICK_DRIFT_E, OP_KICK_DRIFT_U,
   OP_KICK_DRIFT_NONE, OP_SET_H, OP_RECOMPUTE_KICK_E, OP_RECOMPUTE_KICK_U,
-  OP_INIT_ALPHA
+  OP_INIT_ALPHA, OP_DRAG_ACC, OP_DRAG_DEDT, OP_DRAG_DUDT
 };
 cudaError_t launch_elementwise(const Launch & L, const Particles & P,
   const PhysParams & pp, int op, DevTime * t, DevStatus * st);

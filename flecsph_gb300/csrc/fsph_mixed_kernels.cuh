@@ -288,7 +288,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
     double vv = 0;
     for(int d = 0; d < D; ++d)
       vv += P.f[F_VX + d][a] * P.f[F_VX + d][a];
-    double eint = P.f[F_E][a] - .5 * vv;
+    const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
+    double eint = P.f[F_E][a] - .5 * vv - ext_potential<D>(pp, pos);
     if(!(eint > 0)) {
       if(atomicCAS(&st->code, 0, (int)FSPH_ERR_NEG_ENERGY) == 0)
         st->index = a;
@@ -374,8 +375,15 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
         kahan(az, cz, g.dz * sc);
     }
   }
-  const double acc[3] = {(double)ax - (double)cx, (double)ay - (double)cy,
+  double acc[3] = {(double)ax - (double)cx, (double)ay - (double)cy,
     D == 3 ? (double)az - (double)cz : 0.0};
+  if(pp.has_eacc) {  // acc_a += external_force::acceleration (:404)
+    const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
+    double ext[3];
+    ext_acceleration<D>(pp, pos, ext);
+    for(int d = 0; d < D; ++d)
+      acc[d] += ext[d];
+  }
   const double half_dt = kick ? 0.5 * tm->dt : 0.0;
   double v[3] = {0, 0, 0};
   for(int d = 0; d < D; ++d) {
@@ -395,10 +403,15 @@ __global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
 // --------------------------------------------------------------- du/dt --
 template<int D, int K, bool CULL>
 __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
-  PhysParams pp, Lists Ls, Packed Kp) {
+  PhysParams pp, Lists Ls, Packed Kp, const DevTime * tm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
     return;
+  // no internal energy change while relaxing (default_physics.h:423-427)
+  if(tm->iteration < pp.relax_steps) {
+    P.f[F_DUDT][a] = 0.0;
+    return;
+  }
   const float s0 = Kp.qscale[0], s1 = Kp.qscale[1], s2 = D == 3 ? Kp.qscale[2] : 0.f;
   const float eps = (float)pp.eps, alpha = (float)pp.alpha, beta = (float)pp.beta;
   const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
@@ -549,8 +562,8 @@ inline void run_density_mixed(const Launch & L, const Particles & P,
 
 template<bool CULL>
 inline void run_dudt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K) {
-  MIX_DISPATCH(k_dudt_mixed, CULL, P, pp, Ls, K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t) {
+  MIX_DISPATCH(k_dudt_mixed, CULL, P, pp, Ls, K, t);
 }
 
 template<bool CULL>
@@ -604,7 +617,7 @@ void run_accel_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
   const DevTime * t, int fused_vsig);
 void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
 void run_alpha_mixed(const Launch & L, const Particles & P,

@@ -5,6 +5,7 @@
 #pragma once
 
 #include "fsph_internal.cuh"
+#include "fsph_eforce.cuh"
 
 namespace fsph {
 

@@ -437,12 +437,15 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
 // node's raw mass moments (ten FP64 sums: children add, so every level
 // costs ten additions whatever the order of the multipoles built from
 // them).
+// refboxes: also the reference's x +- h/2 node boxes (box2, fbox2), which
+// the walk's node tests read: with varying h, or in the ordered (FP64) mode
+// where equal-h ties take them too.
 __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
-  const unsigned long long * rbits) {
+  const unsigned long long * rbits, int refboxes) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
-  const bool nonuni = rbits[6] != rbits[7];
+  const bool nonuni = refboxes || rbits[6] != rbits[7];
   double rc[3] = {0.0, 0.0, 0.0};
   if(T.gmom)
     for(int d = 0; d < dim; ++d)
@@ -585,9 +588,10 @@ __device__ __forceinline__ int node_level(const unsigned long long * K,
 // first octree ancestor holding more than 128 particles
 // (tree_topology.h:220-235, sub_entities_ = 128 at :2121).
 __global__ void k_refgroups(const unsigned long long * K, int n, int dim,
-  Tree T, const unsigned long long * rbits) {
+  Tree T, const unsigned long long * rbits, int refboxes) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= n || rbits[6] == rbits[7])  // only read when h varies
+  // read only when h varies, or for ties in the ordered mode
+  if(i >= n || (!refboxes && rbits[6] == rbits[7]))
     return;
   const int lead = 64 - (63 / dim) * dim;
   int p = T.leaf_parent[i];
@@ -620,9 +624,10 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   k_karras<<<(n + 254) / 256, 256, 0, L.stream>>>(P.key, n, T);
   if(ordered)  // reference octree depths order the FP64 lists
     k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
-  k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits);
+  k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits, ordered);
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max);
-  k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits);
+  k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits,
+    ordered);
   *L.counter += 5;
   return cudaGetLastError();
 }
@@ -750,8 +755,9 @@ __device__ __forceinline__ int sphere_box_f(const float4 & lo,
 // With varying h the reference's walk drops a candidate b of particle a
 // unless the box of b's octree parent passes both node tests against a's
 // traversal group G (tree_topology.h:323-355): box-box with G's box when G
-// is a node, and sphere-box with at least one member of G.  Neither test
-// can fail for a pair passing the predicate when every h is equal.  Each
+// is a node, and sphere-box with at least one member of G.  When every h
+// is equal only the box-box test can fail, and only for a pair whose
+// separation along an axis ties with h to rounding.  Each
 // test is decided in FP32 first and in FP64 (box_box, sphere_box) only when
 // the FP32 answer is not certain, so the answers are the FP64 ones.
 __device__ bool ref_node_tests_mixed(const Tree & T, const double * X,
@@ -893,7 +899,9 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
     double g2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     float4 fglo = make_float4(0.f, 0.f, 0.f, 0.f), fghi = fglo;
     float cax = 0.f, cay = 0.f, caz = 0.f;
-    if(mem && nonuni) {
+    // the reference's group and boxes exist with varying h, and in the
+    // ordered mode (k_bounds, k_refgroups)
+    if(mem && (nonuni || ORDERED)) {
       gnode = T.gref[a];
       if(gnode >= 0) {
         const double * gp = (const double *)&T.box2[gnode];
@@ -1034,6 +1042,15 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
             return ref_node_tests_mixed(T, X, Y, Z, H, dim, b, a, xa, ya, za, ha,
               cax, cay, caz, haf, gnode, g2, fglo, fghi, rlo, ftol);
           };
+          // Equal h: the node tests can only drop a pair whose separation
+          // along some axis ties with h, where the rounding of x +- h/2 in
+          // the boxes decides (box-box, tree_topology.h:326-330).  In the
+          // ordered mode such pairs (none off a lattice) take the tests,
+          // decided exactly; the mixed path keeps them (W(h) = 0 for the
+          // compactly supported kernels).
+          auto tie = [&](float fx, float fy, float fz, float rf) {
+            return fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= rf - kq;
+          };
           auto append = [&](int b) {
             if(nonuni && !refdone && cnt == maxnb) {
               int kept = 0;
@@ -1064,14 +1081,13 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
               const float rf = fmaxf(haf, __int_as_float(qb.w));
               const float t = d2f - rf * rf;
               const float mg = rf * (4e-5f * rf + kq);
-              if(decide(t, mg, b))
+              if(decide(t, mg, b) && (nonuni || !tie(fx, fy, fz, rf) || refok(b)))
                 append(b);
             }
           }
           else if(!nonuni) {
             // every h is equal: r and the margin are constants of the group
-            // and the predicate alone decides (the reference's node tests
-            // cannot fail, ref_node_tests)
+            // and the predicate decides (ties included, see tie)
             const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay);
             const float2 az2 = make_float2(az, az);
             const float r2 = haf * haf;

@@ -93,8 +93,23 @@ bool set_param(fsph_params & p, const std::string & kv) {
   if(eq == std::string::npos)
     return false;
   std::string k = kv.substr(0, eq);
+  if(k == "external_force_type")
+    return fsph_params_set_external_force(&p, kv.c_str() + eq + 1) == FSPH_OK;
   double v = std::atof(kv.c_str() + eq + 1);
   if(k == "poly_gamma") p.poly_gamma = v;
+  else if(k == "sph_viscosity") p.sph_viscosity = (int32_t)v;
+  else if(k == "relaxation_steps") p.relaxation_steps = (int32_t)v;
+  else if(k == "relaxation_beta") p.relaxation_beta = v;
+  else if(k == "relaxation_gamma") p.relaxation_gamma = v;
+  else if(k == "relaxation_repulsion_radius") p.relaxation_repulsion_radius = v;
+  else if(k == "relaxation_repulsion_gamma") p.relaxation_repulsion_gamma = v;
+  else if(k == "gravity_acceleration_constant") p.gravity_acceleration_constant = v;
+  else if(k == "sphere_radius") p.sphere_radius = v;
+  else if(k == "extforce_wall_powerindex") p.extforce_wall_powerindex = v;
+  else if(k == "extforce_wall_steepness") p.extforce_wall_steepness = v;
+  else if(k == "box_length") p.box_length = v;
+  else if(k == "box_width") p.box_width = v;
+  else if(k == "box_height") p.box_height = v;
   else if(k == "sph_eta") p.sph_eta = v;
   else if(k == "sph_kernel") p.sph_kernel = (int32_t)v;
   else if(k == "eos_type") p.eos_type = (int32_t)v;
@@ -141,6 +156,7 @@ int main(int argc, char ** argv) {
     fsph_soa_view v = s.view();
     bs.read_bodies(v);
     for(int it = 0; it < iterations; ++it) {
+      const bool relax = bs.iteration() < p.relaxation_steps;
       if(it == 0) {
         bs.update_iteration();
         bs.apply_all(eos::init);
@@ -154,16 +170,24 @@ int main(int argc, char ** argv) {
           bs.apply_in_smoothinglength(viscosity::compute_alpha);
         bs.reset_ghosts();
         bs.apply_in_smoothinglength(physics::compute_acceleration);
+        if(relax) {
+          bs.apply_all(physics::add_drag_acceleration);
+          bs.apply_in_smoothinglength(physics::add_short_range_repulsion);
+        }
         if(p.adaptive_timestep) {
           bs.apply_all(physics::compute_dt);
           bs.get_all(physics::set_adaptive_timestep);
         }
         if(p.thermokinetic_formulation) {
           bs.apply_in_smoothinglength(physics::compute_dedt);
+          if(relax)
+            bs.apply_all(physics::add_drag_dedt);
           bs.apply_all(physics::recompute_pressure_soundspeed_thermokinetic);
         }
         else {
           bs.apply_in_smoothinglength(physics::compute_dudt);
+          if(relax)
+            bs.apply_all(physics::add_drag_dudt);
           bs.apply_all(physics::recompute_pressure_soundspeed);
         }
       }
@@ -181,15 +205,23 @@ int main(int argc, char ** argv) {
           bs.apply_in_smoothinglength(viscosity::compute_alpha);
         bs.reset_ghosts();
         bs.apply_in_smoothinglength(physics::compute_acceleration);
+        if(relax) {
+          bs.apply_all(physics::add_drag_acceleration);
+          bs.apply_in_smoothinglength(physics::add_short_range_repulsion);
+        }
         bs.apply_all(integration::leapfrog_kick_v);
         bs.reset_ghosts();
         if(p.thermokinetic_formulation) {
           bs.apply_in_smoothinglength(physics::compute_dedt);
+          if(relax)
+            bs.apply_all(physics::add_drag_dedt);
           bs.apply_all(physics::recompute_pressure_soundspeed_thermokinetic);
           bs.apply_all(integration::leapfrog_kick_e);
         }
         else {
           bs.apply_in_smoothinglength(physics::compute_dudt);
+          if(relax)
+            bs.apply_all(physics::add_drag_dudt);
           bs.apply_all(physics::recompute_pressure_soundspeed);
           bs.apply_all(integration::leapfrog_kick_u);
         }

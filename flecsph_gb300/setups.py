@@ -288,6 +288,103 @@ def ensemble2d(nproblems=256, nmin=2000, nmax=200000, seed=2024):
     return out
 
 
+EXTERNAL_FORCE_PROBLEMS = ["gravity_walls_2d", "spherical_wall_3d", "density_support_3d",
+                           "mesa_support_2d", "airfoil_2d", "orbit_3d", "relaxation_3d",
+                           "relaxation_dudt_2d"]
+
+
+def external_force_problem(name):
+    """Small problems exercising each external force of include/physics/
+    eforce.h and the particle relaxation terms; returns (state, params).
+
+    gravity_walls_2d: a Sod tube in uniform gravity (plus a potential shift)
+        between walls in y placed inside the lattice, so that the outer rows
+        feel them; spherical_wall_3d: a Sedov blast inside a spherical wall of
+        radius 0.45 (the corners are outside); density_support_3d /
+        mesa_support_2d: a polytrope / disc held by the parabolic / mesa
+        support potential; airfoil_2d: a uniform stream past an airfoil tilted
+        by 5 degrees; orbit_3d: a Sod tube scaled to 1e8 cm in the
+        neutron-star + white-dwarf co-rotating potential; relaxation_3d /
+        relaxation_dudt_2d: drag and short-range repulsion while relaxing (e
+        and u formulations).
+    """
+    from .abi import (DENSITY_MESA, DENSITY_PARABOLIC, EFORCE_AIRFOIL, EFORCE_GRAVITY,
+                      EFORCE_ORBIT, EFORCE_POISON, EFORCE_SPHERICAL_DENSITY_SUPPORT,
+                      EFORCE_SPHERICAL_WALL, EFORCE_WALLS_X, EFORCE_WALLS_Y)
+    if name == "gravity_walls_2d":
+        s, p, m = sod2d(100, 10)
+        p.set_forces([EFORCE_GRAVITY, EFORCE_WALLS_Y, EFORCE_POISON, EFORCE_WALLS_X])
+        p.gravity_acceleration_constant = 2.0
+        p.zero_potential_poison_value = 0.3
+        p.box_length, p.box_width = 0.98, 0.08
+    elif name == "spherical_wall_3d":
+        s, p, m = sedov3d(16, eta=1.44)
+        p.set_forces([EFORCE_SPHERICAL_WALL])
+        p.sphere_radius = 0.45
+        p.extforce_wall_steepness = 20.0
+        p.extforce_wall_powerindex = 3.0
+    elif name == "density_support_3d":
+        s, p, m = polytrope3d(3000)
+        p.enable_fmm = 0
+        p.set_forces([EFORCE_SPHERICAL_DENSITY_SUPPORT])
+        p.density_profile = DENSITY_PARABOLIC
+        p.sphere_radius = 0.9
+        p.rho_initial, p.pressure_initial = 2.0, 0.5
+        p.extforce_wall_steepness = 10.0
+    elif name == "mesa_support_2d":
+        s, p, m = noh2d(40)
+        for k in ("vx", "vy"):
+            s[k][:] = 0.0
+        s["u"][:] = 1.0
+        s["P"][:] = (p.poly_gamma - 1.0) * s["rho"] * s["u"]
+        p.set_forces([EFORCE_SPHERICAL_DENSITY_SUPPORT])
+        p.density_profile = DENSITY_MESA
+        p.sphere_radius = 0.45
+        p.mesa_rim_width = 0.3
+        p.extforce_wall_steepness = 100.0
+    elif name == "airfoil_2d":
+        s, p, m = sod2d(200, 20)
+        s["rho"][:] = 1.0
+        s["m"][:] = (1.0 / 200) ** 2
+        s["P"][:] = 1.0
+        s["u"][:] = s["P"] / ((p.poly_gamma - 1.0) * s["rho"])
+        s["vx"][:] = 0.5
+        p.set_forces([EFORCE_AIRFOIL])
+        p.airfoil_size, p.airfoil_thickness, p.airfoil_camber = 0.8, 0.06, 0.02
+        p.airfoil_anchor_x, p.airfoil_anchor_y = -0.4, 0.0
+        p.airfoil_attack_angle = 5.0
+    elif name == "orbit_3d":
+        s, p, m = sod3d(20, 10, 10)
+        L = 1.0e8
+        for k in ("x", "y", "z", "h"):
+            s[k] *= L
+        s["m"] *= L ** 3
+        s["u"] *= 1.0e10
+        s["P"] *= 1.0e10
+        p.set_forces([EFORCE_ORBIT])
+        p.gravitational_constant = 6.674e-8
+    elif name == "relaxation_3d":
+        s, p, m = sedov3d(16, eta=1.44)
+        p.relaxation_steps = 8
+        p.relaxation_beta, p.relaxation_gamma = 0.2, 3.0
+        p.relaxation_repulsion_radius, p.relaxation_repulsion_gamma = 0.5, 1e-7
+        rng = np.random.Generator(np.random.PCG64(5))
+        for k in ("vx", "vy", "vz"):
+            s[k][:] = rng.normal(0.0, 0.05, len(s["x"]))
+    elif name == "relaxation_dudt_2d":
+        s, p, m = sod2d(100, 10)
+        p.thermokinetic_formulation = 0
+        p.relaxation_steps = 8
+        p.relaxation_beta, p.relaxation_gamma = 0.1, 1.0
+        p.relaxation_repulsion_radius, p.relaxation_repulsion_gamma = 0.6, 1e-6
+        s["vx"][:] = 0.1 * np.sin(2 * np.pi * s["x"])
+    else:
+        raise ValueError(name)
+    if p.dimension == 3:
+        p.max_neighbors = 1024  # walls and supports compress the outer layers
+    return s, p
+
+
 def shuffled(state, seed=99):
     """The same particles in a seeded random order (ids travel along)."""
     n = len(state["x"])

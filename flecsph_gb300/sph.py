@@ -32,7 +32,8 @@ _STEP_FUNCS = [
     "recompute_pressure_soundspeed_thermokinetic", "compute_dt", "check_nans",
     "check_negativity", "set_adaptive_timestep", "compute_smoothinglength",
     "compute_average_smoothinglength", "gravitation", "advance_time", "step", "sync",
-    "timers_reset", "compute_alpha", "initialize_alpha",
+    "timers_reset", "compute_alpha", "initialize_alpha", "add_drag_acceleration",
+    "add_short_range_repulsion", "add_drag_dedt", "add_drag_dudt",
 ]
 
 
@@ -50,6 +51,7 @@ def library():
     lib.fsph_destroy.argtypes = [C.c_void_p]
     lib.fsph_destroy.restype = None
     lib.fsph_params_default.argtypes = [C.POINTER(Params)]
+    lib.fsph_params_set_external_force.argtypes = [C.POINTER(Params), C.c_char_p]
     lib.fsph_params_default.restype = None
     lib.fsph_abi_version.restype = C.c_int32
     lib.fsph_status_string.restype = C.c_char_p
@@ -307,6 +309,16 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+def set_external_force(params, external_force_type):
+    """Fill params.external_force from an external_force_type string, as
+    external_force::select parses it (fsph_params_set_external_force)."""
+    st = library().fsph_params_set_external_force(C.byref(params),
+                                                  external_force_type.encode())
+    if st:
+        raise FsphError(st, "set_external_force", external_force_type)
+    return params
 
 
 def capacity_for(params, n, state=None, margin=0.25):

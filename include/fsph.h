@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FSPH_ABI_VERSION 4
+#define FSPH_ABI_VERSION 5
 
 /* Status codes.  They replace the reference's assert()/mpi_assert() aborts
  * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
@@ -89,6 +89,29 @@ enum fsph_eos {
 };
 /* param::sph_viscosity_keyword (include/params.h:148-152). */
 enum fsph_viscosity { FSPH_VISC_CONSTANT = 0, FSPH_VISC_CULLEN = 1 };
+/* The terms external_force::select (include/physics/eforce.h:359-434)
+ * builds from external_force_type, one code per potential/acceleration in
+ * the order the string names them ("walls:xyz" gives three codes). */
+enum fsph_eforce {
+  FSPH_EFORCE_NONE = 0,                      /* ends the list */
+  FSPH_EFORCE_WALLS_X = 1,                   /* eforce.h:46-82, box_length */
+  FSPH_EFORCE_WALLS_Y = 2,                   /* box_width */
+  FSPH_EFORCE_WALLS_Z = 3,                   /* box_height */
+  FSPH_EFORCE_SPHERICAL_WALL = 4,            /* eforce.h:84-121 */
+  FSPH_EFORCE_SPHERICAL_DENSITY_SUPPORT = 5, /* eforce.h:123-168 */
+  FSPH_EFORCE_GRAVITY = 6,                   /* eforce.h:170-192 */
+  FSPH_EFORCE_AIRFOIL = 7,                   /* eforce.h:194-271 (2D) */
+  FSPH_EFORCE_ORBIT = 8,                     /* eforce.h:273-313 (3D) */
+  FSPH_EFORCE_POISON = 9                     /* eforce.h:315-321 (potential only) */
+};
+#define FSPH_MAX_EFORCE 8
+/* param::density_profile (include/physics/density_profiles.h:355-398); the
+ * tabulated "from file" profile is not supported. */
+enum fsph_density_profile {
+  FSPH_DENSITY_CONSTANT = 0,
+  FSPH_DENSITY_PARABOLIC = 1,
+  FSPH_DENSITY_MESA = 2
+};
 enum fsph_precision {
   FSPH_PRECISION_FP64 = 0,  /* every pair term in FP64 (plain method) */
   FSPH_PRECISION_MIXED = 1  /* FP32 pair math with compensated sums; FP64 state */
@@ -127,7 +150,7 @@ typedef struct fsph_params {
   int32_t pressure_updates_number;   /* [194] 1 */
   int32_t sph_variable_h;            /* [244] false */
   int32_t sph_update_uniform_h;      /* [238] false */
-  int32_t relaxation_steps;          /* [563] 0 (only 0 is supported) */
+  int32_t relaxation_steps;          /* [563] 0 */
   int32_t enable_fmm;                /* [537] false */
   int32_t periodic_boundary_x;       /* [292] false */
   int32_t periodic_boundary_y;       /* [296] false */
@@ -144,6 +167,34 @@ typedef struct fsph_params {
   double sph_sinc_index;             /* [232] 4.0, sinc kernel power */
   double poly_gamma2;                /* [483] 2.5, eos_ppt upper segment */
   double ppt_density_thr;            /* [488] 5e14, eos_ppt threshold */
+  /* external forces: external_force_type [597] "none" as the list of
+   * fsph_eforce codes that external_force::select builds from it
+   * (fsph_params_set_external_force parses the string) */
+  int32_t external_force[FSPH_MAX_EFORCE];
+  int32_t density_profile;           /* [671] "constant" (enum fsph_density_profile) */
+  int32_t reserved_pad2;
+  double extforce_wall_powerindex;   /* [608] 5.0 */
+  double extforce_wall_steepness;    /* [613] 1e12 */
+  double sphere_radius;              /* [270] 1.0 */
+  double gravity_acceleration_constant; /* [623] 9.81 */
+  double orbital_separation;         /* [637] 2.5e9 */
+  double mass_neutron_star;          /* [642] 1.26 * 1.988435e33 */
+  double mass_white_dwarf;           /* [647] 1.10 * 1.988435e33 */
+  double zero_potential_poison_value;/* [603] 0.0 */
+  double airfoil_size;               /* [761] 2.0 */
+  double airfoil_thickness;          /* [765] 0.05 */
+  double airfoil_camber;             /* [769] 0.1 */
+  double airfoil_anchor_x;           /* [773] -1.0 */
+  double airfoil_anchor_y;           /* [777] 0.0 */
+  double airfoil_attack_angle;       /* [781] 0.0 (degrees) */
+  double rho_initial;                /* [682] 1.0 */
+  double pressure_initial;           /* [687] 1.0 */
+  double mesa_rim_width;             /* [618] 0.25 */
+  /* particle relaxation, iterations < relaxation_steps */
+  double relaxation_beta;            /* [568] 1e-6 */
+  double relaxation_gamma;           /* [572] 0.0 */
+  double relaxation_repulsion_radius;/* [576] 0.25 */
+  double relaxation_repulsion_gamma; /* [580] 0.0 */
   int32_t reserved[8];
 } fsph_params;
 
@@ -211,6 +262,14 @@ typedef struct fsph_ctx fsph_ctx;
 
 /* -- lifetime ------------------------------------------------------------ */
 void fsph_params_default(fsph_params * p);
+/* external_force::select (include/physics/eforce.h:359-434): fill
+ * p->external_force from an external_force_type string, a comma-separated
+ * list of "spherical wall", "airfoil", "spherical density support",
+ * "gravity", "orbit", "walls:<xyz>", "poison" (case-insensitive; "none" or
+ * "zero" alone for no force).  An unknown term returns FSPH_ERR_ARG, where
+ * the reference stops with log_fatal; more than FSPH_MAX_EFORCE terms too. */
+fsph_status fsph_params_set_external_force(fsph_params * p,
+  const char * external_force_type);
 int32_t fsph_abi_version(void);
 /* Creates a context on `device` able to hold `capacity` particles. */
 fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
@@ -259,6 +318,16 @@ fsph_status fsph_initialize_alpha(fsph_ctx * ctx);
 fsph_status fsph_acceleration(fsph_ctx * ctx);
 fsph_status fsph_dudt(fsph_ctx * ctx);
 fsph_status fsph_dedt(fsph_ctx * ctx);
+/* particle relaxation terms (default_physics.h:571-599,699-753), which the
+ * hydro driver adds while iteration < relaxation_steps
+ * (hydro/main_driver.cc:129-134,150-165,204-207): */
+/* apply_all(physics::add_drag_acceleration) */
+fsph_status fsph_add_drag_acceleration(fsph_ctx * ctx);
+/* apply_in_smoothinglength(physics::add_short_range_repulsion) */
+fsph_status fsph_add_short_range_repulsion(fsph_ctx * ctx);
+/* apply_all(physics::add_drag_dedt) / apply_all(physics::add_drag_dudt) */
+fsph_status fsph_add_drag_dedt(fsph_ctx * ctx);
+fsph_status fsph_add_drag_dudt(fsph_ctx * ctx);
 /* apply_all(...) */
 fsph_status fsph_eos_init(fsph_ctx * ctx);
 fsph_status fsph_set_total_energy(fsph_ctx * ctx);

@@ -52,6 +52,14 @@ struct check_negativity_t {};
 struct set_adaptive_timestep_t {};
 struct compute_smoothinglength_t {};
 struct compute_average_smoothinglength_t {};
+struct add_drag_acceleration_t {};
+struct add_short_range_repulsion_t {};
+struct add_drag_dedt_t {};
+struct add_drag_dudt_t {};
+constexpr add_drag_acceleration_t add_drag_acceleration{};          // default_physics.h:699-708
+constexpr add_short_range_repulsion_t add_short_range_repulsion{};  // :723-753
+constexpr add_drag_dedt_t add_drag_dedt{};                          // :571-579
+constexpr add_drag_dudt_t add_drag_dudt{};                          // :586-594
 constexpr density_pressure_soundspeed_t compute_density_pressure_soundspeed{};
 constexpr acceleration_t compute_acceleration{};
 constexpr dudt_t compute_dudt{};
@@ -164,6 +172,14 @@ public:
       "recompute_pressure_soundspeed_thermokinetic");
   }
   void apply_all(physics::compute_dt_t) { check(fsph_compute_dt(ctx_), "compute_dt"); }
+  void apply_all(physics::add_drag_acceleration_t) {
+    check(fsph_add_drag_acceleration(ctx_), "add_drag_acceleration");
+  }
+  void apply_in_smoothinglength(physics::add_short_range_repulsion_t) {
+    check(fsph_add_short_range_repulsion(ctx_), "add_short_range_repulsion");
+  }
+  void apply_all(physics::add_drag_dedt_t) { check(fsph_add_drag_dedt(ctx_), "add_drag_dedt"); }
+  void apply_all(physics::add_drag_dudt_t) { check(fsph_add_drag_dudt(ctx_), "add_drag_dudt"); }
   void apply_all(physics::check_nans_t) { check(fsph_check_nans(ctx_), "check_nans"); }
   void apply_all(physics::check_negativity_t) {
     check(fsph_check_negativity(ctx_), "check_negativity");

@@ -473,6 +473,260 @@ static void eos_pressure(orc_ctx * c, int64_t i, double uval, double * P,
 }
 
 /* ------------------------------------------------------------ context -- */
+/* ---- external forces (include/physics/eforce.h), density profiles
+ * (include/physics/density_profiles.h:64-230) and the relaxation drag ---- */
+#define ORC_PI 3.14159265358979323846
+static double sq_(double x) { return x * x; }
+static double cu_(double x) { return x * x * x; }
+
+/* mesa_mass_helper (density_profiles.h:163-177) */
+static double mesa_mass_helper(int D, double r, double q) {
+  const double dr = q, r0 = 1. - q;
+  double mm = 0.0;
+  if(D == 2)
+    mm = sq_(r) * (1. - (.5 * sq_(r) + sq_(r0)) / sq_(dr)) +
+         (.5 * cu_(r0) + 4. * cu_(r)) * r0 / (3. * sq_(dr));
+  if(D == 3)
+    mm = cu_(r0) / 3. + (cu_(r) - cu_(r0)) / 3. * (1. - sq_(r0) / sq_(dr)) +
+         r0 * (sq_(r) - sq_(r0)) * (sq_(r) + sq_(r0)) / (2. * sq_(dr)) -
+         (sq_(r) * cu_(r) - sq_(r0) * cu_(r0)) / (5 * sq_(dr));
+  return mm;
+}
+/* density_profiles::select (:355-398) sets mesa_rho0 this way */
+static double mesa_rho0(const orc_ctx * c) {
+  const double q = c->p.mesa_rim_width;
+  return c->D == 2 ? 1. / (ORC_PI * mesa_mass_helper(2, 1., q))
+                   : 1. / (4. * ORC_PI * mesa_mass_helper(3, 1., q));
+}
+/* spherical_density_profile (:69-80, 107-120, 179-188) */
+static double prof_rho(const orc_ctx * c, double r) {
+  const int D = c->D;
+  if(c->p.density_profile == FSPH_DENSITY_PARABOLIC)
+    return D == 2 ? 2. / ORC_PI * (1. - sq_(r)) : 15. / (8. * ORC_PI) * (1. - sq_(r));
+  if(c->p.density_profile == FSPH_DENSITY_MESA) {
+    const double q = c->p.mesa_rim_width, rho0 = mesa_rho0(c), r0 = 1. - q;
+    double rho = 0.0;
+    if(r < 1. - q)
+      rho = rho0;
+    else if(r < .9999)
+      rho = rho0 * (1. - sq_(r - r0) / sq_(q));
+    return rho;
+  }
+  return D == 2 ? 1.0 / ORC_PI : 0.75 / ORC_PI;
+}
+/* spherical_drho_dr (:98-101, 137-150, 215-222) */
+static double prof_drho(const orc_ctx * c, double r) {
+  const int D = c->D;
+  if(c->p.density_profile == FSPH_DENSITY_PARABOLIC)
+    return D == 2 ? -4. / ORC_PI * r : -15. / (4. * ORC_PI) * r;
+  if(c->p.density_profile == FSPH_DENSITY_MESA) {
+    const double q = c->p.mesa_rim_width, rho0 = mesa_rho0(c), r0 = 1. - q;
+    double drhodr = 0.0;
+    if(r > 1. - q && r < .9999)
+      drhodr = -2. * rho0 * (r - r0) / sq_(q);
+    return drhodr;
+  }
+  return 0.;
+}
+
+static double radius3(int D, const double * rp) {
+  double r = rp[0] * rp[0];
+  for(int i = 1; i < D; ++i)
+    r += rp[i] * rp[i];
+  return sqrt(r);
+}
+
+/* wall potentials and accelerations (eforce.h:46-121) */
+static double wall_pot(const orc_ctx * c, int I, const double * rp) {
+  const double box[3] = {.5 * c->p.box_length, .5 * c->p.box_width, .5 * c->p.box_height};
+  const double pw_n = c->p.extforce_wall_powerindex, pw_a = c->p.extforce_wall_steepness;
+  return (((rp[I] < -box[I]) ? pow(-rp[I] - box[I], pw_n) : 0.0) +
+          ((rp[I] > box[I]) ? pow(rp[I] - box[I], pw_n) : 0.0)) * pw_a;
+}
+static double wall_acc(const orc_ctx * c, int I, const double * rp) {
+  const double box[3] = {.5 * c->p.box_length, .5 * c->p.box_width, .5 * c->p.box_height};
+  const double pw_n = c->p.extforce_wall_powerindex, pw_a = c->p.extforce_wall_steepness;
+  return (((rp[I] < -box[I]) ? pow(-rp[I] - box[I], pw_n - 1) : 0.0) -
+          ((rp[I] > box[I]) ? pow(rp[I] - box[I], pw_n - 1) : 0.0)) * pw_n * pw_a;
+}
+static void sphwall_acc(const orc_ctx * c, const double * rp, double * a) {
+  const double pw_n = c->p.extforce_wall_powerindex, pw_a = c->p.extforce_wall_steepness;
+  const double R = c->p.sphere_radius;
+  for(int i = 0; i < 3; ++i)
+    a[i] = 0.0;
+  double r = radius3(c->D, rp);
+  if(r > R) {
+    const double ar = pw_n * pw_a * pow(r - R, pw_n - 1);
+    for(int i = 0; i < c->D; ++i)
+      a[i] = -rp[i] / r * ar;
+  }
+}
+static double sphwall_pot(const orc_ctx * c, const double * rp) {
+  double phi = 0.0;
+  double r = radius3(c->D, rp);
+  if(r > c->p.sphere_radius)
+    phi = c->p.extforce_wall_steepness * pow(r - c->p.sphere_radius, c->p.extforce_wall_powerindex);
+  return phi;
+}
+
+/* airfoil (eforce.h:213-271) */
+static int airfoil(const orc_ctx * c, const double * rp, double * xo, double * yo,
+  double * cam, double * phi) {
+  const fsph_params * p = &c->p;
+  const double x1 = rp[0] - p->airfoil_anchor_x, y1 = rp[1] - p->airfoil_anchor_y,
+               alpha = p->airfoil_attack_angle * ORC_PI / 180.0;
+  const double x = x1 * cos(alpha) + y1 * sin(alpha), y = -x1 * sin(alpha) + y1 * cos(alpha);
+  const int inside = fabs(y) < 5.0 * p->airfoil_thickness && x > -p->airfoil_size * 0.02 &&
+                     x < p->airfoil_size * 1.02;
+  double upper = p->airfoil_thickness * x * sqrt(p->airfoil_size * p->airfoil_size - x * x);
+  double camber_line = p->airfoil_camber * sin(ORC_PI * x / 2.);
+  *phi = sq_(upper) - sq_(y - camber_line) + 0.002;
+  *xo = x;
+  *yo = y;
+  *cam = camber_line;
+  return inside;
+}
+
+/* one term of external_force::potential (eforce.h:336-346) */
+static double eforce_pot(const orc_ctx * c, int code, const double * rp) {
+  const fsph_params * p = &c->p;
+  const int D = c->D;
+  switch(code) {
+    case FSPH_EFORCE_WALLS_X: return wall_pot(c, 0, rp);
+    case FSPH_EFORCE_WALLS_Y: return wall_pot(c, 1, rp);
+    case FSPH_EFORCE_WALLS_Z: return wall_pot(c, 2, rp);
+    case FSPH_EFORCE_SPHERICAL_WALL: return sphwall_pot(c, rp);
+    case FSPH_EFORCE_SPHERICAL_DENSITY_SUPPORT: {
+      const double K0 = p->pressure_initial / pow(p->rho_initial, p->poly_gamma);
+      const double rho0 = prof_rho(c, 0.);
+      double r = radius3(D, rp);
+      const double x = r / p->sphere_radius;
+      double rho = p->rho_initial / rho0 * prof_rho(c, x);
+      double phi = (rho > 0) ? (-K0 * p->poly_gamma * pow(rho, p->poly_gamma - 1.) /
+                                (p->poly_gamma - 1.)) : 0;
+      return phi + sphwall_pot(c, rp);
+    }
+    case FSPH_EFORCE_GRAVITY: {
+      double height = rp[0];
+      if(D > 1)
+        height = rp[1];
+      return height * p->gravity_acceleration_constant;
+    }
+    case FSPH_EFORCE_AIRFOIL: {
+      double x, y, cam, aux, phi = 0.0;
+      int inside = airfoil(c, rp, &x, &y, &cam, &aux);
+      if(inside && aux > 0.0)
+        phi = p->extforce_wall_steepness * pow(aux, p->extforce_wall_powerindex);
+      return phi;
+    }
+    case FSPH_EFORCE_ORBIT: {
+      const double grav = p->gravitational_constant, a_sp = p->orbital_separation,
+                   m_ns = p->mass_neutron_star, m_wd = p->mass_white_dwarf;
+      const double m_t = m_ns + m_wd;
+      double term1 = sqrt(sq_(rp[0] - a_sp) + sq_(rp[1]) + sq_(rp[2]));
+      term1 = -grav * m_ns / term1;
+      double term2 = -0.5 * grav * m_t / cu_(a_sp);
+      term2 = term2 * (sq_(rp[0] - a_sp * m_ns / m_t) + sq_(rp[1]));
+      return term1 + term2;
+    }
+    case FSPH_EFORCE_POISON: return p->zero_potential_poison_value;
+  }
+  return 0.0;
+}
+
+static double ext_potential(const orc_ctx * c, const double * rp) {
+  double phi = 0.0;
+  for(int k = 0; k < FSPH_MAX_EFORCE && c->p.external_force[k] != FSPH_EFORCE_NONE; ++k)
+    phi += eforce_pot(c, c->p.external_force[k], rp);
+  return phi;
+}
+
+/* external_force::acceleration (eforce.h:325-334) */
+static void ext_acceleration(const orc_ctx * c, const double * rp, double * a) {
+  const fsph_params * p = &c->p;
+  const int D = c->D;
+  for(int i = 0; i < 3; ++i)
+    a[i] = 0.0;
+  for(int k = 0; k < FSPH_MAX_EFORCE && p->external_force[k] != FSPH_EFORCE_NONE; ++k) {
+    double t[3] = {0.0, 0.0, 0.0};
+    switch(p->external_force[k]) {
+      case FSPH_EFORCE_WALLS_X: t[0] = wall_acc(c, 0, rp); break;
+      case FSPH_EFORCE_WALLS_Y: t[1] = wall_acc(c, 1, rp); break;
+      case FSPH_EFORCE_WALLS_Z: t[2] = wall_acc(c, 2, rp); break;
+      case FSPH_EFORCE_SPHERICAL_WALL: sphwall_acc(c, rp, t); break;
+      case FSPH_EFORCE_SPHERICAL_DENSITY_SUPPORT: {
+        const double K0 = p->pressure_initial / pow(p->rho_initial, p->poly_gamma);
+        const double rho0 = prof_rho(c, 0.);
+        double r = radius3(D, rp);
+        const double x = r / p->sphere_radius;
+        if(x > 1e-12) {
+          double rho = p->rho_initial / rho0 * prof_rho(c, x);
+          double drhodr = p->rho_initial / (rho0 * p->sphere_radius) * prof_drho(c, x);
+          double a_r = (rho > 0) ? (K0 * p->poly_gamma * pow(rho, p->poly_gamma - 2) * drhodr) : 0;
+          for(int i = 0; i < D; ++i)
+            t[i] = a_r * rp[i] / r;
+        }
+        double w[3];
+        sphwall_acc(c, rp, w);
+        for(int i = 0; i < D; ++i)
+          t[i] = t[i] + w[i];
+        break;
+      }
+      case FSPH_EFORCE_GRAVITY:
+        if(D > 1)
+          t[1] = -p->gravity_acceleration_constant;
+        else
+          t[0] = -p->gravity_acceleration_constant;
+        break;
+      case FSPH_EFORCE_AIRFOIL: {
+        double x, y, cam, phi;
+        int inside = airfoil(c, rp, &x, &y, &cam, &phi);
+        if(inside && phi > 0.0) {
+          const double alpha = p->airfoil_attack_angle * ORC_PI / 180.0;
+          const double pw_n = p->extforce_wall_powerindex, pw_a = p->extforce_wall_steepness;
+          const double ac = p->airfoil_camber, th = p->airfoil_thickness, sz = p->airfoil_size;
+          double a0 = pw_n * pw_a * pow(phi, pw_n - 1) *
+                      (2. * (y - cam) * (-ac * ORC_PI / 2. * cos(ORC_PI / 2. * x)) -
+                       th * th * 2 * x * (sz * sz - 2 * x * x));
+          double a1 = pw_n * pw_a * pow(phi, pw_n - 1) * 2. * (y - cam);
+          t[0] = a0 * cos(alpha) - a1 * sin(alpha);
+          t[1] = a0 * sin(alpha) + a1 * cos(alpha);
+        }
+        break;
+      }
+      case FSPH_EFORCE_ORBIT: {
+        const double grav = p->gravitational_constant, a_sp = p->orbital_separation,
+                     m_ns = p->mass_neutron_star, m_wd = p->mass_white_dwarf;
+        const double m_t = m_ns + m_wd;
+        double temp = sq_(rp[0] - a_sp) + sq_(rp[1]) + sq_(rp[2]);
+        temp = cu_(temp);
+        temp = sqrt(temp);
+        double term1 = -grav * m_ns / temp;
+        t[0] += term1 * (rp[0] - a_sp);
+        t[1] += term1 * rp[1];
+        t[2] += term1 * rp[2];
+        double term2 = grav * m_t / cu_(a_sp);
+        t[0] += term2 * (rp[0] - a_sp * m_ns / m_t);
+        t[1] += term2 * rp[1];
+        break;
+      }
+      default: /* poison: no acceleration term */
+        continue;
+    }
+    for(int i = 0; i < D; ++i)
+      a[i] += t[i];
+  }
+}
+
+/* external_force::acceleration_drag (eforce.h:441-451) */
+static void drag_acc(const orc_ctx * c, const double * vel, double * acc) {
+  double v2 = vel[0] * vel[0];
+  for(int i = 1; i < c->D; ++i)
+    v2 += vel[i] * vel[i];
+  for(int i = 0; i < c->D; ++i)
+    acc[i] = 0.0 - (c->p.relaxation_beta + c->p.relaxation_gamma * v2) * vel[i];
+}
+
 static void * xalloc(size_t n) {
   void * p = calloc(n ? n : 1, 1);
   return p;
@@ -1283,7 +1537,7 @@ static int density_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
     for(int d = 0; d < D; ++d)
       vv += c->v[d][a] * c->v[d][a];
     double ekin = .5 * vv;
-    double eint = c->e[a] - ekin - 0.0;
+    double eint = c->e[a] - ekin - ext_potential(c, pa);
     if(!(eint > 0))
       return FSPH_ERR_NEG_ENERGY;
     c->u[a] = eint;
@@ -1444,8 +1698,10 @@ static void accel_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
     for(int d = 0; d < D; ++d)
       acc[d] += DiWa[d] * s;
   }
+  double ext[3] = {0.0, 0.0, 0.0};
+  ext_acceleration(c, pa, ext); /* acc_a += external_force::acceleration (:404) */
   for(int d = 0; d < D; ++d) {
-    c->a[d][a] = acc[d] + 0.0; /* + external_force::acceleration ("none") */
+    c->a[d][a] = acc[d] + ext[d];
     c->ga[d][a] = 0;
   }
   c->gpot[a] = 0;
@@ -1534,7 +1790,36 @@ static void dedt_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
   c->dedt[a] = dedt;
 }
 
-enum { PASS_DENSITY, PASS_VSIG, PASS_ACCEL, PASS_DUDT, PASS_DEDT, PASS_ALPHA };
+/* add_short_range_repulsion (default_physics.h:723-753) */
+static void repulsion_one(orc_ctx * c, int64_t a, const int64_t * nb, int64_t nn) {
+  const int D = c->D;
+  const double h_a = c->h[a];
+  const int64_t id_a = c->id[a];
+  double pa[3], acc_r[3] = {0.0, 0.0, 0.0};
+  getx(c, a, pa);
+  for(int64_t j = 0; j < nn; ++j) {
+    int64_t b = nb[j];
+    if(c->id[b] == id_a)
+      continue;
+    double dx[3], r = 0.0;
+    for(int d = 0; d < D; ++d) {
+      dx[d] = pa[d] - c->x[d][b];
+      r += dx[d] * dx[d];
+    }
+    double h_ab = .5 * (h_a + c->h[b]);
+    double r_ab = sqrt(r);
+    if(r_ab > h_ab * c->p.relaxation_repulsion_radius)
+      continue;
+    double m_b = c->m[b];
+    for(int d = 0; d < D; ++d)
+      acc_r[d] += m_b * dx[d] / (r_ab * r_ab * r_ab);
+  }
+  for(int d = 0; d < D; ++d)
+    c->a[d][a] = c->a[d][a] + acc_r[d] * c->p.relaxation_repulsion_gamma;
+}
+
+enum { PASS_DENSITY, PASS_VSIG, PASS_ACCEL, PASS_DUDT, PASS_DEDT, PASS_ALPHA,
+       PASS_REPULSION };
 
 /* apply_in_smoothinglength: walk every group and apply the pass to its
  * members (tree_topology.h:253-409). */
@@ -1569,6 +1854,7 @@ static int run_pass(orc_ctx * c, int pass) {
           case PASS_DUDT: dudt_one(c, a, s.nb[k], s.nbn[k]); break;
           case PASS_DEDT: dedt_one(c, a, s.nb[k], s.nbn[k]); break;
           case PASS_ALPHA: alpha_one(c, a, s.nb[k], s.nbn[k]); break;
+          case PASS_REPULSION: repulsion_one(c, a, s.nb[k], s.nbn[k]); break;
         }
       }
     }
@@ -1609,6 +1895,33 @@ int orc_initialize_alpha(orc_ctx * c) {
   return FSPH_OK;
 }
 int orc_dudt(orc_ctx * c) { return run_pass(c, PASS_DUDT); }
+int orc_add_short_range_repulsion(orc_ctx * c) { return run_pass(c, PASS_REPULSION); }
+
+/* add_drag_acceleration, add_drag_dedt, add_drag_dudt
+ * (default_physics.h:571-594, 699-708) */
+static int drag(orc_ctx * c, int which) {
+  for(int64_t i = 0; i < c->n; ++i) {
+    double vel[3] = {0.0, 0.0, 0.0}, acc[3];
+    for(int d = 0; d < c->D; ++d)
+      vel[d] = c->v[d][i];
+    drag_acc(c, vel, acc);
+    if(which == 0) {
+      for(int d = 0; d < c->D; ++d)
+        c->a[d][i] = c->a[d][i] + acc[d];
+    }
+    else {
+      double v_dot_a = 0.0;
+      for(int d = 0; d < c->D; ++d)
+        v_dot_a += vel[d] * acc[d];
+      double * f = which == 1 ? c->dedt : c->dudt;
+      f[i] = f[i] + v_dot_a;
+    }
+  }
+  return FSPH_OK;
+}
+int orc_add_drag_acceleration(orc_ctx * c) { return drag(c, 0); }
+int orc_add_drag_dedt(orc_ctx * c) { return drag(c, 1); }
+int orc_add_drag_dudt(orc_ctx * c) { return drag(c, 2); }
 int orc_dedt(orc_ctx * c) { return run_pass(c, PASS_DEDT); }
 
 /* ------------------------------------------------------- apply_all -- */
@@ -1639,8 +1952,9 @@ int orc_set_total_energy(orc_ctx * c) {
     double vv = 0;
     for(int d = 0; d < c->D; ++d)
       vv += c->v[d][i] * c->v[d][i];
-    double ekin = .5 * vv;
-    c->e[i] = ekin + c->u[i] + 0.0;
+    double ekin = .5 * vv, pos[3];
+    getx(c, i, pos);
+    c->e[i] = ekin + c->u[i] + ext_potential(c, pos);
   }
   return FSPH_OK;
 }
@@ -1702,7 +2016,9 @@ int orc_recompute_pressure_soundspeed_thermokinetic(orc_ctx * c) {
     for(int d = 0; d < c->D; ++d)
       vv += c->v[d][i] * c->v[d][i];
     double ekin = .5 * vv;
-    double eint = c->e[i] - ekin - 0.0;
+    double pos[3];
+    getx(c, i, pos);
+    double eint = c->e[i] - ekin - ext_potential(c, pos);
     if(!(eint > 0))
       return FSPH_ERR_NEG_ENERGY;
     c->u[i] = eint;
@@ -1742,12 +2058,18 @@ int orc_compute_dt(orc_ctx * c) {
       const double eint = c->u[i];
       if(!(eint > 0))
         return FSPH_ERR_NEG_ENERGY;
+      double pos[3];
+      getx(c, i, pos);
+      const double epot = ext_potential(c, pos);
       int it;
       for(it = 0; it < 20; ++it) {
         double gdv = 0;
         for(int d = 0; d < c->D; ++d)
           gdv += c->v[d][i] * c->ga[d][i];
-        double delta_epot = 0.0 - 0.0;
+        double p1[3] = {0.0, 0.0, 0.0};
+        for(int d = 0; d < c->D; ++d)
+          p1[d] = pos[d] + dtmin * c->v[d][i];
+        double delta_epot = ext_potential(c, p1) - epot;
         double delta_egrv = -dtmin * gdv;
         if(delta_epot + delta_egrv < eint * 0.5)
           break;
@@ -1908,10 +2230,12 @@ int orc_gravity_direct(orc_ctx * c, int64_t s0, int64_t s1) {
  * gravity standing in for the FMM). */
 int orc_step(orc_ctx * c) {
   const fsph_params * p = &c->p;
-  if(p->relaxation_steps != 0 ||
-     (p->sph_viscosity != FSPH_VISC_CONSTANT && p->sph_viscosity != FSPH_VISC_CULLEN))
+  if(p->sph_viscosity != FSPH_VISC_CONSTANT && p->sph_viscosity != FSPH_VISC_CULLEN)
     return FSPH_ERR_ARG;
   const int cullen = p->sph_viscosity == FSPH_VISC_CULLEN;
+  /* relaxation terms: hydro driver only (hydro/main_driver.cc:129-134,
+   * 150-165, 204-207, 219-234) */
+  const int relax = !p->enable_fmm && c->iteration < p->relaxation_steps;
   if(c->iteration == p->initial_iteration) {
     TRY(orc_update_iteration(c));
     TRY(orc_eos_init(c));
@@ -1925,6 +2249,10 @@ int orc_step(orc_ctx * c) {
       TRY(orc_compute_alpha(c));
     TRY(orc_reset_ghosts(c));
     TRY(orc_acceleration(c));
+    if(relax) {
+      TRY(orc_add_drag_acceleration(c));
+      TRY(orc_add_short_range_repulsion(c));
+    }
     if(p->enable_fmm)
       TRY(orc_gravity_direct(c, 0, c->n));
     if(p->thermokinetic_formulation && p->enable_fmm)
@@ -1937,10 +2265,14 @@ int orc_step(orc_ctx * c) {
       for(int m = 1; m <= p->pressure_updates_number; ++m) {
         if(p->thermokinetic_formulation) {
           TRY(orc_dedt(c));
+          if(relax)
+            TRY(orc_add_drag_dedt(c));
           TRY(orc_recompute_pressure_soundspeed_thermokinetic(c));
         }
         else {
           TRY(orc_dudt(c));
+          if(relax)
+            TRY(orc_add_drag_dudt(c));
           TRY(orc_recompute_pressure_soundspeed(c));
         }
         if(m < p->pressure_updates_number)
@@ -1964,6 +2296,10 @@ int orc_step(orc_ctx * c) {
       TRY(orc_compute_alpha(c));
     TRY(orc_reset_ghosts(c));
     TRY(orc_acceleration(c));
+    if(relax) {
+      TRY(orc_add_drag_acceleration(c));
+      TRY(orc_add_short_range_repulsion(c));
+    }
     if(p->enable_fmm)
       TRY(orc_gravity_direct(c, 0, c->n));
     TRY(orc_leapfrog_kick_v(c));
@@ -1972,10 +2308,14 @@ int orc_step(orc_ctx * c) {
       for(int m = 1; m <= p->pressure_updates_number; ++m) {
         if(p->thermokinetic_formulation) {
           TRY(orc_dedt(c));
+          if(relax)
+            TRY(orc_add_drag_dedt(c));
           TRY(orc_recompute_pressure_soundspeed_thermokinetic(c));
         }
         else {
           TRY(orc_dudt(c));
+          if(relax)
+            TRY(orc_add_drag_dudt(c));
           TRY(orc_recompute_pressure_soundspeed(c));
         }
         if(m < p->pressure_updates_number)

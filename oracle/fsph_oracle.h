@@ -48,6 +48,10 @@ int orc_initialize_alpha(orc_ctx * c);
 int orc_acceleration(orc_ctx * c);
 int orc_dudt(orc_ctx * c);
 int orc_dedt(orc_ctx * c);
+int orc_add_drag_acceleration(orc_ctx * c);
+int orc_add_short_range_repulsion(orc_ctx * c);
+int orc_add_drag_dedt(orc_ctx * c);
+int orc_add_drag_dudt(orc_ctx * c);
 int orc_eos_init(orc_ctx * c);
 int orc_set_total_energy(orc_ctx * c);
 int orc_save_velocityhalf(orc_ctx * c);

@@ -46,7 +46,9 @@ _FUNCS0 = ["update_iteration", "reset_ghosts", "density_pressure_soundspeed",
            "recompute_pressure_soundspeed_thermokinetic", "compute_dt",
            "set_adaptive_timestep", "compute_smoothinglength",
            "compute_average_smoothinglength", "check_nans", "check_negativity",
-           "advance_time", "step", "compute_alpha", "initialize_alpha"]
+           "advance_time", "step", "compute_alpha", "initialize_alpha",
+           "add_drag_acceleration", "add_short_range_repulsion", "add_drag_dedt",
+           "add_drag_dudt"]
 
 _libs = {}
 
@@ -79,12 +81,30 @@ def _load(path):
     return lib
 
 
+def _fresh_copy(path):
+    """Load a private copy of a library: new globals and function statics.
+
+    The reference's external-force functions keep their parameters in
+    function-local statics set at the first call (eforce.h:51-52, 71-72,
+    132-133, 156-157, 180, 191, 256, 286, 311), so one loaded copy serves
+    one set of external-force parameters."""
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp(prefix="fsph_ref_")
+    dst = os.path.join(d, os.path.basename(path))
+    shutil.copy(path, dst)
+    return _load(dst)
+
+
 class Oracle:
     def __init__(self, kind, params, threads=None):
         self.kind = kind
         self.params = params
         path = PORT_LIB if kind == "port" else ref_lib_path(params.dimension)
-        self.lib = _load(path)
+        if kind != "port" and params.forces():
+            self.lib = _fresh_copy(path)
+        else:
+            self.lib = _load(path)
         self.ctx = self.lib.orc_create(C.byref(params))
         if not self.ctx:
             raise FsphError(1, "orc_create")

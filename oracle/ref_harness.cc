@@ -16,7 +16,9 @@
 #include <mpi.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "params.h"
@@ -34,6 +36,19 @@ struct orc_ctx {
   bool built;
   std::vector<int64_t> order;
 };
+
+/* the external_force_type string whose select() gives the code list */
+static std::string external_force_string(const fsph_params * p) {
+  static const char * name[] = {"", "walls:x", "walls:y", "walls:z", "spherical wall",
+    "spherical density support", "gravity", "airfoil", "orbit", "poison"};
+  std::string out;
+  for(int k = 0; k < FSPH_MAX_EFORCE && p->external_force[k] != FSPH_EFORCE_NONE; ++k) {
+    if(!out.empty())
+      out += ",";
+    out += name[p->external_force[k]];
+  }
+  return out.empty() ? std::string("none") : out;
+}
 
 static void set_params(const fsph_params * p) {
   using namespace param;
@@ -77,10 +92,36 @@ static void set_params(const fsph_params * p) {
   _periodic_boundary_y = p->periodic_boundary_y;
   _periodic_boundary_z = p->periodic_boundary_z;
   fmm::gc = p->gravitational_constant;
+  _extforce_wall_powerindex = p->extforce_wall_powerindex;
+  _extforce_wall_steepness = p->extforce_wall_steepness;
+  _sphere_radius = p->sphere_radius;
+  _gravity_acceleration_constant = p->gravity_acceleration_constant;
+  _orbital_separation = p->orbital_separation;
+  _mass_neutron_star = p->mass_neutron_star;
+  _mass_white_dwarf = p->mass_white_dwarf;
+  _zero_potential_poison_value = p->zero_potential_poison_value;
+  _airfoil_size = p->airfoil_size;
+  _airfoil_thickness = p->airfoil_thickness;
+  _airfoil_camber = p->airfoil_camber;
+  _airfoil_anchor_x = p->airfoil_anchor_x;
+  _airfoil_anchor_y = p->airfoil_anchor_y;
+  _airfoil_attack_angle = p->airfoil_attack_angle;
+  _rho_initial = p->rho_initial;
+  _pressure_initial = p->pressure_initial;
+  _mesa_rim_width = p->mesa_rim_width;
+  _relaxation_beta = p->relaxation_beta;
+  _relaxation_gamma = p->relaxation_gamma;
+  _relaxation_repulsion_radius = p->relaxation_repulsion_radius;
+  _relaxation_repulsion_gamma = p->relaxation_repulsion_gamma;
+  {
+    static const char * prof[] = {"constant", "parabolic", "mesa"};
+    std::snprintf(_density_profile, STRING_MAXLEN, "%s",
+      prof[p->density_profile >= 0 && p->density_profile <= 2 ? p->density_profile : 0]);
+  }
   kernels::select();
   viscosity::select();
   eos::select();
-  external_force::select("none");
+  external_force::select(external_force_string(p));
   /* analysis::set_initial_time_iteration (analysis.h:221-249) */
   physics::iteration = initial_iteration;
   physics::totaltime = initial_time;
@@ -323,6 +364,15 @@ int orc_dedt(orc_ctx * c) {
   c->tree->traversal_sph(physics::compute_dedt);
   return FSPH_OK;
 }
+int orc_add_drag_acceleration(orc_ctx * c) {
+  return apply_all(c, physics::add_drag_acceleration);
+}
+int orc_add_short_range_repulsion(orc_ctx * c) {
+  c->tree->traversal_sph(physics::add_short_range_repulsion);
+  return FSPH_OK;
+}
+int orc_add_drag_dedt(orc_ctx * c) { return apply_all(c, physics::add_drag_dedt); }
+int orc_add_drag_dudt(orc_ctx * c) { return apply_all(c, physics::add_drag_dudt); }
 
 int orc_eos_init(orc_ctx * c) { return apply_all(c, eos::init); }
 int orc_set_total_energy(orc_ctx * c) {
@@ -390,6 +440,10 @@ int orc_step(orc_ctx * c) {
       orc_compute_alpha(c);
     orc_reset_ghosts(c);
     orc_acceleration(c);
+    if(physics::iteration < relaxation_steps) {
+      orc_add_drag_acceleration(c);
+      orc_add_short_range_repulsion(c);
+    }
     if(adaptive_timestep) {
       orc_compute_dt(c);
       orc_set_adaptive_timestep(c);
@@ -398,10 +452,14 @@ int orc_step(orc_ctx * c) {
       for(int m = 1; m <= pressure_updates_number; ++m) {
         if(thermokinetic_formulation) {
           orc_dedt(c);
+          if(physics::iteration < relaxation_steps)
+            orc_add_drag_dedt(c);
           orc_recompute_pressure_soundspeed_thermokinetic(c);
         }
         else {
           orc_dudt(c);
+          if(physics::iteration < relaxation_steps)
+            orc_add_drag_dudt(c);
           orc_recompute_pressure_soundspeed(c);
         }
         if(m < pressure_updates_number)
@@ -425,16 +483,24 @@ int orc_step(orc_ctx * c) {
       orc_compute_alpha(c);
     orc_reset_ghosts(c);
     orc_acceleration(c);
+    if(physics::iteration < relaxation_steps) {
+      orc_add_drag_acceleration(c);
+      orc_add_short_range_repulsion(c);
+    }
     orc_leapfrog_kick_v(c);
     orc_reset_ghosts(c);
     if(evolve_internal_energy) {
       for(int m = 1; m <= pressure_updates_number; ++m) {
         if(thermokinetic_formulation) {
           orc_dedt(c);
+          if(physics::iteration < relaxation_steps)
+            orc_add_drag_dedt(c);
           orc_recompute_pressure_soundspeed_thermokinetic(c);
         }
         else {
           orc_dudt(c);
+          if(physics::iteration < relaxation_steps)
+            orc_add_drag_dudt(c);
           orc_recompute_pressure_soundspeed(c);
         }
         if(m < pressure_updates_number)

@@ -65,6 +65,10 @@ def cases():
     # the other equations of state
     for name, seed, s, p in eos_cases():
         yield name, setups.shuffled(s, seed), p, 2
+    # external forces and particle relaxation
+    for k, name in enumerate(setups.EXTERNAL_FORCE_PROBLEMS):
+        s, p = setups.external_force_problem(name)
+        yield "eforce_" + name, setups.shuffled(s, 20 + k), p, 2
     # periodic boundaries: copies regenerated at every update_iteration;
     # a few particles start outside the box and are teleported back
     s, p, m = setups.kh2d(40)

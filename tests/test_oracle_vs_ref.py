@@ -221,3 +221,33 @@ def test_other_equations_of_state(oracle_port, case):
             assert np.array_equal(a[f], b[f]), f
     last = res["port"][-1][0]
     assert np.isfinite(last["ax"]).all() and np.abs(last["ax"]).max() > 0
+
+
+@pytest.mark.parametrize("case", __import__("flecsph_gb300.setups", fromlist=["x"]).EXTERNAL_FORCE_PROBLEMS)
+def test_external_forces_and_relaxation(oracle_port, case):
+    """Every external force of eforce.h (walls, spherical wall, density
+    support with the parabolic and mesa profiles, uniform gravity, airfoil,
+    orbit, potential shift) and the relaxation drag and repulsion, through
+    three driver iterations, bit-exact against the compiled reference."""
+    from flecsph_gb300 import setups
+    s, p = setups.external_force_problem(case)
+    s = setups.shuffled(s, 91)
+    if not oracle_port.have_ref(p.dimension):
+        if not oracle_port.build_ref():
+            pytest.skip("reference sources not present")
+    res = {}
+    for kind in ("reference", "port"):
+        o = oracle_port.Oracle(kind, p)
+        o.upload(s)
+        steps = []
+        for _ in range(3):
+            o.step()
+            steps.append((o.download(), o.time()))
+        res[kind] = steps
+        o.close()
+    for k, ((a, ta), (b, tb)) in enumerate(zip(res["reference"], res["port"])):
+        assert ta == tb, k
+        for f in DOUBLE_FIELDS:
+            assert np.array_equal(a[f], b[f]), (k, f)
+    last = res["port"][-1][0]
+    assert np.isfinite(last["ax"]).all()
