@@ -18,6 +18,16 @@ __device__ __forceinline__ double ord_dec_m(unsigned long long u) {
 // ------------------------------------------------------------- packing --
 __global__ void k_pack_pos(Particles P, int dim,
   const unsigned long long * rbits, Packed K) {
+  // any monotone mapping shared by all particles will do: multiply by the
+  // reciprocal, computed once per block (FP64 division is costly here)
+  __shared__ double s_lo[3], s_inv[3];
+  if(threadIdx.x < dim) {
+    const int d = threadIdx.x;
+    const double lo = ord_dec_m(rbits[d]), hi = ord_dec_m(rbits[3 + d]);
+    s_lo[d] = lo;
+    s_inv[d] = 2147483648.0 / (hi - lo);
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i < 3 && i < dim) {
     double ext = ord_dec_m(rbits[3 + i]) - ord_dec_m(rbits[i]);
@@ -27,10 +37,7 @@ __global__ void k_pack_pos(Particles P, int dim,
     return;
   int q[3] = {0, 0, 0};
   for(int d = 0; d < dim; ++d) {
-    // any monotone mapping shared by all particles will do: multiply by the
-    // reciprocal instead of dividing (FP64 division is costly on this part)
-    double lo = ord_dec_m(rbits[d]), hi = ord_dec_m(rbits[3 + d]);
-    double t = (P.f[F_X + d][i] - lo) * (2147483648.0 / (hi - lo));
+    double t = (P.f[F_X + d][i] - s_lo[d]) * s_inv[d];
     t = fmin(fmax(t, 0.0), 2147483647.0);
     q[d] = __double2int_rn(t);
   }

@@ -33,6 +33,11 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a,
+  unsigned long long b) {
+  return b < a ? b : a;
+}
+
 // ---------------------------------------------------------------- range --
 // body_system::mpi_compute_range (mpisph/bodies_system.h:231-268): the
 // bounding box of [x - h, x + h] over all particles, initialised from the
@@ -50,29 +55,34 @@ __global__ void k_range_init(Particles P, int dim, unsigned long long * bits) {
   }
 }
 
+// The comparisons run on the ordered integer encodings (the integer pipe);
+// only x + h and x - h use the FP64 pipe, which is the bound of this
+// kernel on a part with GB300's FP64 rate.
 __global__ void __launch_bounds__(256) k_range_reduce(Particles P, int dim,
   unsigned long long * bits) {
-  double lo[3] = {1e308, 1e308, 1e308}, hi[3] = {-1e308, -1e308, -1e308};
-  double hmn = 1e308, hmx = -1e308;
+  // v[k]: minima of the encodings of lo[0..2], h and of the complemented
+  // encodings of hi[0..2], h (so that every slot is a minimum)
+  unsigned long long v[8];
+  for(int k = 0; k < 8; ++k)
+    v[k] = ~0ull;
   const double * H = P.f[F_H];
   for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
       i += gridDim.x * blockDim.x) {
-    double h = H[i];
-    hmn = fmin(hmn, h);
-    hmx = fmax(hmx, h);
+    const double h = H[i];
+    const unsigned long long eh = ord_enc(h);
+    v[6] = umin64(v[6], eh);
+    v[7] = umin64(v[7], ~eh);
     for(int d = 0; d < dim; ++d) {
-      double x = P.f[F_X + d][i];
-      double a = x + h, b = x - h;
-      hi[d] = a > hi[d] ? a : hi[d];
-      lo[d] = b < lo[d] ? b : lo[d];
+      const double x = P.f[F_X + d][i];
+      v[d] = umin64(v[d], ord_enc(x - h));
+      v[3 + d] = umin64(v[3 + d], ~ord_enc(x + h));
     }
   }
   // warp, then block, then one atomic per block and quantity
-  __shared__ double red[8][8];
-  double v[8] = {lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2], hmn, -hmx};
+  __shared__ unsigned long long red[8][8];
   for(int k = 0; k < 8; ++k)
     for(int o = 16; o; o >>= 1)
-      v[k] = fmin(v[k], __shfl_xor_sync(FULL, v[k], o));
+      v[k] = umin64(v[k], __shfl_xor_sync(FULL, v[k], o));
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if(lane == 0)
     for(int k = 0; k < 8; ++k)
@@ -80,19 +90,19 @@ __global__ void __launch_bounds__(256) k_range_reduce(Particles P, int dim,
   __syncthreads();
   if(threadIdx.x < 8) {
     const int k = threadIdx.x;
-    double m = red[0][k];
+    unsigned long long m = red[0][k];
     for(int q = 1; q < (int)(blockDim.x >> 5); ++q)
-      m = fmin(m, red[q][k]);
+      m = umin64(m, red[q][k]);
     if(k < 3) {
-      if(k < dim) atomicMin(&bits[k], ord_enc(m));
+      if(k < dim) atomicMin(&bits[k], m);
     }
     else if(k < 6) {
-      if(k - 3 < dim) atomicMax(&bits[k], ord_enc(-m));
+      if(k - 3 < dim) atomicMax(&bits[k], ~m);
     }
     else if(k == 6)
-      atomicMin(&bits[6], ord_enc(m));
+      atomicMin(&bits[6], m);
     else
-      atomicMax(&bits[7], ord_enc(-m));
+      atomicMax(&bits[7], ~m);
   }
 }
 
@@ -120,23 +130,36 @@ __device__ __forceinline__ unsigned long long spread2(unsigned long long x) {
 
 __global__ void k_keys(Particles P, int dim, const unsigned long long * bits,
   unsigned long long * keys, int * idx) {
+  // the range and its reciprocal scaled by 2^md, once per block (FP64
+  // division is costly at this part's FP64 rate)
+  __shared__ double s_mn[3], s_scale[3], s_rs[3];
+  const int md = 63 / dim;
+  const double mult = (double)(1ull << md);
+  if(threadIdx.x < dim) {
+    const int d = threadIdx.x;
+    const double mn = ord_dec(bits[d]);
+    const double scale = ord_dec(bits[3 + d]) - mn;
+    s_mn[d] = mn;
+    s_scale[d] = scale;
+    s_rs[d] = (1.0 / scale) * mult;
+  }
+  __syncthreads();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
-  const int md = 63 / dim;
   const unsigned long long maxv = (1ull << md) - 1;
-  const double mult = (double)(1ull << md);
   unsigned long long c[3] = {0, 0, 0};
   for(int d = 0; d < dim; ++d) {
-    const double mn = ord_dec(bits[d]);
-    const double mx = ord_dec(bits[3 + d]);
-    const double scale = mx - mn;
+    const double mn = s_mn[d];
+    const double scale = s_scale[d];
     const double t = P.f[F_X + d][i] - mn;
     // The reference quantises fl(t / scale) * 2^md (a power of two, exact).
     // t * (1 / scale) can differ from fl(t / scale) by an ulp, which moves
     // the integer part only when the scaled value lies within ~7e-7 of an
     // integer (2D: 2^31 scale); there the correctly rounded division decides.
-    double q = t * (1.0 / scale) * mult;
+    // Scaling by 2^md commutes with rounding, so t * ((1 / scale) * 2^md)
+    // equals fl(t * (1 / scale)) * 2^md.
+    double q = t * s_rs[d];
     const double fq = floor(q);
     if(q - fq < 1e-5 || q - fq > 1.0 - 1e-5)
       q = t / scale * mult;
