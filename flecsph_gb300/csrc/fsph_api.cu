@@ -532,6 +532,13 @@ void fsph_destroy(fsph_ctx * c) {
   for(auto & e : c->marks)
     if(e)
       cudaEventDestroy(e);
+  if(c->io.stream) {
+    cudaStreamSynchronize(c->io.stream);
+    for(auto & e : c->io.ev)
+      if(e)
+        cudaEventDestroy(e);
+    cudaStreamDestroy(c->io.stream);
+  }
   if(c->stream)
     cudaStreamDestroy(c->stream);
   delete c;
@@ -782,6 +789,11 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
     CK(radix_sort_pairs(L, c->skeys, c->svals, c->skeys_tmp, c->svals_tmp, n,
       c->hist, 0));
     CK(launch_check_duplicates(L, c->skeys, n, c->d_status));
+    if(c->io.h2d_pending) {
+      // fsph_step_io: input fields copied on the copy stream land first
+      CK(cudaStreamWaitEvent(c->stream, c->io.ev[0], 0));
+      c->io.h2d_pending = false;
+    }
     CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys));
     Particles t = c->P;
     c->P = c->Palt;
@@ -1063,6 +1075,153 @@ fsph_status fsph_gravitation(fsph_ctx * c) {
 // One iteration of the driver loop (app/drivers/hydro/main_driver.cc:98-279;
 // newtonian/main_driver.cc:103-298 when enable_fmm).  Elementwise steps that
 // the reference runs back to back are fused; every fusion only combines
+// ---- fsph_step_io ---------------------------------------------------------
+enum { IO_UPDATE = 1, IO_DENSITY = 2, IO_ACCEL = 3, IO_END = 4 };
+
+static double ** view_fields(const fsph_soa_view * v, double ** f) {
+  double * const src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
+    v->vhy, v->vhz, v->ax, v->ay, v->az, v->gax, v->gay, v->gaz, v->gpot, v->m,
+    v->h, v->rho, v->P, v->cs, v->u, v->e, v->dudt, v->dedt, v->K, v->alpha,
+    v->vsig, v->dt, v->divv, v->ddivvdt, v->Ye};
+  for(int k = 0; k < NF; ++k)
+    f[k] = src[k];
+  return f;
+}
+
+// The stage of a regular iteration of fsph_step after which field k is not
+// written again: the drift and the permute of update_iteration, the density
+// pass (and the alpha pass), the acceleration (with gravity, relaxation and
+// the velocity kick), and the energy passes, h and dt updates at the end.
+static int io_final_stage(const fsph_ctx * c, int k) {
+  const fsph_params & p = c->p;
+  const bool thermo = p.thermokinetic_formulation, evolve = p.evolve_internal_energy;
+  const bool cullen = c->pp.cullen;
+  switch(k) {
+    case F_X: case F_Y: case F_Z: case F_VHX: case F_VHY: case F_VHZ:
+    case F_M: case F_K: case F_YE:
+      return IO_UPDATE;
+    case F_H:
+      return (p.sph_variable_h || p.sph_update_uniform_h) ? IO_END : IO_UPDATE;
+    case F_DUDT:
+      return (evolve && !thermo) ? IO_END : IO_UPDATE;
+    case F_DEDT:
+      return (evolve && thermo) ? IO_END : IO_UPDATE;
+    case F_E:
+      return (evolve && thermo) ? IO_END : IO_UPDATE;
+    case F_U:
+      return evolve ? IO_END : IO_UPDATE;
+    case F_ALPHA:
+      return cullen ? IO_ACCEL : IO_UPDATE;
+    case F_DIVV: case F_DDIVVDT:
+      return cullen ? IO_DENSITY : IO_UPDATE;
+    case F_RHO:
+      return IO_DENSITY;
+    case F_AX: case F_AY: case F_AZ: case F_GAX: case F_GAY: case F_GAZ:
+    case F_GPOT: case F_VX: case F_VY: case F_VZ: case F_VSIG:
+      return IO_ACCEL;
+    default:  // P, c_s, dt
+      return IO_END;
+  }
+}
+
+// Send the output fields that are final at `stage` on the copy stream, after
+// the work enqueued so far on the context's stream.
+static fsph_status io_stage(fsph_ctx * c, int stage) {
+  if(!c->io.active)
+    return FSPH_OK;
+  CK(cudaEventRecord(c->io.ev[stage], c->stream));
+  CK(cudaStreamWaitEvent(c->io.stream, c->io.ev[stage], 0));
+  double * dst[NF];
+  view_fields(&c->io.out, dst);
+  const size_t bytes = sizeof(double) * (size_t)c->n;
+  for(int k = 0; k < NF; ++k) {
+    if(!dst[k] || c->io.sent[k] || io_final_stage(c, k) > stage)
+      continue;
+    if(c->p.dimension == 2 &&
+       (k == F_Z || k == F_VZ || k == F_VHZ || k == F_AZ || k == F_GAZ))
+      continue;
+    CK(cudaMemcpyAsync(dst[k], c->P.f[k], bytes, cudaMemcpyDeviceToHost, c->io.stream));
+    c->io.sent[k] = true;
+  }
+  if(c->io.out.id && !c->io.sent[NF]) {
+    CK(cudaMemcpyAsync(c->io.out.id, c->P.id, sizeof(long long) * c->n,
+      cudaMemcpyDeviceToHost, c->io.stream));
+    c->io.sent[NF] = true;
+  }
+  if(c->io.out.key && !c->io.sent[NF + 1]) {
+    CK(cudaMemcpyAsync(c->io.out.key, c->P.key, sizeof(unsigned long long) * c->n,
+      cudaMemcpyDeviceToHost, c->io.stream));
+    c->io.sent[NF + 1] = true;
+  }
+  return FSPH_OK;
+}
+
+fsph_status fsph_step_io(fsph_ctx * c, const fsph_soa_view * in, fsph_soa_view * out) {
+  if(!c || !c->uploaded || !out || (in && in->n != c->n))
+    return FSPH_ERR_ARG;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  const bool overlap = c->iteration != c->p.initial_iteration && !c->periodic &&
+                       out->n == c->n;
+  if(!overlap) {
+    if(in)
+      TRY(fsph_upload_fields(c, in));
+    TRY(fsph_step(c));
+    return fsph_download(c, out);
+  }
+  if(!c->io.stream) {
+    CK(cudaStreamCreateWithFlags(&c->io.stream, cudaStreamNonBlocking));
+    for(int k = 0; k < 6; ++k)
+      CK(cudaEventCreateWithFlags(&c->io.ev[k], cudaEventDisableTiming));
+  }
+  if(in) {
+    // fields the kick, drift, range, keys and sort read or write go in
+    // first on the context's stream, the rest on the copy stream, which the
+    // permute waits for
+    double * src[NF];
+    view_fields(in, src);
+    const size_t bytes = sizeof(double) * (size_t)c->n;
+    bool late_any = false;
+    CK(cudaEventRecord(c->io.ev[5], c->stream));
+    CK(cudaStreamWaitEvent(c->io.stream, c->io.ev[5], 0));
+    for(int k = 0; k < NF; ++k) {
+      if(!src[k])
+        continue;
+      const bool early = k <= F_GAZ || k == F_H || k == F_U || k == F_E ||
+                         k == F_DUDT || k == F_DEDT;
+      CK(cudaMemcpyAsync(c->P.f[k], src[k], bytes, cudaMemcpyHostToDevice,
+        early ? c->stream : c->io.stream));
+      late_any = late_any || !early;
+    }
+    if(in->id)
+      CK(cudaMemcpyAsync(c->P.id, in->id, sizeof(long long) * c->n,
+        cudaMemcpyHostToDevice, c->stream));
+    if(late_any) {
+      CK(cudaEventRecord(c->io.ev[0], c->io.stream));
+      c->io.h2d_pending = true;
+    }
+  }
+  c->io.active = true;
+  c->io.out = *out;
+  for(int k = 0; k < NF + 2; ++k)
+    c->io.sent[k] = false;
+  s = fsph_step(c);
+  if(!s)
+    s = io_stage(c, IO_END);
+  c->io.active = false;
+  if(c->io.h2d_pending) {  // the step stopped before the permute
+    cudaStreamWaitEvent(c->stream, c->io.ev[0], 0);
+    c->io.h2d_pending = false;
+  }
+  // the context's stream continues after the copies
+  CK(cudaEventRecord(c->io.ev[4], c->io.stream));
+  CK(cudaStreamWaitEvent(c->stream, c->io.ev[4], 0));
+  if(s)
+    return s;
+  return fsph_sync(c);
+}
+
 // per-particle updates whose inputs the fused pass does not read from
 // neighbours.
 fsph_status fsph_step(fsph_ctx * c) {
@@ -1124,9 +1283,11 @@ fsph_status fsph_step(fsph_ctx * c) {
     TRY(elem(c, !evolve ? OP_KICK_DRIFT_NONE : (thermo ? OP_KICK_DRIFT_E : OP_KICK_DRIFT_U),
       FSPH_TIMER_INTEGRATE));
     TRY(fsph_update_iteration(c));
+    TRY(io_stage(c, IO_UPDATE));
     TRY(density_impl(c, !c->mixed));
     if(cullen)
       TRY(fsph_compute_alpha(c));
+    TRY(io_stage(c, IO_DENSITY));
     if(grav) {
       // newtonian/main_driver.cc:217-227: gravity between the hydro
       // acceleration and the velocity kick
@@ -1142,6 +1303,7 @@ fsph_status fsph_step(fsph_ctx * c) {
     }
     else
       TRY(accel_impl(c, 1, c->mixed));
+    TRY(io_stage(c, IO_ACCEL));
     if(evolve) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         const bool lastp = m == p.pressure_updates_number;

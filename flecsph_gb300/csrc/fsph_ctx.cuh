@@ -58,6 +58,16 @@ struct fsph_ctx {
   std::string last_error;
   std::vector<void *> allocs;
   cudaEvent_t marks[64] = {};
+  // fsph_step_io: a copy stream, the output view of the step in progress
+  // and which of its fields are already on their way to the host
+  struct Io {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    bool active = false;
+    bool h2d_pending = false;  // late input fields on the copy stream
+    fsph_soa_view out{};
+    bool sent[fsph::NF + 2] = {};  // NF fields, then id, key
+  } io;
 
   fsph::Launch L() { return fsph::Launch{stream, &launches}; }
 };

@@ -93,6 +93,7 @@ def library():
     lib.fsph_particle_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
                                         C.POINTER(C.c_int64)]
     lib.fsph_upload_fields.argtypes = [C.c_void_p, C.POINTER(SoAView)]
+    lib.fsph_step_io.argtypes = [C.c_void_p, C.POINTER(SoAView), C.POINTER(SoAView)]
     lib.fsph_host_register.argtypes = [C.c_void_p, C.c_int64]
     lib.fsph_host_unregister.argtypes = [C.c_void_p]
     lib.fsph_mark.argtypes = [C.c_void_p, C.c_int32]
@@ -192,6 +193,13 @@ class BodySystem:
 
     def download_into(self, view):
         self._check(self.lib.fsph_download(self.ctx, C.byref(view)), "download")
+
+    def step_io(self, vin, vout):
+        """One iteration with its host copies (fsph_step_io): the non-NULL
+        fields of vin go in, those of vout come back; copies overlap the
+        step in regular iterations."""
+        self._check(self.lib.fsph_step_io(self.ctx, C.byref(vin) if vin is not None else None,
+                                          C.byref(vout)), "step_io")
 
     def mark(self, slot):
         self._check(self.lib.fsph_mark(self.ctx, slot), "mark")

@@ -304,6 +304,19 @@ fsph_status fsph_set_time(fsph_ctx * ctx, double dt, double totaltime,
 /* Range [min0,min1,(min2),max0,max1,(max2)] of the last update_iteration. */
 fsph_status fsph_get_range(fsph_ctx * ctx, double * range);
 
+/* One iteration with its host copies: the non-NULL fields of `in` (host,
+ * current particle order, as fsph_upload_fields) go in, the step runs, and
+ * the non-NULL fields of `out` (host, n = the particle count) come back in
+ * the order fsph_download gives.  The result equals fsph_upload_fields +
+ * fsph_step + fsph_download; in a regular (not the initial) iteration
+ * without periodic copies the copies overlap the step: input fields the
+ * kick, drift and key sort do not touch go in on a second stream while those
+ * run, and each output field goes out as soon as the step has written it
+ * for the last time.  Synchronous: returns after `out` is complete, with the
+ * step's device status. */
+fsph_status fsph_step_io(fsph_ctx * ctx, const fsph_soa_view * in,
+  fsph_soa_view * out);
+
 /* -- body_system --------------------------------------------------------- */
 fsph_status fsph_update_iteration(fsph_ctx * ctx);
 fsph_status fsph_reset_ghosts(fsph_ctx * ctx);
