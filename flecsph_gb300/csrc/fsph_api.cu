@@ -794,7 +794,7 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
       CK(cudaStreamWaitEvent(c->stream, c->io.ev[0], 0));
       c->io.h2d_pending = false;
     }
-    CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys));
+    CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys, c->permute_skip));
     Particles t = c->P;
     c->P = c->Palt;
     c->Palt = t;
@@ -1282,7 +1282,24 @@ fsph_status fsph_step(fsph_ctx * c) {
   else {
     TRY(elem(c, !evolve ? OP_KICK_DRIFT_NONE : (thermo ? OP_KICK_DRIFT_E : OP_KICK_DRIFT_U),
       FSPH_TIMER_INTEGRATE));
-    TRY(fsph_update_iteration(c));
+    // fields the rest of the iteration writes before reading stay behind
+    // in the permute
+    unsigned skip = (1u << F_AX) | (1u << F_AY) | (1u << F_GAX) | (1u << F_GAY) |
+                    (1u << F_GPOT) | (1u << F_RHO) | (1u << F_VSIG);
+    if(p.dimension == 3)
+      skip |= (1u << F_AZ) | (1u << F_GAZ);
+    if(p.adaptive_timestep)
+      skip |= 1u << F_DT;
+    if(p.eos_type != FSPH_EOS_NO_EOS)
+      skip |= 1u << F_P;
+    if(evolve && thermo)
+      skip |= (1u << F_DEDT) | (1u << F_U);
+    if(evolve && !thermo)
+      skip |= 1u << F_DUDT;
+    c->permute_skip = skip;
+    const fsph_status us = fsph_update_iteration(c);
+    c->permute_skip = 0;
+    TRY(us);
     TRY(io_stage(c, IO_UPDATE));
     TRY(density_impl(c, !c->mixed));
     if(cullen)

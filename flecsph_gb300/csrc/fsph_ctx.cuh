@@ -45,6 +45,7 @@ struct fsph_ctx {
   fsph::DevStatus * d_status = nullptr;
   double * d_cons = nullptr;
   int64_t iteration = 0;
+  unsigned permute_skip = 0;  // fields the next permute may leave behind
   bool tree_ok = false;
   bool uploaded = false;
   long long launches = 0;

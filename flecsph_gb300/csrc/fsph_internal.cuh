@@ -173,7 +173,8 @@ size_t radix_hist_entries(int n);
 cudaError_t launch_check_duplicates(const Launch & L,
   const unsigned long long * keys, int n, DevStatus * st);
 cudaError_t launch_permute(const Launch & L, const Particles & src,
-  const Particles & dst, const int * perm, const unsigned long long * keys);
+  const Particles & dst, const int * perm, const unsigned long long * keys,
+  unsigned skip);
 struct Packed;
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,

@@ -311,7 +311,7 @@ cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
     src.n = (int)nreal;
     Particles dst = Palt;
     dst.n = (int)nreal;
-    if((e = launch_permute(L, src, dst, S.perm, P.key)))
+    if((e = launch_permute(L, src, dst, S.perm, P.key, 0u)))
       return e;
     Particles t = P;
     P = Palt;

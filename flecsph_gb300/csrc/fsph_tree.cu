@@ -209,10 +209,17 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(
   sh[threadIdx.x] = 0;
   __syncthreads();
   int base = blockIdx.x * RS_TILE;
+  unsigned long long kreg[RS_ITEMS];
+#pragma unroll
   for(int r = 0; r < RS_ITEMS; ++r) {
-    int i = base + r * RS_THREADS + threadIdx.x;
+    const int i = base + r * RS_THREADS + threadIdx.x;
+    kreg[r] = i < n ? keys[i] : 0ull;
+  }
+#pragma unroll
+  for(int r = 0; r < RS_ITEMS; ++r) {
+    const int i = base + r * RS_THREADS + threadIdx.x;
     if(i < n)
-      atomicAdd(&sh[(keys[i] >> shift) & 255], 1u);
+      atomicAdd(&sh[(kreg[r] >> shift) & 255], 1u);
   }
   __syncthreads();
   hist[threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
@@ -287,13 +294,24 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
   running[t] = 0;
   for(int k = 0; k < RS_THREADS / 32; ++k)
     wcnt[k][t] = 0;
+  // the tile's keys and values into registers first: all loads in flight
+  // at once instead of one dependent load per ranking round
+  const int tile = blockIdx.x * RS_TILE;
+  unsigned long long kreg[RS_ITEMS];
+  int vreg[RS_ITEMS];
+#pragma unroll
+  for(int r = 0; r < RS_ITEMS; ++r) {
+    const int i = tile + r * RS_THREADS + t;
+    kreg[r] = i < n ? kin[i] : 0ull;
+    vreg[r] = i < n ? vin[i] : 0;
+  }
   __syncthreads();
   const unsigned lt = lanemask_lt();
-  const int tile = blockIdx.x * RS_TILE;
+#pragma unroll
   for(int r = 0; r < RS_ITEMS; ++r) {
     int i = tile + r * RS_THREADS + t;
     bool valid = i < n;
-    unsigned long long key = valid ? kin[i] : 0ull;
+    unsigned long long key = kreg[r];
     int digit = valid ? (int)((key >> shift) & 255) : 256;
     unsigned mask = __match_any_sync(FULL, digit);
     int rank = __popc(mask & lt);
@@ -307,7 +325,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
         pre += wcnt[k][digit];
       unsigned pos = base[digit] + pre + rank;
       kout[pos] = key;
-      vout[pos] = vin[i];
+      vout[pos] = vreg[r];
     }
     __syncthreads();
     unsigned s = 0;
@@ -361,22 +379,26 @@ cudaError_t launch_check_duplicates(const Launch & L,
   return cudaGetLastError();
 }
 
+// Fields whose bit is set in `skip` are left behind: the caller overwrites
+// them before anything reads them.
 __global__ void k_permute(Particles src, Particles dst, const int * perm,
-  const unsigned long long * keys) {
+  const unsigned long long * keys, unsigned skip) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= src.n)
     return;
   int p = perm[i];
 #pragma unroll
   for(int k = 0; k < NF; ++k)
-    dst.f[k][i] = src.f[k][p];
+    if(!((skip >> k) & 1u))
+      dst.f[k][i] = src.f[k][p];
   dst.id[i] = src.id[p];
   dst.key[i] = keys[i];
 }
 
 cudaError_t launch_permute(const Launch & L, const Particles & src,
-  const Particles & dst, const int * perm, const unsigned long long * keys) {
-  k_permute<<<(src.n + 255) / 256, 256, 0, L.stream>>>(src, dst, perm, keys);
+  const Particles & dst, const int * perm, const unsigned long long * keys,
+  unsigned skip) {
+  k_permute<<<(src.n + 255) / 256, 256, 0, L.stream>>>(src, dst, perm, keys, skip);
   *L.counter += 1;
   return cudaGetLastError();
 }
