@@ -260,6 +260,16 @@ __device__ __forceinline__ double ext_potential(const PhysParams & pp,
   return phi;
 }
 
+// The potential at particle i's position; no loads without external forces.
+template<int D>
+__device__ __forceinline__ double ext_potential_of(const PhysParams & pp,
+  double * const * f, int i) {
+  if(pp.n_eforce == 0)
+    return 0.0;
+  const double pos[3] = {f[F_X][i], f[F_Y][i], D == 3 ? f[F_Z][i] : 0.0};
+  return ext_potential<D>(pp, pos);
+}
+
 // external_force::acceleration (eforce.h:325-334): the sum of the terms,
 // starting from zero
 template<int D>

@@ -29,8 +29,7 @@ __device__ __forceinline__ double recover_u(const Particles & P,
   for(int d = 0; d < D; ++d)
     vv += P.f[F_VX + d][i] * P.f[F_VX + d][i];
   double ekin = .5 * vv;
-  const double pos[3] = {P.f[F_X][i], P.f[F_Y][i], D == 3 ? P.f[F_Z][i] : 0.0};
-  double eint = P.f[F_E][i] - ekin - ext_potential<D>(pp, pos);
+  double eint = P.f[F_E][i] - ekin - ext_potential_of<D>(pp, P.f, i);
   if(!(eint > 0))
     raise_status(st, FSPH_ERR_NEG_ENERGY, i);
   return eint;
@@ -67,8 +66,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_elem(Particles P,
       for(int d = 0; d < D; ++d)
         vv += f[F_VX + d][i] * f[F_VX + d][i];
       double ekin = .5 * vv;
-      const double pos[3] = {f[F_X][i], f[F_Y][i], D == 3 ? f[F_Z][i] : 0.0};
-      f[F_E][i] = ekin + f[F_U][i] + ext_potential<D>(pp, pos);
+      f[F_E][i] = ekin + f[F_U][i] + ext_potential_of<D>(pp, f, i);
       break;
     }
     case OP_SAVE_VHALF:  // integration.h:52-55
@@ -226,10 +224,12 @@ __device__ __forceinline__ bool bits_negative(double x) {  // x < 0, not -0, not
 template<int D, bool CHECKS, bool F32>
 __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
   PhysParams pp, DevTime * tm, DevStatus * st) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // grid-stride: one atomic per block of a grid sized to the machine
   double dtmin = 1e24;
-  if(i < P.n) {
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
+      i += gridDim.x * blockDim.x) {
     double ** f = P.f;
+    double dtp = 1e24;
     if(CHECKS) {
       bool bad = false;
       for(int d = 0; d < D; ++d)
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
       const float dt_v = dx / (sqrtf(vn) + tiny);
       const float dt_a = sqrtf(dx / (sqrtf(acc) + tiny));
       const float dt_c = dx / (tiny + (float)f[F_VSIG][i] * (1.f + 0.6f * (float)pp.alpha));
-      dtmin = (double)((float)pp.cfl * fminf(fminf(dt_v, dt_a), dt_c));
+      dtp = (double)((float)pp.cfl * fminf(fminf(dt_v, dt_a), dt_c));
     }
     else {
       const double tiny = 1e-24, mc = 0.6;
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
       acc = sqrt(acc);
       const double dt_a = sqrt(dx / (acc + tiny));
       const double dt_c = dx / (tiny + f[F_VSIG][i] * (1 + mc * pp.alpha));
-      dtmin = pp.cfl * dmin_(dmin_(dt_v, dt_a), dt_c);
+      dtp = pp.cfl * dmin_(dmin_(dt_v, dt_a), dt_c);
     }
     if(pp.evolve_u && pp.thermokinetic) {
       const double eint = f[F_U][i];
@@ -295,18 +295,19 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_compute_dt(Particles P,
         for(it = 0; it < 20; ++it) {
           double p1[3] = {0.0, 0.0, 0.0};
           for(int d = 0; d < D; ++d)
-            p1[d] = pos[d] + dtmin * f[F_VX + d][i];
+            p1[d] = pos[d] + dtp * f[F_VX + d][i];
           double delta_epot = ext_potential<D>(pp, p1) - epot;
-          double delta_egrv = -dtmin * gdv;
+          double delta_egrv = -dtp * gdv;
           if(delta_epot + delta_egrv < eint * 0.5)
             break;
-          dtmin *= 0.25;
+          dtp *= 0.25;
         }
         if(it >= 20)
           raise_status(st, FSPH_ERR_DT, i);
       }
     }
-    f[F_DT][i] = dtmin;
+    f[F_DT][i] = dtp;
+    dtmin = dmin_(dtmin, dtp);
   }
   // block minimum first, then one atomic per block
   __shared__ double wmin[ELEM_THREADS / 32];
@@ -327,7 +328,10 @@ cudaError_t launch_compute_dt(const Launch & L, const Particles & P,
   const PhysParams & pp, DevTime * t, DevStatus * st, int with_checks,
   int f32) {
   k_dt_init<<<1, 1, 0, L.stream>>>(t);
-  const int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
+  // a few blocks per SM: the per-block minima meet in one atomic each
+  int nb = (P.n + ELEM_THREADS - 1) / ELEM_THREADS;
+  if(nb > 152 * 8)
+    nb = 152 * 8;
 #define DT_LAUNCH(D, C, F) \
   k_compute_dt<D, C, F><<<nb, ELEM_THREADS, 0, L.stream>>>(P, pp, t, st)
   if(pp.dim == 3) {

@@ -109,6 +109,7 @@ struct Packed {
   float4 * vhm;     // {vh_x, vh_y, vh_z, m}
   float4 * vel;     // {v_x, v_y, v_z, 0}
   float4 * thermo;  // {rho, P/rho^2, c_s (new), c_s (previous)}
+  float * mass;     // m alone, for the density pass (4 B per pair instead of 16)
   float2 * visc;    // Cullen & Dehnen: {c_s, sign(div v)} in the alpha pass,
                     // {alpha, 0} in the pair passes
   float * qscale;   // device [3]: range extent / 2^31 per axis

@@ -55,9 +55,12 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
-  if(what & PACK_VHM)
+  if(what & PACK_VHM) {
+    const float m = (float)P.f[F_M][i];
     K.vhm[i] = make_float4((float)P.f[F_VHX][i], (float)P.f[F_VHY][i],
-      dim == 3 ? (float)P.f[F_VHZ][i] : 0.f, (float)P.f[F_M][i]);
+      dim == 3 ? (float)P.f[F_VHZ][i] : 0.f, m);
+    K.mass[i] = m;
+  }
   if(what & PACK_VEL)
     K.vel[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, 0.f);

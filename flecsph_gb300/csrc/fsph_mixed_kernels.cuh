@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
     for(int u = 0; u < 4; ++u) {
       const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
       const int4 qb = Kp.qpos[b];
-      const float mb = Kp.vhm[b].w;
+      const float mb = Kp.mass[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
       const float ih = 1.0f / hab;
@@ -288,8 +288,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
     double vv = 0;
     for(int d = 0; d < D; ++d)
       vv += P.f[F_VX + d][a] * P.f[F_VX + d][a];
-    const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
-    double eint = P.f[F_E][a] - .5 * vv - ext_potential<D>(pp, pos);
+    double eint = P.f[F_E][a] - .5 * vv - ext_potential_of<D>(pp, P.f, a);
     if(!(eint > 0)) {
       if(atomicCAS(&st->code, 0, (int)FSPH_ERR_NEG_ENERGY) == 0)
         st->index = a;
