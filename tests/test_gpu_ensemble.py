@@ -101,3 +101,44 @@ def test_tune_and_member_error_reported():
         ens.sync()
     assert "LIST_OVERFLOW" in str(e.value)
     ens.close()
+
+
+def test_mixed_physics_members():
+    """Members with Cullen & Dehnen viscosity, external forces, relaxation
+    iterations (stepped eagerly: their passes depend on the iteration
+    number) and the other equations of state, in both precisions, next to
+    plain members: each equals its problem stepped alone."""
+    sph = _lib()
+    from flecsph_gb300.abi import EOS_PPT, PRECISION_MIXED, VISC_CULLEN
+    probs = []
+    s, p, m = setups.noh2d(40)
+    p.sph_viscosity = VISC_CULLEN
+    probs.append((s, p))
+    s, p, m = setups.noh2d(40)
+    p.sph_viscosity = VISC_CULLEN
+    p.precision_mode = PRECISION_MIXED
+    probs.append((s, p))
+    s, p = setups.external_force_problem("gravity_walls_2d")
+    probs.append((s, p))
+    s, p = setups.external_force_problem("relaxation_dudt_2d")
+    p.relaxation_steps = 4
+    probs.append((s, p))
+    s, p = setups.external_force_problem("airfoil_2d")
+    p.precision_mode = PRECISION_MIXED
+    probs.append((s, p))
+    s, p, m = setups.sod2d(100, 10)
+    p.eos_type = EOS_PPT
+    p.poly_gamma2, p.ppt_density_thr = 2.5, 0.5
+    probs.append((s, p))
+    probs = [(setups.shuffled(s, 30 + k), p) for k, (s, p) in enumerate(probs)]
+    ens = sph.Ensemble()
+    members = [ens.add(p, len(s["x"])) for s, p in probs]
+    for mb, (s, p) in zip(members, probs):
+        mb.read_bodies(s)
+    ens.set_lanes(2)
+    steps = 8
+    ens.step(steps)
+    ens.sync()
+    for mb, (s, p) in zip(members, probs):
+        _assert_same((mb.download(), mb.time()), _alone(sph, s, p, steps))
+    ens.close()
