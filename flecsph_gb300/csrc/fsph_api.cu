@@ -481,6 +481,8 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.vel, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.thermo, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.mass, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.velp, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.rc, N) == cudaSuccess;
   if(c->pp.cullen)
     ok &= dalloc(c, &c->K.visc, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;

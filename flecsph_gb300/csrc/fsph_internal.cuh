@@ -110,6 +110,8 @@ struct Packed {
   float4 * vel;     // {v_x, v_y, v_z, 0}
   float4 * thermo;  // {rho, P/rho^2, c_s (new), c_s (previous)}
   float * mass;     // m alone, for the density pass (4 B per pair instead of 16)
+  float4 * velp;    // de/dt pass: {v_x, v_y, v_z, P/rho^2}
+  float2 * rc;      // de/dt pass: {rho, c_s} (56 B per pair with qpos, vhm, velp)
   float2 * visc;    // Cullen & Dehnen: {c_s, sign(div v)} in the alpha pass,
                     // {alpha, 0} in the pair passes
   float * qscale;   // device [3]: range extent / 2^31 per axis

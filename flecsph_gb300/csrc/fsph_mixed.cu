@@ -46,7 +46,9 @@ __global__ void k_pack_pos(Particles P, int dim,
 
 // PACK_AV_IN: {c_s, sign(div v)} for the Cullen & Dehnen alpha pass;
 // PACK_AV: {alpha, 0} for the pair passes that weight the viscosity by it.
-enum { PACK_VHM = 1, PACK_VEL = 2, PACK_THERMO = 4, PACK_AV_IN = 8, PACK_AV = 16 };
+// PACK_DEDT: the de/dt pass's {v, P/rho^2} and {rho, c_s} records.
+enum { PACK_VHM = 1, PACK_VEL = 2, PACK_THERMO = 4, PACK_AV_IN = 8, PACK_AV = 16,
+       PACK_DEDT = 32 };
 
 // Refresh the packed records a pass reads from the FP64 state, so every
 // pass sees the current v_half, v, rho, P and c_s whatever the caller did
@@ -77,6 +79,12 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
   }
   if(what & PACK_AV)
     K.visc[i] = make_float2((float)P.f[F_ALPHA][i], 0.f);
+  if(what & PACK_DEDT) {
+    const double rho = P.f[F_RHO][i];
+    K.velp[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
+      dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)(P.f[F_P][i] / (rho * rho)));
+    K.rc[i] = make_float2((float)rho, (float)P.f[F_CS][i]);
+  }
 }
 
 cudaError_t launch_pack_positions(const Launch & L, const Particles & P,
@@ -197,7 +205,7 @@ cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_VEL | PACK_THERMO | (pp.cullen ? PACK_AV : 0));
+    PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
     run_dedt_mixed_cullen(L, P, pp, Ls, K);

@@ -466,8 +466,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
   const int4 qa = Kp.qpos[a];
   const float ha = __int_as_float(qa.w);
   const float4 vha = Kp.vhm[a];
-  const float4 va = Kp.vel[a];
-  const float4 ta = Kp.thermo[a];
+  const float4 va = Kp.velp[a];  // .w = P_a / rho_a^2
+  const float2 ra = Kp.rc[a];
   const int cnt = Ls.cnt[a];
   float sum = 0.f, comp = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
@@ -483,17 +483,16 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
       const float ih = 1.0f / hab;
       const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
-      const float4 vb = Kp.vel[b];
-      const float4 tb = Kp.thermo[b];
+      const float4 vb = Kp.velp[b];
+      const float2 rb = Kp.rc[b];
       const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
                          (vha.z - vhb.z) * g.dz;
       const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-      const float rho_ab = 0.5f * (ta.x + tb.x);
-      const float c_ab = 0.5f * (ta.z + tb.z);
-      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
+        0.5f * (ra.y + rb.y), mu);
       const float vad = f * (va.x * g.dx + va.y * g.dy + va.z * g.dz);
       const float vbd = f * (vb.x * g.dx + vb.y * g.dy + vb.z * g.dz);
-      kahan(sum, comp, vhb.w * (ta.y * vbd + vad * tb.y + 0.5f * Pi * (vbd + vad)));
+      kahan(sum, comp, vhb.w * (va.w * vbd + vad * vb.w + 0.5f * Pi * (vbd + vad)));
     }
   }
   double gv = 0;
