@@ -496,8 +496,11 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
     for(int d = 0; d < dim; ++d)
       rc[d] = 0.5 * (ord_dec(rbits[d]) + ord_dec(rbits[3 + d]));
   int p = T.leaf_parent[i];
+  // Leaves write nothing here, and each node's writes are fenced before the
+  // thread moves up, so one fence per level orders a node's data before the
+  // arrival count its parent's second thread reads it after (with __ldcg,
+  // from L2).
   while(p >= 0) {
-    __threadfence();
     if(atomicAdd(&T.counter[p], 1u) == 0)
       return;  // the sibling subtree is not finished yet
     if(T.gmom) {
@@ -1189,7 +1192,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
               const float2 nrf = make_float2(-rf.x, -rf.y);
               const float2 t = __ffma2_rn(rf, nrf, d2);
               const float2 mg = __fmul2_rn(rf, __ffma2_rn(rf, eps2, kq2));
-              if(decide(t.x, mg.x, id.x))
+              if(id.x >= 0 && decide(t.x, mg.x, id.x))
                 append(id.x);
               if(id.y >= 0 && decide(t.y, mg.y, id.y))
                 append(id.y);
