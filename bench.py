@@ -147,10 +147,21 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # start the region once the sampler is writing (nvidia-smi takes a
+        # moment to come up; a short region would otherwise see no sample)
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < 3.0:
+            try:
+                if os.path.getsize(self.f.name) > 0:
+                    break
+            except OSError:
+                break
+            time.sleep(0.01)
+        self.t_start = time.time()
         return self
 
     def __exit__(self, *a):

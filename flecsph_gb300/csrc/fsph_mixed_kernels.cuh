@@ -317,8 +317,10 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
 // rule as k_vsig_mixed) is evaluated in this loop instead of a pass of its
 // own; it reads the pre-kick velocities packed for the density pass, so the
 // kick below cannot race with it.
+// Three blocks of 256 per SM (<= 85 registers): the pass waits on neighbour
+// gathers, and 24 warps hide more of them than 16.
 template<int D, int K, bool VSIG, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS) k_accel_mixed(Particles P,
+__global__ void __launch_bounds__(MIX_THREADS, 3) k_accel_mixed(Particles P,
   PhysParams pp, Lists Ls, Packed Kp, int kick, const DevTime * tm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
