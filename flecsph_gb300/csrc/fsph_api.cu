@@ -933,9 +933,28 @@ fsph_status fsph_dedt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
-    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K));
+    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, 0, c->d_time, c->d_status));
   else
     CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
+  return FSPH_OK;
+}
+
+// de/dt followed by the element-wise update `op` (OP_RECOMPUTE_THERMO or
+// OP_RECOMPUTE_KICK_E): one pass on the mixed path, two on the FP64 path
+// (whose update stays in the -fmad=false element-wise unit).
+static fsph_status dedt_then(fsph_ctx * c, int op) {
+  if(!c->mixed) {
+    const fsph_status s0 = fsph_dedt(c);
+    return s0 ? s0 : elem(c, op, FSPH_TIMER_INTEGRATE);
+  }
+  if(!c->tree_ok)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_ENERGY);
+  CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status));
   return FSPH_OK;
 }
 
@@ -1268,10 +1287,13 @@ fsph_status fsph_step(fsph_ctx * c) {
     if(evolve) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         if(thermo) {
-          TRY(fsph_dedt(c));
-          if(relax)
+          if(relax) {
+            TRY(fsph_dedt(c));
             TRY(fsph_add_drag_dedt(c));
-          TRY(elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE));
+            TRY(elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE));
+          }
+          else
+            TRY(dedt_then(c, OP_RECOMPUTE_THERMO));
         }
         else {
           TRY(fsph_dudt(c));
@@ -1328,11 +1350,14 @@ fsph_status fsph_step(fsph_ctx * c) {
       for(int m = 1; m <= p.pressure_updates_number; ++m) {
         const bool lastp = m == p.pressure_updates_number;
         if(thermo) {
-          TRY(fsph_dedt(c));
-          if(relax)
+          const int op = lastp ? OP_RECOMPUTE_KICK_E : OP_RECOMPUTE_THERMO;
+          if(relax) {
+            TRY(fsph_dedt(c));
             TRY(fsph_add_drag_dedt(c));
-          TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_E : OP_RECOMPUTE_THERMO,
-            FSPH_TIMER_INTEGRATE));
+            TRY(elem(c, op, FSPH_TIMER_INTEGRATE));
+          }
+          else
+            TRY(dedt_then(c, op));
         }
         else {
           TRY(fsph_dudt(c));

@@ -202,7 +202,8 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
+  const DevTime * t, DevStatus * st);
 
 // ---- fsph_gravity.cu ----
 cudaError_t launch_gravity(const Launch & L, const Particles & P,

@@ -202,15 +202,16 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
 }
 
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K) {
+  const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
+  const DevTime * t, DevStatus * st) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
     PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
-    run_dedt_mixed_cullen(L, P, pp, Ls, K);
+    run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st);
   else
-    run_dedt_mixed<false>(L, P, pp, Ls, K);
+    run_dedt_mixed<false>(L, P, pp, Ls, K, then_op, t, st);
   return cudaGetLastError();
 }
 

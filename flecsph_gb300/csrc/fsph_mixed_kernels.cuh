@@ -456,9 +456,14 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
 }
 
 // --------------------------------------------------------------- de/dt --
+// then_op (OP_RECOMPUTE_THERMO or OP_RECOMPUTE_KICK_E, else 0) applies the
+// element-wise update that follows de/dt in the driver to the particle
+// right away: it reads only the particle's own fields, and the pass reads
+// the neighbours' P and c_s from the packed records, not the fields.
 template<int D, int K, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
-  PhysParams pp, Lists Ls, Packed Kp) {
+__global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_mixed(Particles P,
+  PhysParams pp, Lists Ls, Packed Kp, int then_op, const DevTime * tm,
+  DevStatus * st) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
     return;
@@ -500,7 +505,31 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dedt_mixed(Particles P,
   double gv = 0;
   for(int d = 0; d < D; ++d)
     gv += P.f[F_GAX + d][a] * P.f[F_VX + d][a];
-  P.f[F_DEDT][a] = -((double)sum - (double)comp) + gv;
+  const double dedt = -((double)sum - (double)comp) + gv;
+  P.f[F_DEDT][a] = dedt;
+  if(then_op) {
+    // recompute_pressure_soundspeed_thermokinetic (default_physics.h:169-182)
+    // and, with the kick, leapfrog_kick_e (integration.h:94-98)
+    const double dt = tm->dt;
+    double vv = 0, vda = 0;
+    for(int d = 0; d < D; ++d) {
+      const double v = P.f[F_VX + d][a];
+      vv += v * v;
+      vda += v * P.f[F_AX + d][a];
+    }
+    const double e = P.f[F_E][a];
+    const double eint = e - .5 * vv - ext_potential_of<D>(pp, P.f, a);
+    if(!(eint > 0))
+      raise_status(st, FSPH_ERR_NEG_ENERGY, a);
+    P.f[F_U][a] = eint;
+    double Pn, cs;
+    eos_p_cs(pp, P.f[F_RHO][a], eint + 0.5 * dt * (dedt - vda), P.f[F_K][a],
+      P.f[F_YE][a], P.f[F_P][a], P.f[F_CS][a], Pn, cs);
+    P.f[F_P][a] = Pn;
+    P.f[F_CS][a] = cs;
+    if(then_op == OP_RECOMPUTE_KICK_E)
+      P.f[F_E][a] = e + 0.5 * dt * dedt;
+  }
 }
 
 // ------------------------------------------------------------ dispatch --
@@ -568,8 +597,9 @@ inline void run_dudt_mixed(const Launch & L, const Particles & P,
 
 template<bool CULL>
 inline void run_dedt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K) {
-  MIX_DISPATCH(k_dedt_mixed, CULL, P, pp, Ls, K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
+  const DevTime * t, DevStatus * st) {
+  MIX_DISPATCH(k_dedt_mixed, CULL, P, pp, Ls, K, then_op, t, st);
 }
 
 template<bool CULL>
@@ -619,7 +649,8 @@ void run_accel_mixed_cullen(const Launch & L, const Particles & P,
 void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
+  const DevTime * t, DevStatus * st);
 void run_alpha_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 
