@@ -116,6 +116,7 @@ void make_phys(const fsph_params * p, PhysParams * pp) {
   pp->cfl = p->timestep_cfl_factor;
   pp->gamma2 = p->poly_gamma2;
   pp->rho_thr = p->ppt_density_thr;
+  pp->ppt_k2 = pow(p->ppt_density_thr, p->poly_gamma - p->poly_gamma2);
   pp->out_screen_dt = p->out_screen_dt;
   pp->out_scalar_dt = p->out_scalar_dt;
   pp->out_h5data_dt = p->out_h5data_dt;
@@ -918,7 +919,7 @@ fsph_status fsph_dudt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
-    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time));
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, 0));
   else
     CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
   return FSPH_OK;
@@ -939,12 +940,13 @@ fsph_status fsph_dedt(fsph_ctx * c) {
   return FSPH_OK;
 }
 
-// de/dt followed by the element-wise update `op` (OP_RECOMPUTE_THERMO or
-// OP_RECOMPUTE_KICK_E): one pass on the mixed path, two on the FP64 path
+// de/dt (du/dt) followed by the element-wise update `op`
+// (OP_RECOMPUTE_THERMO or OP_RECOMPUTE_KICK_E; OP_RECOMPUTE or
+// OP_RECOMPUTE_KICK_U): one pass on the mixed path, two on the FP64 path
 // (whose update stays in the -fmad=false element-wise unit).
-static fsph_status dedt_then(fsph_ctx * c, int op) {
+static fsph_status energy_then(fsph_ctx * c, bool thermo, int op) {
   if(!c->mixed) {
-    const fsph_status s0 = fsph_dedt(c);
+    const fsph_status s0 = thermo ? fsph_dedt(c) : fsph_dudt(c);
     return s0 ? s0 : elem(c, op, FSPH_TIMER_INTEGRATE);
   }
   if(!c->tree_ok)
@@ -954,7 +956,10 @@ static fsph_status dedt_then(fsph_ctx * c, int op) {
     return s;
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
-  CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status));
+  if(thermo)
+    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status));
+  else
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, op));
   return FSPH_OK;
 }
 
@@ -1293,14 +1298,15 @@ fsph_status fsph_step(fsph_ctx * c) {
             TRY(elem(c, OP_RECOMPUTE_THERMO, FSPH_TIMER_INTEGRATE));
           }
           else
-            TRY(dedt_then(c, OP_RECOMPUTE_THERMO));
+            TRY(energy_then(c, true, OP_RECOMPUTE_THERMO));
         }
-        else {
+        else if(relax) {
           TRY(fsph_dudt(c));
-          if(relax)
-            TRY(fsph_add_drag_dudt(c));
+          TRY(fsph_add_drag_dudt(c));
           TRY(elem(c, OP_RECOMPUTE, FSPH_TIMER_INTEGRATE));
         }
+        else
+          TRY(energy_then(c, false, OP_RECOMPUTE));
       }
     }
   }
@@ -1357,14 +1363,17 @@ fsph_status fsph_step(fsph_ctx * c) {
             TRY(elem(c, op, FSPH_TIMER_INTEGRATE));
           }
           else
-            TRY(dedt_then(c, op));
+            TRY(energy_then(c, true, op));
         }
         else {
-          TRY(fsph_dudt(c));
-          if(relax)
+          const int op = lastp ? OP_RECOMPUTE_KICK_U : OP_RECOMPUTE;
+          if(relax) {
+            TRY(fsph_dudt(c));
             TRY(fsph_add_drag_dudt(c));
-          TRY(elem(c, lastp ? OP_RECOMPUTE_KICK_U : OP_RECOMPUTE,
-            FSPH_TIMER_INTEGRATE));
+            TRY(elem(c, op, FSPH_TIMER_INTEGRATE));
+          }
+          else
+            TRY(energy_then(c, false, op));
         }
       }
     }

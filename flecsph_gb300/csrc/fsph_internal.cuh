@@ -49,6 +49,7 @@ struct PhysParams {
   double alpha_max, visc_l, visc_delta;  // visc_cullen parameters
   double sinc_index, sinc_sigma[3];       // sinc kernel power and norms
   double gamma2, rho_thr;                 // eos_ppt upper segment
+  double ppt_k2;                          // rho_thr^(gamma - gamma2)
   double out_screen_dt, out_scalar_dt, out_h5data_dt;
   double G;
   // external forces (eforce.h) in the order external_force::select lists
@@ -200,7 +201,8 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
   const DevTime * t, int fused_vsig);
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
+  int then_op);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
   const DevTime * t, DevStatus * st);

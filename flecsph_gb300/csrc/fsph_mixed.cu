@@ -189,15 +189,16 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
 }
 
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t) {
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
+  int then_op) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_VEL | PACK_THERMO | (pp.cullen ? PACK_AV : 0));
+    PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
-    run_dudt_mixed_cullen(L, P, pp, Ls, K, t);
+    run_dudt_mixed_cullen(L, P, pp, Ls, K, t, then_op);
   else
-    run_dudt_mixed<false>(L, P, pp, Ls, K, t);
+    run_dudt_mixed<false>(L, P, pp, Ls, K, t, then_op);
   return cudaGetLastError();
 }
 

@@ -21,8 +21,9 @@ void run_accel_mixed_cullen(const Launch & L, const Particles & P,
 }
 
 void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t) {
-  run_dudt_mixed<true>(L, P, pp, Ls, K, t);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
+  int then_op) {
+  run_dudt_mixed<true>(L, P, pp, Ls, K, t, then_op);
 }
 
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,

@@ -402,9 +402,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_accel_mixed(Particles P,
 }
 
 // --------------------------------------------------------------- du/dt --
+// The same records as the de/dt pass ({v, .} and {rho, c_s}: 56 B per pair);
+// then_op (OP_RECOMPUTE or OP_RECOMPUTE_KICK_U, else 0) applies the
+// element-wise update that follows du/dt in the driver to the particle.
 template<int D, int K, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
-  PhysParams pp, Lists Ls, Packed Kp, const DevTime * tm) {
+__global__ void __launch_bounds__(MIX_THREADS, 4) k_dudt_mixed(Particles P,
+  PhysParams pp, Lists Ls, Packed Kp, const DevTime * tm, int then_op) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
     return;
@@ -419,8 +422,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
   const int4 qa = Kp.qpos[a];
   const float ha = __int_as_float(qa.w);
   const float4 vha = Kp.vhm[a];
-  const float4 va = Kp.vel[a];
-  const float4 ta = Kp.thermo[a];
+  const float4 va = Kp.velp[a];
+  const float2 ra = Kp.rc[a];
   const int cnt = Ls.cnt[a];
   float dp = 0.f, cp = 0.f, dv = 0.f, cv = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
@@ -436,14 +439,13 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
       const float ih = 1.0f / hab;
       const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
-      const float4 vb = Kp.vel[b];
-      const float4 tb = Kp.thermo[b];
+      const float4 vb = Kp.velp[b];
+      const float2 rb = Kp.rc[b];
       const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
                          (vha.z - vhb.z) * g.dz;
       const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-      const float rho_ab = 0.5f * (ta.x + tb.x);
-      const float c_ab = 0.5f * (ta.z + tb.z);
-      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
+        0.5f * (ra.y + rb.y), mu);
       const float vdw = f * ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
                              (va.z - vb.z) * g.dz);
       kahan(dp, cp, vhb.w * vdw);
@@ -452,7 +454,20 @@ __global__ void __launch_bounds__(MIX_THREADS) k_dudt_mixed(Particles P,
   }
   const double sp = (double)dp - (double)cp, sv = (double)dv - (double)cv;
   const double rho_a = P.f[F_RHO][a];
-  P.f[F_DUDT][a] = P.f[F_P][a] / (rho_a * rho_a) * sp + .5 * sv;
+  const double dudt = P.f[F_P][a] / (rho_a * rho_a) * sp + .5 * sv;
+  P.f[F_DUDT][a] = dudt;
+  if(then_op) {
+    // recompute_pressure_soundspeed (default_physics.h:153-161) and, with
+    // the kick, leapfrog_kick_u (integration.h:80-84)
+    const double dt = tm->dt, uint = P.f[F_U][a];
+    double Pn, cs;
+    eos_p_cs(pp, rho_a, uint + 0.5 * dt * dudt, P.f[F_K][a], P.f[F_YE][a],
+      P.f[F_P][a], P.f[F_CS][a], Pn, cs);
+    P.f[F_P][a] = Pn;
+    P.f[F_CS][a] = cs;
+    if(then_op == OP_RECOMPUTE_KICK_U)
+      P.f[F_U][a] = uint + 0.5 * dt * dudt;
+  }
 }
 
 // --------------------------------------------------------------- de/dt --
@@ -591,8 +606,9 @@ inline void run_density_mixed(const Launch & L, const Particles & P,
 
 template<bool CULL>
 inline void run_dudt_mixed(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t) {
-  MIX_DISPATCH(k_dudt_mixed, CULL, P, pp, Ls, K, t);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
+  int then_op) {
+  MIX_DISPATCH(k_dudt_mixed, CULL, P, pp, Ls, K, t, then_op);
 }
 
 template<bool CULL>
@@ -647,7 +663,8 @@ void run_accel_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
   const DevTime * t, int fused_vsig);
 void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
-  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
+  const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
+  int then_op);
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
   const DevTime * t, DevStatus * st);

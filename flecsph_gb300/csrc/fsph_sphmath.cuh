@@ -294,18 +294,6 @@ __device__ __forceinline__ double visc_pi_pp(const PhysParams & pp,
 #define FSPH_WD_B 9.73932099e5        // [moles/cm^3]
 #define FSPH_C_LIGHT_CGS 2.99792458e10
 
-__device__ __forceinline__ double wd_pressure(double rho, double Ye) {
-  double x = cbrt(rho * Ye / FSPH_WD_B);
-  double x2 = x * x;
-  return FSPH_WD_A * (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x));
-}
-__device__ __forceinline__ double wd_soundspeed(double rho, double Ye) {
-  double x = cbrt(rho * Ye / FSPH_WD_B);
-  double x2 = x * x;
-  double numer = (1. + x2) * (6. * x2 - 3.) + 3. + x2 * (2. * x2 - 3.);
-  double denom = (1. + x2) * (6. * x2 + 1.) - 1. + x2 * (2. * x2 + 1.);
-  return sqrt(numer / (3. * denom)) * FSPH_C_LIGHT_CGS;
-}
 __device__ __forceinline__ double wd_internal_energy(double rho, double Ye) {
   const double x = cbrt(rho * Ye / FSPH_WD_B), x2 = x * x, x3 = x * x * x;
   return FSPH_WD_A / rho * (8. * x3 * (sqrt(x2 + 1.) - 1.) -
@@ -318,28 +306,31 @@ __device__ __forceinline__ double wd_internal_energy(double rho, double Ye) {
 __device__ __forceinline__ void eos_p_cs(const PhysParams & pp, double rho,
   double u, double K, double Ye, double P_old, double cs_old, double & P,
   double & cs) {
+  // The sound speed of a polytrope, sqrt(K gamma rho^(gamma - 1)), is taken
+  // as sqrt(gamma P / rho): one FP64 pow per particle instead of two (pow
+  // is long on this part's FP64 pipe), equal to rounding.
   const double g = pp.gamma;
   if(pp.eos == FSPH_EOS_POLYTROPIC) {
     P = K * pow(rho, g);
-    cs = sqrt(K * g * pow(rho, g - 1.));
+    cs = sqrt(g * P / rho);
   }
   else if(pp.eos == FSPH_EOS_WD) {
-    P = wd_pressure(rho, Ye);
-    cs = wd_soundspeed(rho, Ye);
+    // both from one x = (rho Ye / B)^(1/3)
+    const double x = cbrt(rho * Ye / FSPH_WD_B), x2 = x * x;
+    P = FSPH_WD_A * (x * (2. * x2 - 3.) * sqrt(x2 + 1.) + 3. * asinh(x));
+    const double numer = (1. + x2) * (6. * x2 - 3.) + 3. + x2 * (2. * x2 - 3.);
+    const double denom = (1. + x2) * (6. * x2 + 1.) - 1. + x2 * (2. * x2 + 1.);
+    cs = sqrt(numer / (3. * denom)) * FSPH_C_LIGHT_CGS;
   }
   else if(pp.eos == FSPH_EOS_PPT) {
-    const double g2 = pp.gamma2, thr = pp.rho_thr;
-    if(rho < thr)
+    // K2 = K1 rho_thr^(gamma - gamma2): the power is a constant of the run
+    if(rho < pp.rho_thr) {
       P = K * pow(rho, g);
-    else {
-      double K2 = K * pow(thr, g - g2);
-      P = K2 * pow(rho, g2);
+      cs = sqrt(g * P / rho);
     }
-    if(rho < thr)
-      cs = sqrt(K * g * pow(rho, g - 1.));
     else {
-      double K2 = K * pow(thr, g - g2);
-      cs = sqrt(K2 * g2 * pow(rho, g2 - 1.));
+      P = K * pp.ppt_k2 * pow(rho, pp.gamma2);
+      cs = sqrt(pp.gamma2 * P / rho);
     }
   }
   else if(pp.eos == FSPH_EOS_NO_EOS) {
