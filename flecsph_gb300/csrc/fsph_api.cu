@@ -1103,7 +1103,7 @@ fsph_status fsph_gravitation(fsph_ctx * c) {
 // newtonian/main_driver.cc:103-298 when enable_fmm).  Elementwise steps that
 // the reference runs back to back are fused; every fusion only combines
 // ---- fsph_step_io ---------------------------------------------------------
-enum { IO_UPDATE = 1, IO_DENSITY = 2, IO_ACCEL = 3, IO_END = 4 };
+enum { IO_UPDATE = 1, IO_DENSITY = 2, IO_ACCEL = 3, IO_ENERGY = 4, IO_END = 5 };
 
 static double ** view_fields(const fsph_soa_view * v, double ** f) {
   double * const src[NF] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->vhx,
@@ -1118,7 +1118,8 @@ static double ** view_fields(const fsph_soa_view * v, double ** f) {
 // The stage of a regular iteration of fsph_step after which field k is not
 // written again: the drift and the permute of update_iteration, the density
 // pass (and the alpha pass), the acceleration (with gravity, relaxation and
-// the velocity kick), and the energy passes, h and dt updates at the end.
+// the velocity kick), the energy passes with the pressure updates and the
+// energy kick, and the h and dt updates at the end.
 static int io_final_stage(const fsph_ctx * c, int k) {
   const fsph_params & p = c->p;
   const bool thermo = p.thermokinetic_formulation, evolve = p.evolve_internal_energy;
@@ -1130,13 +1131,15 @@ static int io_final_stage(const fsph_ctx * c, int k) {
     case F_H:
       return (p.sph_variable_h || p.sph_update_uniform_h) ? IO_END : IO_UPDATE;
     case F_DUDT:
-      return (evolve && !thermo) ? IO_END : IO_UPDATE;
+      return (evolve && !thermo) ? IO_ENERGY : IO_UPDATE;
     case F_DEDT:
-      return (evolve && thermo) ? IO_END : IO_UPDATE;
+      return (evolve && thermo) ? IO_ENERGY : IO_UPDATE;
     case F_E:
-      return (evolve && thermo) ? IO_END : IO_UPDATE;
+      return (evolve && thermo) ? IO_ENERGY : IO_UPDATE;
     case F_U:
-      return evolve ? IO_END : IO_UPDATE;
+      return evolve ? IO_ENERGY : IO_UPDATE;
+    case F_P: case F_CS:
+      return evolve ? IO_ENERGY : IO_ACCEL;
     case F_ALPHA:
       return cullen ? IO_ACCEL : IO_UPDATE;
     case F_DIVV: case F_DDIVVDT:
@@ -1146,7 +1149,7 @@ static int io_final_stage(const fsph_ctx * c, int k) {
     case F_AX: case F_AY: case F_AZ: case F_GAX: case F_GAY: case F_GAZ:
     case F_GPOT: case F_VX: case F_VY: case F_VZ: case F_VSIG:
       return IO_ACCEL;
-    default:  // P, c_s, dt
+    default:  // dt
       return IO_END;
   }
 }
@@ -1199,7 +1202,7 @@ fsph_status fsph_step_io(fsph_ctx * c, const fsph_soa_view * in, fsph_soa_view *
   }
   if(!c->io.stream) {
     CK(cudaStreamCreateWithFlags(&c->io.stream, cudaStreamNonBlocking));
-    for(int k = 0; k < 6; ++k)
+    for(int k = 0; k < 8; ++k)
       CK(cudaEventCreateWithFlags(&c->io.ev[k], cudaEventDisableTiming));
   }
   if(in) {
@@ -1210,8 +1213,8 @@ fsph_status fsph_step_io(fsph_ctx * c, const fsph_soa_view * in, fsph_soa_view *
     view_fields(in, src);
     const size_t bytes = sizeof(double) * (size_t)c->n;
     bool late_any = false;
-    CK(cudaEventRecord(c->io.ev[5], c->stream));
-    CK(cudaStreamWaitEvent(c->io.stream, c->io.ev[5], 0));
+    CK(cudaEventRecord(c->io.ev[6], c->stream));
+    CK(cudaStreamWaitEvent(c->io.stream, c->io.ev[6], 0));
     for(int k = 0; k < NF; ++k) {
       if(!src[k])
         continue;
@@ -1242,8 +1245,8 @@ fsph_status fsph_step_io(fsph_ctx * c, const fsph_soa_view * in, fsph_soa_view *
     c->io.h2d_pending = false;
   }
   // the context's stream continues after the copies
-  CK(cudaEventRecord(c->io.ev[4], c->io.stream));
-  CK(cudaStreamWaitEvent(c->stream, c->io.ev[4], 0));
+  CK(cudaEventRecord(c->io.ev[7], c->io.stream));
+  CK(cudaStreamWaitEvent(c->stream, c->io.ev[7], 0));
   if(s)
     return s;
   return fsph_sync(c);
@@ -1378,6 +1381,7 @@ fsph_status fsph_step(fsph_ctx * c) {
       }
     }
   }
+  TRY(io_stage(c, IO_ENERGY));
   if(p.sph_variable_h)
     TRY(fsph_compute_smoothinglength(c));
   else if(p.sph_update_uniform_h)

@@ -63,7 +63,9 @@ struct fsph_ctx {
   // and which of its fields are already on their way to the host
   struct Io {
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
+    // ev[1..5]: the stages of the step; ev[0]: late input fields copied;
+    // ev[6]: copies may start; ev[7]: the copy stream's work is done
+    cudaEvent_t ev[8] = {};
     bool active = false;
     bool h2d_pending = false;  // late input fields on the copy stream
     fsph_soa_view out{};
