@@ -54,7 +54,9 @@ HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
 # DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) for kernels whose traffic grows with the particle
 # count: profiles/k_neighbors_mixed_sedov3d_64.md (148.2 MB / 262,144)
-MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 565.0}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the walk, per particle,
+# from a 96^3 capture (lists 341 MB, well above L2): 450.7 MB / 884,736
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 509.4}
 
 
 def work_model(phase, nb, mixed):
@@ -516,7 +518,7 @@ def gpu_arm(args):
     tpp = MEASURED_TRAFFIC_PER_PARTICLE.get(top)
     roof["traffic"] = tpp * head["ntot"] if (tpp and mixed_run) else None
     if roof["traffic"] is not None:
-        roof["traffic_source"] = ("ncu dram bytes of a 64^3 capture, per particle, "
+        roof["traffic_source"] = ("ncu dram bytes of a 96^3 capture, per particle, "
                                   "scaled to this launch")
     roof["peak_source"] = ("MEASURED_PEAKS.json hbm_gbs" if roof.get("bound") == "hbm" else
                            "in-repo FMA-chain probe (fsph_measure_peak), measured this run")
