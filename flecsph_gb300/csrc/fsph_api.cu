@@ -773,7 +773,7 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
     int ntot = 0;
     const char * why = nullptr;
     CK(launch_periodic(L, c->P, c->Palt, c->pp, len, per, c->nreal, (int)c->cap,
-      c->PS, &ntot, &why));
+      c->PS, &ntot, &why, c->permute_skip));
     if(why) {
       c->last_error = std::string(why) + ": need " + std::to_string(ntot) +
                       ", capacity " + std::to_string(c->cap);

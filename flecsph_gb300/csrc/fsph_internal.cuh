@@ -231,7 +231,7 @@ cudaError_t launch_exclusive_scan(const Launch & L, const int * in, int * out,
 cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
   const PhysParams & pp, const double * box_len, const int * periodic,
   long long nreal, int cap, PeriodicScratch & S, int * n_out,
-  const char ** why);
+  const char ** why, unsigned skip);
 
 // ---- fsph_fp64.cu ----
 cudaError_t launch_density_fp64(const Launch & L, const Particles & P,

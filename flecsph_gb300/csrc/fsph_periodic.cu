@@ -295,7 +295,7 @@ __global__ void k_write_copies(Particles P, int nreal, PBox B,
 cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
   const PhysParams & pp, const double * box_len, const int * periodic,
   long long nreal, int cap, PeriodicScratch & S, int * n_out,
-  const char ** why) {
+  const char ** why, unsigned skip) {
   cudaError_t e;
   const int n = P.n;
   *why = nullptr;
@@ -311,7 +311,7 @@ cudaError_t launch_periodic(const Launch & L, Particles & P, Particles & Palt,
     src.n = (int)nreal;
     Particles dst = Palt;
     dst.n = (int)nreal;
-    if((e = launch_permute(L, src, dst, S.perm, P.key, 0u)))
+    if((e = launch_permute(L, src, dst, S.perm, P.key, skip)))
       return e;
     Particles t = P;
     P = Palt;
