@@ -51,12 +51,10 @@ sys.path.insert(0, ROOT)
 # per neighbour pair for the pair passes, compulsory HBM bytes for the rest.
 FLOPS_PAIR = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
 HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
-# DRAM bytes per particle per launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) for kernels whose traffic grows with the particle
-# count: profiles/k_neighbors_mixed_sedov3d_64.md (148.2 MB / 262,144)
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the walk, per particle,
-# from a 96^3 capture (lists 341 MB, well above L2): 450.7 MB / 884,736
-MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 509.4}
+# from a 96^3 capture (lists 341 MB, well above L2; the mean of two
+# launches, 488.3 MB / 884,736): profiles/k_neighbors_traffic_sedov3d_96.md
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9}
 
 
 def work_model(phase, nb, mixed):
