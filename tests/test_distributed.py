@@ -1,4 +1,4 @@
-"""Key-range decomposition over two ranks (gloo, on the host), with the CPU
+"""Key-range decomposition over two and four ranks (gloo, on the host), with the CPU
 oracle as each rank's engine: the partition, the halo and the ghost
 refreshes must reproduce the one-rank run.
 
@@ -107,27 +107,29 @@ def _free_port():
         return sk.getsockname()[1]
 
 
-@pytest.fixture(scope="module")
-def two_rank_run(oracle_port, tmp_path_factory):
+@pytest.fixture(scope="module", params=[2, 4], ids=["2ranks", "4ranks"])
+def rank_run(request, oracle_port, tmp_path_factory):
     import torch.multiprocessing as mp
-    outdir = str(tmp_path_factory.mktemp("dist"))
+    world = request.param
+    outdir = str(tmp_path_factory.mktemp(f"dist{world}"))
     steps = 3
-    mp.start_processes(_rank_main, args=(2, _free_port(), outdir, steps), nprocs=2,
-                       join=True, start_method="spawn")
-    ranks = [dict(np.load(os.path.join(outdir, f"rank{r}.npz"))) for r in range(2)]
+    mp.start_processes(_rank_main, args=(world, _free_port(), outdir, steps),
+                       nprocs=world, join=True, start_method="spawn")
+    ranks = [dict(np.load(os.path.join(outdir, f"rank{r}.npz"))) for r in range(world)]
     return ranks, steps
 
 
-def test_partition_balanced_and_halo_present(two_rank_run):
-    ranks, _ = two_rank_run
+def test_partition_balanced_and_halo_present(rank_run):
+    ranks, _ = rank_run
     n = [int(r["nlocal"]) for r in ranks]
     assert sum(n) == 4000
-    assert max(n) - min(n) <= 0.2 * 2000      # sample sort: near-equal counts
+    # sample sort: near-equal counts
+    assert max(n) - min(n) <= 0.2 * 4000 / len(ranks)
     assert all(int(r["nghost"]) > 0 for r in ranks)
 
 
-def test_lists_match_one_rank(two_rank_run, oracle_port):
-    ranks, _ = two_rank_run
+def test_lists_match_one_rank(rank_run, oracle_port):
+    ranks, _ = rank_run
     s, p = _problem()
     o = oracle_port.Oracle("port", p)
     o.upload(s)
@@ -146,8 +148,8 @@ def test_lists_match_one_rank(two_rank_run, oracle_port):
     assert seen == 4000
 
 
-def test_steps_match_one_rank(two_rank_run, oracle_port):
-    ranks, steps = two_rank_run
+def test_steps_match_one_rank(rank_run, oracle_port):
+    ranks, steps = rank_run
     s, p = _problem()
     o = oracle_port.Oracle("port", p)
     o.upload(s)
