@@ -692,12 +692,13 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 //     (dx*dx + dy*dy) + dz*dz <= max(h_a, h_b)^2   in FP64, no FMA.
 // The candidate order makes each list come out in the order in which the
 // reference's breadth-first walk appends neighbours (by depth, then key).
-// Launch shape: one-warp blocks, 20 resident per SM (96 registers, no
-// spills to speak of; 10 KB of shared memory each), against two eight-warp
-// blocks at 122 registers before: 20 warps per SM instead of 16 hide more of
-// the walk's fixed-latency stalls (11 % faster on Sedov 128^3; 80 registers
-// for 24 warps spill and lose).  The FP64 (ordered) walk keeps its larger
-// candidate buffer and eight blocks per SM.
+// Launch shape: one-warp blocks, 20 resident per SM (96 registers, a few
+// bytes of spills; 9 KB of shared memory each: 256 candidates and a
+// 1,024-entry stack).  Two eight-warp blocks at 122 registers hold 16 warps
+// per SM; the 20 here hide more of the walk's fixed-latency stalls and run
+// the Sedov 128^3 walk 11 % faster.  At 80 registers (24 warps) the spills
+// make it slower.  The FP64 (ordered) walk keeps its larger candidate buffer
+// and runs eight blocks per SM.
 #ifndef NB_WARPS
 #define NB_WARPS 1
 #endif
