@@ -83,6 +83,21 @@ def work_model(phase, nb, mixed):
     return ("byte", bytes_pp) if bytes_pp else (None, None)
 
 
+def step_roofline(per_phase, phase_ms, ms_per_step):
+    """Step-level roofline of the work model: t_roof = sum over the modelled
+    phases of work / peak (= frac x measured time, frac as in
+    `roofline_all`), against the measured step.  Phases without a work model
+    (gravity, periodic copies) count as measured time with no roofline
+    time, and are listed."""
+    t_roof = sum(per_phase[k]["frac"] * phase_ms[k] for k in per_phase if k in phase_ms)
+    unmodelled = {k: v for k, v in phase_ms.items() if k not in per_phase}
+    return {"t_roof_ms": t_roof, "t_step_ms": ms_per_step,
+            "frac": t_roof / ms_per_step if ms_per_step > 0 else None,
+            "unmodelled_ms": unmodelled,
+            "model": "sum_k max(F_k / peak_flop, B_k / peak_hbm) over the timer "
+                     "phases, one bound per phase as in roofline_all"}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -538,6 +553,8 @@ def gpu_arm(args):
         "roofline_all": per_phase,
         "per_kernel_ms_per_step": {k: v[0] / K for k, v in t.items() if v[1]},
     }
+    line["roofline_step"] = step_roofline(per_phase, line["per_kernel_ms_per_step"],
+                                          line["ms_per_step"])
     if "fp64" in results:
         line["fp64"] = {"value": world * n * K / (results["fp64"]["ms"] * 1e-3),
                         "ms_per_step": results["fp64"]["ms"] / K}
