@@ -432,13 +432,12 @@ cudaError_t launch_gravity(const Launch & L, const Particles & P,
     return cudaSuccess;
   k_grav_nodes<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, G, rbits, order);
   const size_t smem = (mixed ? gw_warp_bytes<true>() : gw_warp_bytes<false>()) * GW_WARPS;
-  static bool attr = false;
-  if(!attr) {
+  static unsigned long long attr_devices = 0;
+  if(first_on_device(&attr_devices)) {
     cudaFuncSetAttribute(k_gravity_walk<true>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<true>() * GW_WARPS));
     cudaFuncSetAttribute(k_gravity_walk<false>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<false>() * GW_WARPS));
-    attr = true;
   }
   int blocks = nsm * 4;
   const int maxb = (n + GW_WARPS * 32 - 1) / (GW_WARPS * 32) * 4;

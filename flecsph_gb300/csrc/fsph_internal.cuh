@@ -166,6 +166,21 @@ struct Launch {
   long long * counter;  // launches issued
 };
 
+// Kernel attributes (cudaFuncSetAttribute) belong to a device.  True the
+// first time this is asked for the current device, with bit d of *mask
+// recording device d, so a process with contexts on several devices sets
+// them once on each (devices past 64 are always asked).
+inline bool first_on_device(unsigned long long * mask) {
+  int dev = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return true;
+  const unsigned long long bit = 1ull << dev;
+  if(*mask & bit)
+    return false;
+  *mask |= bit;
+  return true;
+}
+
 // ---- fsph_tree.cu ----
 cudaError_t launch_range_keys(const Launch & L, const Particles & P,
   const PhysParams & pp, double * d_range, unsigned long long * keys_out,

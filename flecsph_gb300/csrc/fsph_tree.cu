@@ -1274,13 +1274,12 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
                         (size_t)NB_WARPS * NB_STACK * 4;
   const size_t smem_u = (size_t)NB_WARPS * NB_CAND * 20 +
                         (size_t)NB_WARPS * NB_STACK * 4;
-  static bool attr_set = false;
-  if(!attr_set) {
+  static unsigned long long attr_devices = 0;
+  if(first_on_device(&attr_devices)) {
     cudaFuncSetAttribute(k_neighbors<true>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
     cudaFuncSetAttribute(k_neighbors<false>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
-    attr_set = true;
   }
   int blocks = nsm * (ordered ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM);
   int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
