@@ -526,8 +526,11 @@ void fsph_destroy(fsph_ctx * c) {
   if(!c)
     return;
   cudaSetDevice(c->device);
+  // both streams drain before any buffer they may still touch is freed
   if(c->stream)
     cudaStreamSynchronize(c->stream);
+  if(c->io.stream)
+    cudaStreamSynchronize(c->io.stream);
   for(void * p : c->allocs)
     cudaFree(p);
   for(auto & e : c->events)
@@ -537,7 +540,6 @@ void fsph_destroy(fsph_ctx * c) {
     if(e)
       cudaEventDestroy(e);
   if(c->io.stream) {
-    cudaStreamSynchronize(c->io.stream);
     for(auto & e : c->io.ev)
       if(e)
         cudaEventDestroy(e);
