@@ -29,8 +29,9 @@ members stepped one by one.
 
 `--impl reference` times the reference algorithm on the host cores instead
 (the CPU oracle: the reference compiled from its sources where those exist
-on this machine, otherwise the plain-C restatement), on a 64^3 sample of
-the same problem.
+on this machine, otherwise the plain-C restatement) on the same 128^3
+problem with every host thread, and reports the single-core rate of a 64^3
+sample beside it.
 """
 import argparse
 import ctypes as C
@@ -47,9 +48,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Algorithmic work per particle and timer phase (include/fsph_work.h): flops
-# per neighbour pair for the pair passes, compulsory HBM bytes for the rest.
-FLOPS_PAIR = {"density": 31, "vsig": 27, "accel": 82, "dudt": 84, "energy": 96}
+# Algorithmic work per particle and timer phase: the constants of
+# include/fsph_work.h (the one table both this file and the design notes
+# use), parsed from the header.
 HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the walk, per particle,
 # from a 96^3 capture (lists 341 MB, well above L2; the mean of two
@@ -57,30 +58,62 @@ HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
 MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9}
 
 
-def work_model(phase, nb, mixed):
-    """(kind, amount per particle) for a timer phase; kind 'flop' or 'byte'."""
-    if phase in FLOPS_PAIR:
-        f = FLOPS_PAIR[phase]
-        if phase == "accel" and mixed:  # the signal speed rides in this pass
-            f += FLOPS_PAIR["vsig"]
-        return "flop", f * nb
-    fields = 8  # bytes per FP64 field
-    bytes_pp = {
-        # read positions + h and the previous order, write keys + indices
-        "range_keys": 4 * fields * 2 + 12,
-        # 8 LSD passes of (key, index): histogram read + scatter read/write,
-        # then one gather of 31 arrays
-        "sort": 8 * 36 + 31 * fields * 2,
-        # packed record + radix tree nodes (children, ranges, boxes)
-        "tree": 64 + 4 * 6 + 64,
-        # packed record read, list of nb ints and the count written
-        "neighbors": 64 + 4 * nb + 4,
-        # elementwise kicks/drift/EOS: ~24 fields read or written twice a step
-        "integrate": 2 * 24 * fields,
-        # checks + dt: ~22 fields read, dt written
-        "dt": 23 * fields,
-    }.get(phase)
-    return ("byte", bytes_pp) if bytes_pp else (None, None)
+def read_work_header(path=os.path.join(ROOT, "include", "fsph_work.h")):
+    """{name without the FSPH_ prefix: value} of the #defines in fsph_work.h."""
+    import re
+    out = {}
+    for line in open(path):
+        m = re.match(r"\s*#define\s+FSPH_(\w+)\s+([0-9.]+)", line)
+        if m:
+            out[m.group(1)] = float(m.group(2))
+    return out
+
+
+WORK = read_work_header()
+
+
+def work_model(phase, nb, mixed, thermokinetic=True):
+    """Algorithmic work per particle of a timer phase: {"flop": F, "byte": B}
+    (either may be 0), or None for phases the table does not model (gravity,
+    periodic copies).  nb is the mean neighbour count including self."""
+    W = WORK
+    lst = W["BYTES_PAIR_LIST"] * nb  # the list read by a pair pass
+    energy_flops = W["FLOPS_PAIR_DEDT"] if thermokinetic else W["FLOPS_PAIR_DUDT"]
+    table = {
+        "range_keys": (0.0, W["BYTES_RANGE_KEYS"]),
+        "sort": (0.0, W["BYTES_SORT"]),
+        "tree": (0.0, W["BYTES_TREE"]),
+        "neighbors": (0.0, W["BYTES_NEIGHBORS"] + lst),
+        "density": (W["FLOPS_PAIR_DENSITY"] * nb, W["BYTES_DENSITY"] + lst),
+        "vsig": (W["FLOPS_PAIR_VSIG"] * nb, lst),
+        # the mixed path evaluates the signal speed in the acceleration loop
+        "accel": ((W["FLOPS_PAIR_ACCEL"] + (W["FLOPS_PAIR_VSIG"] if mixed else 0.0)) * nb,
+                  W["BYTES_ACCEL"] + lst),
+        # de/dt (du/dt) with the pressure predictor that follows it
+        "energy": (energy_flops * nb, W["BYTES_DEDT"] + W["BYTES_RECOMPUTE_P"] + lst),
+        "integrate": (0.0, W["BYTES_INTEGRATE"]),
+        "dt": (0.0, W["BYTES_DT"]),
+    }
+    if phase not in table:
+        return None
+    f, b = table[phase]
+    return {"flop": f, "byte": b}
+
+
+def phase_roofline(work, n, seconds, peak_flop, flop_kind, peak_hbm=HBM_PEAK):
+    """Roofline of one launch of a phase over n particles taking `seconds`:
+    the bound is the larger of F / peak_flop and B / peak_hbm; `achieved`
+    and `frac` are in that bound's unit."""
+    t_f = n * work["flop"] / (peak_flop * 1e12) if work["flop"] else 0.0
+    t_b = n * work["byte"] / (peak_hbm * 1e9) if work["byte"] else 0.0
+    if t_f >= t_b:
+        ach = n * work["flop"] / seconds / 1e12
+        return {"bound": flop_kind, "achieved": ach, "peak": peak_flop,
+                "unit": "TFLOP/s", "frac": ach / peak_flop,
+                "t_roof_ms": 1e3 * t_f}
+    ach = n * work["byte"] / seconds / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": peak_hbm, "unit": "GB/s",
+            "frac": ach / peak_hbm, "t_roof_ms": 1e3 * t_b}
 
 
 def step_roofline(per_phase, phase_ms, ms_per_step):
@@ -211,8 +244,10 @@ class Clocks:
         return out
 
 
-def run_cpu_oracle(n1d, steps, threads, min_seconds=10.0, max_steps=None):
-    """Time the reference algorithm on the host cores on a Sedov sample."""
+def run_cpu_oracle(n1d, steps, threads, min_seconds=10.0, max_steps=None, warmup=0):
+    """Time the reference algorithm on the host cores on the Sedov problem
+    (`warmup` untimed iterations after the initial one, then `max_steps`
+    timed ones, or as many as fill `min_seconds`)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     from flecsph_gb300 import setups
@@ -223,6 +258,8 @@ def run_cpu_oracle(n1d, steps, threads, min_seconds=10.0, max_steps=None):
     o = pyoracle.Oracle(kind, p, threads=threads)
     o.upload(s)
     o.step()  # initial iteration (not timed)
+    for _ in range(warmup):
+        o.step()
     done = 0
     t0 = time.perf_counter()
     while True:
@@ -242,28 +279,32 @@ def run_cpu_oracle(n1d, steps, threads, min_seconds=10.0, max_steps=None):
 
 
 def reference_arm(args):
+    """The reference algorithm on the host cores (all threads), on the same
+    workload as the GPU line: the oracle built from the reference's sources
+    where those exist, else the plain-C restatement.  Beside it, the
+    single-core rate on a 64^3 sample of the same problem (one iteration)."""
     rank, world, local = dist_info()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n1d = 64
+    n1d = args.n1d or 128
     steps, warm = args.steps, args.warmup
-    r0 = run_cpu_oracle(n1d, max(1, warm), threads, max_steps=max(1, warm))
-    r = run_cpu_oracle(n1d, steps, threads, max_steps=steps)
+    r = run_cpu_oracle(n1d, steps, threads, max_steps=steps, warmup=warm)
+    one = run_cpu_oracle(64, 1, 1, max_steps=1)
     line = {
         "metric": "particle-steps/s", "value": r["value"], "unit": "particle-steps/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
         "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"sedov3d_{n1d}^3 sample of sedov3d_128^3",
-                   "n_particles": (n1d ** 3), "kernel": "wendland_c6",
-                   "threads": r["cores"]},
+        "config": {"workload": f"sedov3d_{n1d}^3", "n_particles": n1d ** 3,
+                   "kernel": "wendland_c6", "threads": r["cores"]},
         "cpu_baseline": {"value": r["value"], "unit": "particle-steps/s",
                          "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
+        "single_core": {"value": one["value"], "unit": "particle-steps/s", "cores": 1,
+                        "kind": one["kind"], "sample": one["sample"]},
         "e2e": {"value": r["value"], "unit": "particle-steps/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    del r0
     print(json.dumps(line), flush=True)
 
 
@@ -287,6 +328,44 @@ def drift(c0, c1, s, s1=None):
     return {"energy": abs(c1["energy"] - c0["energy"]) / abs(c0["energy"]),
             "momentum": float(np.linalg.norm(dp)) / max(scale_p, 1e-300),
             "mass": abs(c1["mass"] - c0["mass"]) / c0["mass"]}
+
+
+def per_field_errors(ref, test, p):
+    """Per-field error of `test` against `ref` (both downloaded states of
+    the same particles, matched by id): normwise max|d| / max|ref| and the
+    median, 99th percentile and maximum per particle.  Scalars with a
+    positive scale (rho, P, c_s) use |d| / |ref|; signed or vanishing fields
+    (a, de/dt or du/dt, g_acc) use |d| / max(|ref|, 1e-3 rms|ref|)."""
+    o_r = np.argsort(ref["id"])
+    o_t = np.argsort(test["id"])
+
+    def stats(err, normwise):
+        return {"normwise": float(normwise), "median": float(np.median(err)),
+                "p99": float(np.percentile(err, 99)), "max": float(err.max())}
+
+    out = {}
+    for f in ("rho", "P", "cs"):
+        r, t = ref[f][o_r], test[f][o_t]
+        if not np.any(r):
+            continue
+        err = np.abs(t - r) / np.maximum(np.abs(r), 1e-300)
+        out[f] = stats(err, np.abs(t - r).max() / np.abs(r).max())
+    vec = {"a": ("ax", "ay", "az")}
+    if p.enable_fmm:
+        vec["g_acc"] = ("gax", "gay", "gaz")
+    for name, ks in vec.items():
+        R = np.stack([ref[k][o_r] for k in ks], 1)
+        T = np.stack([test[k][o_t] for k in ks], 1)
+        mag = np.linalg.norm(R, axis=1)
+        rms = np.sqrt((mag ** 2).mean())
+        err = np.linalg.norm(T - R, axis=1) / np.maximum(mag, 1e-3 * rms)
+        out[name] = stats(err, np.abs(T - R).max() / max(np.abs(R).max(), 1e-300))
+    f = "dedt" if p.thermokinetic_formulation else "dudt"
+    r, t = ref[f][o_r], test[f][o_t]
+    rms = np.sqrt((r ** 2).mean())
+    err = np.abs(t - r) / np.maximum(np.abs(r), max(1e-3 * rms, 1e-300))
+    out[f] = stats(err, np.abs(t - r).max() / max(np.abs(r).max(), 1e-300))
+    return out
 
 
 def gravity_check(bs, p, blocks=64, block=1024, seed=7):
@@ -460,10 +539,15 @@ def gpu_arm(args):
         bs.density_pressure_soundspeed()
         bs.save_velocityhalf()
         bs.acceleration()
+        if p.thermokinetic_formulation:
+            bs.dedt()
+        else:
+            bs.dudt()
         if p.enable_fmm:
             bs.gravitation()
         results[mode]["same_state"] = bs.download(
-            fields=["ax", "ay", "az", "gax", "gay", "gaz", "id"])
+            fields=["ax", "ay", "az", "gax", "gay", "gaz", "rho", "P", "cs", "dedt",
+                    "dudt", "id"])
         if args.workload == "polytrope" and rank == 0 and mode == modes[-1]:
             results[mode]["gravity_check"] = gravity_check(bs, p)
         # end to end through the C ABI with pinned host buffers
@@ -514,16 +598,12 @@ def gpu_arm(args):
     for ph, (ms_tot, calls) in t.items():
         if not calls:
             continue
-        kind, amount = work_model(ph, head["nb_mean"], mixed_run)
+        work = work_model(ph, head["nb_mean"], mixed_run, bool(p.thermokinetic_formulation))
+        if work is None:
+            continue
         per_launch_s = ms_tot / calls * 1e-3
-        if kind == "flop":
-            ach = n * amount / per_launch_s / 1e12
-            per_phase[ph] = {"bound": "fp32" if mixed_run else "fp64", "achieved": ach,
-                             "peak": pk_flop, "unit": "TFLOP/s", "frac": ach / pk_flop}
-        elif kind == "byte":
-            ach = n * amount / per_launch_s / 1e9
-            per_phase[ph] = {"bound": "hbm", "achieved": ach, "peak": HBM_PEAK,
-                             "unit": "GB/s", "frac": ach / HBM_PEAK}
+        per_phase[ph] = phase_roofline(work, head["ntot"], per_launch_s, pk_flop,
+                                       "fp32" if mixed_run else "fp64")
     top = max((k for k in t if t[k][1] > 0), key=lambda k: t[k][0])
     roof = dict(per_phase.get(top, {"bound": "hbm", "achieved": None,
                                     "peak": HBM_PEAK, "unit": "GB/s", "frac": None}))
@@ -563,28 +643,21 @@ def gpu_arm(args):
         # two runs have drifted apart, which says nothing about one pass)
         a64 = results["fp64"]["same_state"]
         am = results["mixed"]["same_state"]
-        o64 = np.argsort(a64["id"])
-        om = np.argsort(am["id"])
-        A64 = np.stack([a64[k][o64] for k in ("ax", "ay", "az")], 1)
-        AM = np.stack([am[k][om] for k in ("ax", "ay", "az")], 1)
-        mag = np.linalg.norm(A64, axis=1)
-        rms = np.sqrt((mag ** 2).mean())
-        err = np.linalg.norm(AM - A64, axis=1) / np.maximum(mag, 1e-3 * rms)
-        norm = float(np.abs(AM - A64).max() / np.abs(A64).max())
+        pf = per_field_errors(a64, am, p)
         line["mixed_vs_fp64"] = {"speedup": results["fp64"]["ms"] / results["mixed"]["ms"],
-                                 "accel_rel_err_max": float(err.max()),
-                                 "accel_rel_err_median": float(np.median(err)),
-                                 "accel_normwise": norm,
-                                 "measured_on": "one acceleration pass of each precision "
-                                                "from the input state; per-particle "
-                                                "|da|/max(|a|, 1e-3 rms|a|)"}
+                                 "accel_rel_err_max": pf["a"]["max"],
+                                 "accel_rel_err_median": pf["a"]["median"],
+                                 "accel_normwise": pf["a"]["normwise"],
+                                 "per_field": pf,
+                                 "measured_on": "one pass of each precision from the "
+                                                "input state (density, acceleration, "
+                                                "energy rate, gravity); per particle "
+                                                "|d|/|ref| for rho, P, c_s and "
+                                                "|d|/max(|ref|, 1e-3 rms|ref|) for a, "
+                                                "de/dt (du/dt), g_acc"}
         if p.enable_fmm:
-            G64 = np.stack([a64[k][o64] for k in ("gax", "gay", "gaz")], 1)
-            GM = np.stack([am[k][om] for k in ("gax", "gay", "gaz")], 1)
-            gm = np.linalg.norm(G64, axis=1)
-            ge = np.linalg.norm(GM - G64, axis=1) / np.maximum(gm, 1e-3 * np.sqrt((gm ** 2).mean()))
-            line["mixed_vs_fp64"]["gravity_rel_err_max"] = float(ge.max())
-            line["mixed_vs_fp64"]["gravity_rel_err_median"] = float(np.median(ge))
+            line["mixed_vs_fp64"]["gravity_rel_err_max"] = pf["g_acc"]["max"]
+            line["mixed_vs_fp64"]["gravity_rel_err_median"] = pf["g_acc"]["median"]
     if "e2e" in head:
         e = head["e2e"]
         line["e2e"] = {"value": world * n * K / (e["ms"] * 1e-3), "unit": "particle-steps/s",
@@ -595,7 +668,7 @@ def gpu_arm(args):
         line["gravity_check"] = head.get("gravity_check")
         line["drift"] = {m: results[m]["drift"] for m in results}
     if not args.no_cpu and args.workload == "sedov":
-        cpu = run_cpu_oracle(64, None, os.cpu_count() or 1, min_seconds=10.0)
+        cpu = run_cpu_oracle(n1d, None, os.cpu_count() or 1, min_seconds=10.0)
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line["peaks_measured"] = {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}
     print(json.dumps(line), flush=True)

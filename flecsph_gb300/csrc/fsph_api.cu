@@ -487,6 +487,11 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   if(c->pp.cullen)
     ok &= dalloc(c, &c->K.visc, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fph, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fpl, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fm, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fA, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fscale, 2) == cudaSuccess;
   c->periodic = p->periodic_boundary_x || p->periodic_boundary_y ||
                 p->periodic_boundary_z;
   if(c->periodic) {

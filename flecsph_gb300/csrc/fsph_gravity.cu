@@ -432,13 +432,18 @@ cudaError_t launch_gravity(const Launch & L, const Particles & P,
     return cudaSuccess;
   k_grav_nodes<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, G, rbits, order);
   const size_t smem = (mixed ? gw_warp_bytes<true>() : gw_warp_bytes<false>()) * GW_WARPS;
-  static unsigned long long attr_devices = 0;
-  if(first_on_device(&attr_devices)) {
-    cudaFuncSetAttribute(k_gravity_walk<true>,
+  static std::atomic<unsigned long long> attr_devices{0};
+  cudaError_t ae = once_per_device(&attr_devices, [&]() {
+    cudaError_t e = cudaFuncSetAttribute(k_gravity_walk<true>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<true>() * GW_WARPS));
-    cudaFuncSetAttribute(k_gravity_walk<false>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gw_warp_bytes<false>() * GW_WARPS));
-  }
+    if(e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_gravity_walk<false>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)(gw_warp_bytes<false>() * GW_WARPS));
+    return e;
+  });
+  if(ae != cudaSuccess)
+    return ae;
   int blocks = nsm * 4;
   const int maxb = (n + GW_WARPS * 32 - 1) / (GW_WARPS * 32) * 4;
   if(blocks > maxb)

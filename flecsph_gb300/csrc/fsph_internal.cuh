@@ -3,6 +3,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
 #include <stdint.h>
 
 #include "../../include/fsph.h"
@@ -116,6 +119,16 @@ struct Packed {
   float2 * visc;    // Cullen & Dehnen: {c_s, sign(div v)} in the alpha pass,
                     // {alpha, 0} in the pair passes
   float * qscale;   // device [3]: range extent / 2^31 per axis
+  // Float-float records of the density and acceleration passes (Wendland
+  // kernels).  Positions are X = 1 + (x - lo) / E with E the largest range
+  // extent (slightly enlarged), so every X lies in [1, 2): the high words
+  // of two positions share one exponent and their difference is exact;
+  // h is in the same units.
+  float4 * fph;     // {X_h, Y_h, Z_h, h_h}
+  float4 * fpl;     // {X_l, Y_l, Z_l, h_l}
+  float2 * fm;      // {m_h, m_l}
+  float2 * fA;      // {(P/rho^2)_h, (P/rho^2)_l}
+  double * fscale;  // device [2]: E, 1 / E
 };
 
 // Multipole of a radix-tree node (FP64): mass, centre of mass, traceless
@@ -166,19 +179,36 @@ struct Launch {
   long long * counter;  // launches issued
 };
 
-// Kernel attributes (cudaFuncSetAttribute) belong to a device.  True the
-// first time this is asked for the current device, with bit d of *mask
-// recording device d, so a process with contexts on several devices sets
-// them once on each (devices past 64 are always asked).
-inline bool first_on_device(unsigned long long * mask) {
+// Kernel attributes (cudaFuncSetAttribute) belong to a device.  Runs
+// `apply` (returning a cudaError_t) once for the current device, bit d of
+// *mask recording device d, so a process with contexts on several devices
+// sets them once on each (devices past 64 apply every time).  Contexts on
+// different host threads may share a device: the bit is set only after
+// `apply` has succeeded, under a process-wide lock, so no thread sees the
+// device marked and launches before the attributes are in place.
+inline std::mutex & attr_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+template<class F>
+inline cudaError_t once_per_device(std::atomic<unsigned long long> * mask, F apply) {
   int dev = 0;
-  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
-    return true;
+  cudaError_t e = cudaGetDevice(&dev);
+  if(e != cudaSuccess)
+    return e;
+  if(dev < 0 || dev >= 64)
+    return apply();
   const unsigned long long bit = 1ull << dev;
-  if(*mask & bit)
-    return false;
-  *mask |= bit;
-  return true;
+  if(mask->load(std::memory_order_acquire) & bit)
+    return cudaSuccess;
+  std::lock_guard<std::mutex> lock(attr_mutex());
+  if(mask->load(std::memory_order_acquire) & bit)
+    return cudaSuccess;
+  e = apply();
+  if(e == cudaSuccess)
+    mask->fetch_or(bit, std::memory_order_release);
+  return e;
 }
 
 // ---- fsph_tree.cu ----

@@ -20,12 +20,24 @@ __global__ void k_pack_pos(Particles P, int dim,
   const unsigned long long * rbits, Packed K) {
   // any monotone mapping shared by all particles will do: multiply by the
   // reciprocal, computed once per block (FP64 division is costly here)
-  __shared__ double s_lo[3], s_inv[3];
+  __shared__ double s_lo[3], s_inv[3], s_iE;
   if(threadIdx.x < dim) {
     const int d = threadIdx.x;
     const double lo = ord_dec_m(rbits[d]), hi = ord_dec_m(rbits[3 + d]);
     s_lo[d] = lo;
     s_inv[d] = 2147483648.0 / (hi - lo);
+  }
+  if(threadIdx.x == 0) {
+    // float-float positions: X = 1 + (x - lo) / E in [1, 2 - 2^-20]
+    double E = 0.0;
+    for(int d = 0; d < dim; ++d)
+      E = fmax(E, ord_dec_m(rbits[3 + d]) - ord_dec_m(rbits[d]));
+    E *= 1.0 + 0x1p-19;
+    s_iE = 1.0 / E;
+    if(blockIdx.x == 0) {
+      K.fscale[0] = E;
+      K.fscale[1] = s_iE;
+    }
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,12 +48,26 @@ __global__ void k_pack_pos(Particles P, int dim,
   if(i >= P.n)
     return;
   int q[3] = {0, 0, 0};
+  float xh[4] = {1.f, 1.f, 1.f, 0.f}, xl[4] = {0.f, 0.f, 0.f, 0.f};
   for(int d = 0; d < dim; ++d) {
     double t = (P.f[F_X + d][i] - s_lo[d]) * s_inv[d];
     t = fmin(fmax(t, 0.0), 2147483647.0);
     q[d] = __double2int_rn(t);
+    const double X = fmin(fmax(1.0 + (P.f[F_X + d][i] - s_lo[d]) * s_iE, 1.0),
+      2.0 - 0x1p-20);
+    xh[d] = (float)X;
+    xl[d] = (float)(X - (double)xh[d]);
   }
-  K.qpos[i] = make_int4(q[0], q[1], q[2], __float_as_int((float)P.f[F_H][i]));
+  const double h = P.f[F_H][i];
+  const double hX = h * s_iE;
+  xh[3] = (float)hX;
+  xl[3] = (float)(hX - (double)xh[3]);
+  K.qpos[i] = make_int4(q[0], q[1], q[2], __float_as_int((float)h));
+  K.fph[i] = make_float4(xh[0], xh[1], xh[2], xh[3]);
+  K.fpl[i] = make_float4(xl[0], xl[1], xl[2], xl[3]);
+  const double m = P.f[F_M][i];
+  const float mh = (float)m;
+  K.fm[i] = make_float2(mh, (float)(m - (double)mh));
 }
 
 // PACK_AV_IN: {c_s, sign(div v)} for the Cullen & Dehnen alpha pass;
@@ -68,8 +94,10 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, 0.f);
   if(what & PACK_THERMO) {
     const double rho = P.f[F_RHO][i], cs = P.f[F_CS][i];
-    K.thermo[i] = make_float4((float)rho, (float)(P.f[F_P][i] / (rho * rho)),
-      (float)cs, (float)cs);
+    const double A = P.f[F_P][i] / (rho * rho);
+    K.thermo[i] = make_float4((float)rho, (float)A, (float)cs, (float)cs);
+    const float Ah = (float)A;
+    K.fA[i] = make_float2(Ah, (float)(A - (double)Ah));
   }
   if(what & PACK_AV_IN) {
     // signnum_c of the reference (viscosity.h:63-67), taken in FP64

@@ -24,6 +24,7 @@
 
 #include "fsph_internal.cuh"
 #include "fsph_sphmath.cuh"  // the FP64 EOS the density pass applies
+#include "fsph_ff.cuh"
 
 namespace fsph {
 
@@ -547,6 +548,307 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_mixed(Particles P,
   }
 }
 
+// ------------------------------------------- float-float Wendland passes --
+// The density sum and the acceleration's pressure-gradient sum for the
+// Wendland kernels, in float-float arithmetic (fsph_ff.cuh): pair geometry
+// from the float-float positions, the kernel polynomial, m_b and
+// P/rho^2 + Pi, and the running sums.  Viscosity (mu, Pi) and the signal
+// speed stay FP32: they are small beside the pressure terms or enter
+// through a maximum.  In t = 1 - q the Wendland polynomials are
+//   W h^D / sigma:             C2 t^4 (5 - 4t)
+//                              C4 t^6 (56 - 88t + 35t^2) / 3
+//                              C6 t^8 (66 - 154t + 121t^2 - 32t^3)
+//   (dW/dr)/r h^(D+2) / sigma: C2 -20 t^3
+//                              C4 -56/3 t^5 (6 - 5t)
+//                              C6 -22 t^7 (24 - 39t + 16t^2)
+// (kernels.h's q-forms expanded about q = 1).  Each Horner step adds a
+// constant larger in magnitude than the running value for t in [0, 1], so
+// the fast two-sum applies.  The constant factors and the unit scale E of
+// the positions multiply the finished sums once, in FP64.
+template<int K>
+__host__ __device__ constexpr bool ff_kernel() {
+  return K == FSPH_KERNEL_WENDLAND_C2 || K == FSPH_KERNEL_WENDLAND_C4 ||
+         K == FSPH_KERNEL_WENDLAND_C6;
+}
+
+template<int K>
+__device__ __forceinline__ ffloat ff_wpoly(ffloat t) {
+  const ffloat t2 = ff_sqr(t);
+  const ffloat t4 = ff_sqr(t2);
+  if(K == FSPH_KERNEL_WENDLAND_C2)
+    return ff_mul(t4, ff_cadd(5.f, ff_mul_f(t, -4.f)));
+  if(K == FSPH_KERNEL_WENDLAND_C4) {
+    const ffloat p = ff_cadd(56.f, ff_mul(ff_cadd(-88.f, ff_mul_f(t, 35.f)), t));
+    return ff_mul(ff_mul(t4, t2), p);
+  }
+  const ffloat a1 = ff_cadd(121.f, ff_mul_f(t, -32.f));
+  const ffloat a2 = ff_cadd(-154.f, ff_mul(a1, t));
+  const ffloat p = ff_cadd(66.f, ff_mul(a2, t));
+  return ff_mul(ff_sqr(t4), p);
+}
+
+template<int K>
+__device__ __forceinline__ ffloat ff_gpoly(ffloat t) {
+  const ffloat t2 = ff_sqr(t);
+  if(K == FSPH_KERNEL_WENDLAND_C2)
+    return ff_mul(t2, t);
+  const ffloat t4 = ff_sqr(t2);
+  if(K == FSPH_KERNEL_WENDLAND_C4)
+    return ff_mul(ff_mul(t4, t), ff_cadd(6.f, ff_mul_f(t, -5.f)));
+  const ffloat b1 = ff_cadd(-39.f, ff_mul_f(t, 16.f));
+  const ffloat p = ff_cadd(24.f, ff_mul(b1, t));
+  return ff_mul(ff_mul(ff_mul(t4, t2), t), p);
+}
+
+// W = wconst / h^D * wpoly(t);  (dW/dr)/r = gconst / h^(D+2) * gpoly(t)
+template<int D, int K>
+__device__ __forceinline__ double ff_wconst() {
+  if(K == FSPH_KERNEL_WENDLAND_C2)
+    return wc2_sigma(D);
+  if(K == FSPH_KERNEL_WENDLAND_C4)
+    return wc4_sigma(D) / 3.;
+  return wc6_sigma(D);
+}
+template<int D, int K>
+__device__ __forceinline__ double ff_gconst() {
+  if(K == FSPH_KERNEL_WENDLAND_C2)
+    return -20. * wc2_sigma(D);
+  if(K == FSPH_KERNEL_WENDLAND_C4)
+    return -56. / 3. * wc4_sigma(D);
+  return -22. * wc6_sigma(D);
+}
+
+// Pair geometry from the float-float positions: the separation (high words
+// exact, low words the difference of the residuals, so not normalised), its
+// FP32 rounding for the viscosity and signal speed, r^2 and r.
+template<int D>
+struct FFGeom {
+  ffloat dx[3];
+  float dxr[3];
+  float r2f;
+  ffloat r;
+};
+
+template<int D>
+__device__ __forceinline__ FFGeom<D> ff_geom(const float4 & pa, const float4 & la,
+  const float4 & pb, const float4 & lb) {
+  FFGeom<D> g;
+  g.dx[0] = ff_make(__fsub_rn(pa.x, pb.x), __fsub_rn(la.x, lb.x));
+  g.dx[1] = ff_make(__fsub_rn(pa.y, pb.y), __fsub_rn(la.y, lb.y));
+  g.dx[2] = D == 3 ? ff_make(__fsub_rn(pa.z, pb.z), __fsub_rn(la.z, lb.z))
+                   : ff_make(0.f, 0.f);
+  ffloat r2 = ff_add(ff_sqr_wide(g.dx[0]), ff_sqr_wide(g.dx[1]));
+  if(D == 3)
+    r2 = ff_add(r2, ff_sqr_wide(g.dx[2]));
+  r2 = ff_norm(r2);
+  g.r2f = r2.h;
+  for(int d = 0; d < 3; ++d)
+    g.dxr[d] = __fadd_rn(g.dx[d].h, g.dx[d].l);
+  g.r = ff_sqrt(r2);
+  return g;
+}
+
+// 1/h_ab and 1/h_ab^P for P = D or D + 2: the particle's own values when the
+// neighbour's h is the same (every pair of a uniform-h run), else from
+// h_a + h_b.
+template<int P>
+__device__ __forceinline__ ffloat ff_ipow(ffloat ih) {
+  const ffloat i2 = ff_sqr(ih);
+  if(P == 2)
+    return i2;
+  if(P == 3)
+    return ff_mul(i2, ih);
+  const ffloat i4 = ff_sqr(i2);
+  if(P == 4)
+    return i4;
+  return ff_mul(i4, ih);  // P == 5
+}
+
+template<int D, int K, bool CULL>
+__global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
+  PhysParams pp, Lists Ls, Packed Kp, double * cs_new, DevStatus * st,
+  const DevTime * tm) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const float4 pa = Kp.fph[a], la = Kp.fpl[a];
+  const ffloat iha = ff_rcp_scaled(ff_make(pa.w, la.w), 1.f);
+  const ffloat ihDa = ff_ipow<D>(iha);
+  const int cnt = Ls.cnt[a];
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  ffloat sum = ff_make(0.f, 0.f);
+  double gsum[3] = {0.0, 0.0, 0.0};
+  double pa64[3] = {0.0, 0.0, 0.0}, h_a = 0.0;
+  if(CULL) {
+    for(int d = 0; d < D; ++d)
+      pa64[d] = P.f[F_X + d][a];
+    h_a = P.f[F_H][a];
+  }
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const float4 pb = Kp.fph[b], lb = Kp.fpl[b];
+      const float2 mb = Kp.fm[b];
+      const FFGeom<D> g = ff_geom<D>(pa, la, pb, lb);
+      ffloat ih = iha, ihD = ihDa;
+      if(pb.w != pa.w || lb.w != la.w) {
+        ih = ff_rcp_scaled(ff_add(ff_make(pa.w, la.w), ff_make(pb.w, lb.w)), 2.f);
+        ihD = ff_ipow<D>(ih);
+      }
+      const ffloat q = ff_mul(g.r, ih);
+      const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
+      ffloat w = ff_mul(ff_mul(ff_wpoly<K>(t), ihD), ff_make(mb.x, mb.y));
+      if(!(q.h < 1.f) || j0 + u >= cnt)
+        w = ff_make(0.f, 0.f);
+      ff_acc(sum, w);
+      if(CULL) {
+        double pos_ab[3] = {0.0, 0.0, 0.0}, DiW[3];
+        for(int d = 0; d < D; ++d)
+          pos_ab[d] = pa64[d] - P.f[F_X + d][b];
+        kgrad<D, K>(pos_ab, .5 * (h_a + P.f[F_H][b]), DiW, pp);
+        const double mbd = P.f[F_M][b];
+        for(int d = 0; d < D; ++d)
+          gsum[d] += mbd * DiW[d];
+      }
+    }
+  }
+  const double iE = Kp.fscale[1];
+  const double iED = D == 3 ? iE * iE * iE : iE * iE;
+  const double rho = ff_wconst<D, K>() * iED * ff_to_double(sum);
+  if(!(rho > 0)) {
+    if(atomicCAS(&st->code, 0, (int)FSPH_ERR_NEG_DENSITY) == 0)
+      st->index = a;
+  }
+  P.f[F_RHO][a] = rho;
+  double u = P.f[F_U][a];
+  if(pp.evolve_u && pp.thermokinetic) {
+    double vv = 0;
+    for(int d = 0; d < D; ++d)
+      vv += P.f[F_VX + d][a] * P.f[F_VX + d][a];
+    double eint = P.f[F_E][a] - .5 * vv - ext_potential_of<D>(pp, P.f, a);
+    if(!(eint > 0)) {
+      if(atomicCAS(&st->code, 0, (int)FSPH_ERR_NEG_ENERGY) == 0)
+        st->index = a;
+    }
+    u = eint;
+    P.f[F_U][a] = u;
+  }
+  double Pa, cs;
+  eos_p_cs(pp, rho, u, P.f[F_K][a], P.f[F_YE][a], P.f[F_P][a], P.f[F_CS][a], Pa, cs);
+  P.f[F_P][a] = Pa;
+  cs_new[a] = cs;
+  const double A = Pa / (rho * rho);
+  Kp.thermo[a] = make_float4((float)rho, (float)A, (float)cs, (float)P.f[F_CS][a]);
+  const float Ah = (float)A;
+  Kp.fA[a] = make_float2(Ah, (float)(A - (double)Ah));
+  if(CULL) {
+    double div_v = 0.0;
+    for(int d = 0; d < D; ++d)
+      div_v += P.f[F_VX + d][a] * gsum[d];
+    div_v /= rho;
+    P.f[F_DDIVVDT][a] = (div_v - P.f[F_DIVV][a]) / tm->dt;
+    P.f[F_DIVV][a] = div_v;
+  }
+}
+
+// Acceleration with the pressure-gradient sum in float-float:
+//   a_a = -sum_b m_b (P_a/rho_a^2 + P_b/rho_b^2 + Pi_ab) grad_a W_ab
+// and, with VSIG, the signal speed of the density pass (FP32, as
+// k_vsig_mixed).
+template<int D, int K, bool VSIG, bool CULL>
+__global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
+  PhysParams pp, Lists Ls, Packed Kp, int kick, const DevTime * tm) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const float eps = (float)pp.eps, alpha = (float)pp.alpha, beta = (float)pp.beta;
+  const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
+  const float4 pa = Kp.fph[a], la = Kp.fpl[a];
+  const float2 Aa2 = Kp.fA[a];
+  const ffloat Aa = ff_make(Aa2.x, Aa2.y);
+  const ffloat iha = ff_rcp_scaled(ff_make(pa.w, la.w), 1.f);
+  const ffloat ihPa = ff_ipow<D + 2>(iha);
+  const float4 vha = Kp.vhm[a];
+  const float4 ta = Kp.thermo[a];
+  const int cnt = Ls.cnt[a];
+  float4 va = make_float4(0.f, 0.f, 0.f, 0.f);
+  if(VSIG)
+    va = Kp.vel[a];
+  float vsig = 0.f;
+  ffloat sx = ff_make(0.f, 0.f), sy = sx, sz = sx;
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll 2
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const float4 pb = Kp.fph[b], lb = Kp.fpl[b];
+      const FFGeom<D> g = ff_geom<D>(pa, la, pb, lb);
+      ffloat ih = iha, ihP = ihPa;
+      if(pb.w != pa.w || lb.w != la.w) {
+        ih = ff_rcp_scaled(ff_add(ff_make(pa.w, la.w), ff_make(pb.w, lb.w)), 2.f);
+        ihP = ff_ipow<D + 2>(ih);
+      }
+      const ffloat q = ff_mul(g.r, ih);
+      const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
+      const float4 vhb = Kp.vhm[b];
+      const float4 tb = Kp.thermo[b];
+      const float2 mb = Kp.fm[b];
+      const float2 Ab = Kp.fA[b];
+      // viscosity in FP32 (the position unit cancels in mu)
+      const float hab = 0.5f * (pa.w + pb.w);
+      const float dotp = (vha.x - vhb.x) * g.dxr[0] + (vha.y - vhb.y) * g.dxr[1] +
+                         (vha.z - vhb.z) * g.dxr[2];
+      const float mu = dotp < 0.f ? hab * dotp / (g.r2f + eps * hab * hab) : 0.f;
+      const float rho_ab = 0.5f * (ta.x + tb.x);
+      const float c_ab = 0.5f * (ta.z + tb.z);
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
+      ffloat S = ff_add_f(ff_add(Aa, ff_make(Ab.x, Ab.y)), Pi);
+      S = ff_mul(ff_mul(ff_mul(S, ff_make(mb.x, mb.y)), ihP), ff_gpoly<K>(t));
+      if(!(q.h < 1.f))
+        S = ff_make(0.f, 0.f);
+      if(VSIG) {
+        const float4 vb = Kp.vel[b];
+        const float dotv = ((va.x - vb.x) * g.dxr[0] + (va.y - vb.y) * g.dxr[1] +
+                             (va.z - vb.z) * g.dxr[2]) * rsqrtf(g.r2f);
+        const float cb = b > a ? tb.z : tb.w;
+        const float cand = fmaxf(ta.z, cb) - fminf(dotv, 0.f);
+        vsig = fmaxf(vsig, (b != a && g.r2f > 0.f) ? cand : 0.f);
+      }
+      // padding slots and the self pair have dx = 0 and add nothing
+      ff_acc(sx, ff_mul(S, g.dx[0]));
+      ff_acc(sy, ff_mul(S, g.dx[1]));
+      if(D == 3)
+        ff_acc(sz, ff_mul(S, g.dx[2]));
+    }
+  }
+  const double iE = Kp.fscale[1];
+  const double iE2 = iE * iE;
+  // a = -gconst / E^(D+1) * sum
+  const double scale = -ff_gconst<D, K>() * (D == 3 ? iE2 * iE2 : iE2 * iE);
+  double acc[3] = {scale * ff_to_double(sx), scale * ff_to_double(sy),
+    D == 3 ? scale * ff_to_double(sz) : 0.0};
+  if(pp.has_eacc) {  // acc_a += external_force::acceleration (:404)
+    const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
+    double ext[3];
+    ext_acceleration<D>(pp, pos, ext);
+    for(int d = 0; d < D; ++d)
+      acc[d] += ext[d];
+  }
+  const double half_dt = kick ? 0.5 * tm->dt : 0.0;
+  for(int d = 0; d < D; ++d) {
+    P.f[F_AX + d][a] = acc[d];
+    P.f[F_GAX + d][a] = 0.0;
+    if(kick)
+      P.f[F_VX + d][a] = P.f[F_VX + d][a] + acc[d] * half_dt;
+  }
+  P.f[F_GPOT][a] = 0.0;
+  if(VSIG)
+    P.f[F_VSIG][a] = (double)vsig;
+}
+
 // ------------------------------------------------------------ dispatch --
 #define MIX_DISPATCH(KERNEL_T, TA, ...)                                            \
   do {                                                                         \
@@ -597,11 +899,43 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_mixed(Particles P,
 
 // Launch the pair kernels of one viscosity choice for the step's dimension
 // and smoothing kernel.
+// The float-float passes serve the Wendland kernels; the other kernels
+// (cubic and quintic splines, Gaussians, sinc) keep the FP32 passes.
+#define FF_DISPATCH(KERNEL_T, TA, ...)                                         \
+  do {                                                                         \
+    const int nb_ = (P.n + MIX_THREADS - 1) / MIX_THREADS;                     \
+    if(pp.dim == 3) {                                                          \
+      if(pp.kernel == FSPH_KERNEL_WENDLAND_C2)                                 \
+        KERNEL_T<3, FSPH_KERNEL_WENDLAND_C2, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+      else if(pp.kernel == FSPH_KERNEL_WENDLAND_C4)                            \
+        KERNEL_T<3, FSPH_KERNEL_WENDLAND_C4, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+      else                                                                     \
+        KERNEL_T<3, FSPH_KERNEL_WENDLAND_C6, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+    }                                                                          \
+    else {                                                                     \
+      if(pp.kernel == FSPH_KERNEL_WENDLAND_C2)                                 \
+        KERNEL_T<2, FSPH_KERNEL_WENDLAND_C2, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+      else if(pp.kernel == FSPH_KERNEL_WENDLAND_C4)                            \
+        KERNEL_T<2, FSPH_KERNEL_WENDLAND_C4, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+      else                                                                     \
+        KERNEL_T<2, FSPH_KERNEL_WENDLAND_C6, TA><<<nb_, MIX_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+    }                                                                          \
+    *L.counter += 1;                                                           \
+  } while(0)
+
+inline bool wendland_kernel(int k) {
+  return k == FSPH_KERNEL_WENDLAND_C2 || k == FSPH_KERNEL_WENDLAND_C4 ||
+         k == FSPH_KERNEL_WENDLAND_C6;
+}
+
 template<bool CULL>
 inline void run_density_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
   DevStatus * st, const DevTime * tm) {
-  MIX_DISPATCH(k_density_mixed, CULL, P, pp, Ls, K, cs_new, st, tm);
+  if(wendland_kernel(pp.kernel))
+    FF_DISPATCH(k_density_ff, CULL, P, pp, Ls, K, cs_new, st, tm);
+  else
+    MIX_DISPATCH(k_density_mixed, CULL, P, pp, Ls, K, cs_new, st, tm);
 }
 
 template<bool CULL>
@@ -648,6 +982,21 @@ inline void run_accel_mixed(const Launch & L, const Particles & P,
       case FSPH_KERNEL_WENDLAND_C2: PICK(2, FSPH_KERNEL_WENDLAND_C2); break;
       case FSPH_KERNEL_WENDLAND_C4: PICK(2, FSPH_KERNEL_WENDLAND_C4); break;
       default: PICK(2, FSPH_KERNEL_WENDLAND_C6); break;
+    }
+  }
+#undef PICK
+#define PICK(D, KK)                                                            \
+  fn = fused_vsig ? k_accel_ff<D, KK, true, CULL> : k_accel_ff<D, KK, false, CULL>
+  if(wendland_kernel(pp.kernel)) {
+    if(pp.dim == 3) {
+      if(pp.kernel == FSPH_KERNEL_WENDLAND_C2) PICK(3, FSPH_KERNEL_WENDLAND_C2);
+      else if(pp.kernel == FSPH_KERNEL_WENDLAND_C4) PICK(3, FSPH_KERNEL_WENDLAND_C4);
+      else PICK(3, FSPH_KERNEL_WENDLAND_C6);
+    }
+    else {
+      if(pp.kernel == FSPH_KERNEL_WENDLAND_C2) PICK(2, FSPH_KERNEL_WENDLAND_C2);
+      else if(pp.kernel == FSPH_KERNEL_WENDLAND_C4) PICK(2, FSPH_KERNEL_WENDLAND_C4);
+      else PICK(2, FSPH_KERNEL_WENDLAND_C6);
     }
   }
 #undef PICK

@@ -1274,13 +1274,17 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
                         (size_t)NB_WARPS * NB_STACK * 4;
   const size_t smem_u = (size_t)NB_WARPS * NB_CAND * 20 +
                         (size_t)NB_WARPS * NB_STACK * 4;
-  static unsigned long long attr_devices = 0;
-  if(first_on_device(&attr_devices)) {
-    cudaFuncSetAttribute(k_neighbors<true>,
+  static std::atomic<unsigned long long> attr_devices{0};
+  cudaError_t ae = once_per_device(&attr_devices, [&]() {
+    cudaError_t e = cudaFuncSetAttribute(k_neighbors<true>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
-    cudaFuncSetAttribute(k_neighbors<false>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
-  }
+    if(e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_neighbors<false>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
+    return e;
+  });
+  if(ae != cudaSuccess)
+    return ae;
   int blocks = nsm * (ordered ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM);
   int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
   if(blocks > maxb)

@@ -406,12 +406,21 @@ fsph_status fsph_mark_elapsed(fsph_ctx * ctx, int32_t from, int32_t to,
  * and every call shares it: calls that overlap on the GPU (other streams,
  * other threads) race and must be serialised by the caller.  The first call
  * on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  Nothing is allocated. */
+ * make that first call before any stream capture.  That address is kept for
+ * the life of the process: do not call this entry point again on a device
+ * after cudaDeviceReset (or any teardown of its primary context), which can
+ * move the array.  Nothing is allocated.  Two differences from
+ * fsph_update_iteration: equal keys keep their input order (the tie-break
+ * is the input index; the reference's comparator, bodies_system.h:195-206,
+ * breaks ties by id, which is the same order when ids ascend with the
+ * input), and duplicate full keys are not reported (no
+ * FSPH_ERR_DUPLICATE_KEY: the status word would need a synchronisation). */
 fsph_status fsph_sort_keys_noalloc(const double * x, const double * y,
   const double * z, const double * h, int64_t n, int32_t dimension,
   uint64_t * keys_out, int32_t * perm_out, void * stream);
 /* Measured arithmetic peak of `device`: kind 0 = FP64 FMA, 1 = FP32 FMA,
- * in TFLOP/s (2 flops per FMA), from a register-resident FMA chain kernel. */
+ * 2 = FP32 FMA through the packed FP32x2 instruction, in TFLOP/s (2 flops
+ * per FMA), from a register-resident FMA chain kernel. */
 fsph_status fsph_measure_peak(int32_t device, int32_t kind, double * tflops);
 
 /* -- ensembles ----------------------------------------------------------- */

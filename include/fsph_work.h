@@ -1,8 +1,12 @@
 /*
- * fsph_work.h -- the fixed algorithmic work model of the SPH step, used for
- * the roofline fractions reported by bench.py.  The same table applies to
- * both precisions: extra operations of compensated summation, of the exact
- * neighbour predicate or of recomputation are not counted as useful work.
+ * fsph_work.h -- the fixed algorithmic work model of the SPH step.  The
+ * roofline fractions bench.py reports are computed from these constants
+ * (bench.py parses this file), and nothing else: the same table serves both
+ * precisions, because extra operations of compensated or float-float
+ * arithmetic, of the exact neighbour predicate, of recomputation, or bytes
+ * an implementation moves beyond the compulsory ones are not useful work.
+ * What an implementation really moves is reported beside it as `traffic`
+ * (ncu dram bytes).
  *
  * Flops per neighbour pair count +, -, *, /, sqrt as one each, as the
  * reference writes the pair terms (include/physics/default_physics.h,
@@ -19,13 +23,29 @@
 #define FSPH_FLOPS_PAIR_P2P 22       /* gravity particle-particle            */
 #define FSPH_FLOPS_PAIR_M2P_QUAD 62  /* monopole 22 + quadrupole 40          */
 
-/* Compulsory HBM bytes per particle and step (every field read or written
- * once per kernel, neighbour re-reads served from cache):
- *   range+keys 40, sort (key,id) 32 + permute 272, tree 48, density 72,
- *   acceleration 120, de/dt 112, kicks/drift 288, dt 80, lists 4*N_nb*5 */
-#define FSPH_BYTES_PARTICLE_STEP_FP64 1100
+/* Compulsory HBM bytes per particle and step, by phase: FP64 SoA in 3D,
+ * every field read or written once per kernel, neighbour re-reads served
+ * from cache.  The state is FP64 in both precision modes. */
+#define FSPH_BYTES_RANGE_KEYS 40     /* x, y, z, h read; key written          */
+#define FSPH_BYTES_SORT 304          /* (key, id) 2 x 16 + permute 2 x 17 x 8 */
+#define FSPH_BYTES_TREE 48
+#define FSPH_BYTES_NEIGHBORS 40      /* x, y, z, h read; count written       */
+#define FSPH_BYTES_DENSITY 72        /* 40 in + 32 out                       */
+#define FSPH_BYTES_ACCEL 120         /* 96 in + 24 out                       */
+#define FSPH_BYTES_DEDT 112          /* 104 in + 8 out                       */
+#define FSPH_BYTES_RECOMPUTE_P 40
+#define FSPH_BYTES_INTEGRATE 288     /* kicks, drift, v_half: 3 x 96         */
+#define FSPH_BYTES_DT 80
+/* the neighbour list: one int per pair, written by the walk and read by
+ * each pair pass */
+#define FSPH_BYTES_PAIR_LIST 4
+
+/* totals per particle-step (hydro, thermokinetic) */
+#define FSPH_BYTES_PARTICLE_STEP_FP64 1104
+/* ...and if non-position fields were stored in FP32 (not done here: the
+ * leapfrog state stays FP64) */
 #define FSPH_BYTES_PARTICLE_STEP_MIXED 650
-/* neighbour list traffic: one int per pair written once, read by 4 passes */
+/* list traffic per pair and step: written once, read by 4 passes */
 #define FSPH_BYTES_PAIR_LISTS 20
 
 #endif

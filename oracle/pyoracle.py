@@ -28,8 +28,17 @@ def build_port():
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
 
 
-def build_ref(ref_root="/root/reference"):
-    if not os.path.isdir(ref_root):
+def reference_root():
+    """Where the reference's sources are: $FSPH_REFERENCE, else a checkout
+    named `reference` beside this repository; None when neither exists."""
+    cand = os.environ.get("FSPH_REFERENCE") or os.path.join(
+        os.path.dirname(os.path.dirname(HERE)), "reference")
+    return cand if os.path.isdir(cand) else None
+
+
+def build_ref(ref_root=None):
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return True

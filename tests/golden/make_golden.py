@@ -76,6 +76,22 @@ def cases():
     s, p, m = setups.kh3d(12)
     p.periodic_boundary_y = p.periodic_boundary_z = 0
     yield "kh3d_periodic_x_1728", setups.shuffled(_outside(s), 8), p, 2
+    # the driver's energy branches (hydro/main_driver.cc:145-171,214-240):
+    # two pressure updates per step, and no energy evolution
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.pressure_updates_number = 2
+    yield "sod3d_pu2_4000", setups.shuffled(s, 30), p, 2
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.thermokinetic_formulation = 0
+    p.pressure_updates_number = 2
+    yield "sod3d_dudt_pu2_4000", setups.shuffled(s, 31), p, 2
+    s, p, m = setups.sod3d(40, 10, 10)
+    p.evolve_internal_energy = 0
+    yield "sod3d_noevolve_4000", setups.shuffled(s, 32), p, 2
+    s, p, m = setups.sod2d(100, 10)
+    p.thermokinetic_formulation = 0
+    p.evolve_internal_energy = 0
+    yield "sod2d_noevolve_dudt_1000", setups.shuffled(s, 33), p, 2
 
 
 def eos_cases():
@@ -114,8 +130,8 @@ def main():
         k = args.index("--only")
         only = set(args[k + 1:])
         args = args[:k]
-    ref_root = args[0] if args else "/root/reference"
-    if not pyoracle.build_ref(ref_root):
+    ref_root = args[0] if args else pyoracle.reference_root()
+    if not ref_root or not pyoracle.build_ref(ref_root):
         sys.exit(f"reference sources not found at {ref_root}")
     for name, state, params, steps in cases():
         if only is not None and name not in only:

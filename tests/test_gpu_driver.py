@@ -73,3 +73,107 @@ def test_cpp_driver_relaxation_and_external_force(tmp_path):
     assert np.array_equal(out["id"], ref["id"])
     for f in DOUBLE_FIELDS:
         assert np.array_equal(out[f], ref[f]), f
+
+
+def _driver_args(p, extra=()):
+    return [f"sph_kernel={p.sph_kernel}", f"poly_gamma={p.poly_gamma!r}",
+            f"sph_eta={p.sph_eta!r}", f"adaptive_timestep={p.adaptive_timestep}",
+            f"initial_dt={p.initial_dt!r}",
+            f"thermokinetic_formulation={p.thermokinetic_formulation}",
+            f"evolve_internal_energy={p.evolve_internal_energy}",
+            f"pressure_updates_number={p.pressure_updates_number}", *extra]
+
+
+@pytest.mark.parametrize("thermo,evolve,updates", [(1, 1, 2), (0, 1, 2), (1, 0, 1),
+                                                   (0, 0, 1)])
+def test_cpp_driver_energy_branches(tmp_path, thermo, evolve, updates):
+    """The driver's energy branches (hydro/main_driver.cc:145-171,214-240):
+    two pressure updates per step, or no energy evolution, in both energy
+    formulations, equal to the fused step bit for bit (which the golden
+    fixtures sod3d_pu2, sod3d_dudt_pu2, sod3d_noevolve and
+    sod2d_noevolve_dudt pin against the reference)."""
+    build.build()
+    from flecsph_gb300.sph import BodySystem
+    s, p, meta = setups.sod3d(40, 10, 10)
+    p.adaptive_timestep, p.initial_dt = 1, 1e-12
+    p.thermokinetic_formulation, p.evolve_internal_energy = thermo, evolve
+    p.pressure_updates_number = updates
+    s = setups.shuffled(s, 24)
+    src, dst = tmp_path / "in.bin", tmp_path / "out.bin"
+    snapshot.write(src, s, 3)
+    r = subprocess.run([build.DRIVER, str(src), str(dst), "3", *_driver_args(p)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out, dim = snapshot.read(dst)
+    bs = BodySystem(p, meta["n"])
+    bs.read_bodies(s)
+    for _ in range(3):
+        bs.step()
+    ref = bs.download()
+    bs.close()
+    assert np.array_equal(out["id"], ref["id"])
+    for f in DOUBLE_FIELDS:
+        assert np.array_equal(out[f], ref[f]), f
+
+
+def test_cpp_driver_restart(tmp_path):
+    """A run split in two: the first part's snapshot carries (iteration, dt,
+    time); the second part restarts from it at that iteration with the
+    driver's initial-iteration branch and the restored dt and time, as the
+    reference's read_bodies(..., initial_iteration) does
+    (mpisph/io.h:523-586,818-836).  The restarted run equals the same
+    restart of the oracle to 1e-12, and of the fused step bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__))), "oracle"))
+    import pyoracle
+    build.build()
+    pyoracle.build_port()
+    from flecsph_gb300.sph import BodySystem
+    s, p, meta = setups.sod3d(40, 10, 10)
+    p.adaptive_timestep, p.initial_dt = 1, 1e-12
+    s = setups.shuffled(s, 25)
+    src, mid, dst = tmp_path / "in.bin", tmp_path / "mid.bin", tmp_path / "out.bin"
+    snapshot.write(src, s, 3)
+    r = subprocess.run([build.DRIVER, str(src), str(mid), "2", *_driver_args(p)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    st_mid, dim, tm = snapshot.read(mid, with_time=True)
+    assert tm[0] == 2 and tm[1] > 0 and tm[2] > 0
+    # a mismatching initial_iteration is refused, as the reference stops
+    # when no snapshot holds that iteration
+    r = subprocess.run([build.DRIVER, str(mid), str(dst), "3",
+                        *_driver_args(p, ["initial_iteration=7"])],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 2 and "initial_iteration" in r.stderr
+    r = subprocess.run([build.DRIVER, str(mid), str(dst), "3",
+                        *_driver_args(p, ["initial_iteration=2"])],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out, dim, tm_out = snapshot.read(dst, with_time=True)
+    assert tm_out[0] == 5
+    # the same restart through the fused step and through the oracle
+    p.initial_iteration = 2
+    bs = BodySystem(p, meta["n"])
+    bs.read_bodies(st_mid)
+    bs.set_time(tm[1], tm[2], tm[0])
+    for _ in range(3):
+        bs.step()
+    ref = bs.download()
+    dt, t, it = bs.time()
+    bs.close()
+    assert (it, dt, t) == tm_out
+    assert np.array_equal(out["id"], ref["id"])
+    for f in DOUBLE_FIELDS:
+        assert np.array_equal(out[f], ref[f]), f
+    o = pyoracle.Oracle("port", p, threads=4)
+    o.upload(st_mid)
+    o.set_time(tm[1], tm[2], tm[0])
+    for _ in range(3):
+        o.step()
+    oref = o.download()
+    o.close()
+    assert np.array_equal(out["id"], oref["id"])
+    for f in DOUBLE_FIELDS:
+        scale = max(np.abs(oref[f]).max(), 1e-300)
+        assert np.abs(out[f] - oref[f]).max() <= 1e-12 * scale, f

@@ -1,16 +1,16 @@
-"""Mixed-precision path (FP32 pair arithmetic, Kahan sums, FP64 state)
-against the plain FP64 path on identical inputs.
+"""Mixed-precision path (FP32 pair arithmetic with float-float pressure
+and density sums, FP64 state) against the plain FP64 path on identical
+inputs.
 
 Bars: neighbour lists identical to the FP64 path (the FP32 predicate filter
 falls back to the exact FP64 test near the boundary); relative acceleration
-error |a_mixed - a_fp64| / max(|a_fp64|, 1e-3 rms|a_fp64|) <= 1e-5 (the
-stated target); density within 1e-6 relative; de/dt within 1e-5 normwise.
-
-On the perfect Sod lattice the pressure forces of most particles cancel to
-~1e-14 in FP64 while single-precision rounding leaves ~1e-6 of one pair
-term, so a per-particle relative error has no meaning there; that case is
-gated normwise (max |delta a| / max |a|).  A smooth velocity field is added
-so that the viscosity and de/dt terms are exercised."""
+error |a_mixed - a_fp64| / max(|a_fp64|, 1e-3 rms|a_fp64|) <= 1e-5 for EVERY
+particle (the stated target), including the lattices (Sod, KH), where the
+pressure terms of interior particles cancel to ~1e-13 of one term in FP64
+and plain FP32 pair sums missed the bar by 100x; density within 1e-10
+relative (float-float density sum); de/dt (FP32 pair terms) within 1e-5
+normwise.  A smooth velocity field is added so that the viscosity and de/dt
+terms are exercised."""
 import numpy as np
 import pytest
 
@@ -20,7 +20,7 @@ from flecsph_gb300.abi import PRECISION_FP64, PRECISION_MIXED
 pytestmark = pytest.mark.gpu
 
 ACCEL_TOL = 1e-5
-RHO_TOL = 1e-6
+RHO_TOL = 1e-10
 DEDT_TOL = 1e-5
 
 
@@ -54,7 +54,7 @@ def accel_err(a, b):
     return np.linalg.norm(A - B, axis=1) / np.maximum(mag, 1e-3 * rms)
 
 
-@pytest.mark.parametrize("problem", ["sod", "sedov", "polytrope", "kh"])
+@pytest.mark.parametrize("problem", ["sod", "sedov", "polytrope", "polytrope262k", "kh"])
 def test_mixed_matches_fp64(problem):
     if problem == "sod":
         s, p, m = setups.sod3d(40, 10, 10)
@@ -62,6 +62,10 @@ def test_mixed_matches_fp64(problem):
         s, p, m = setups.sedov3d(32)
     elif problem == "kh":
         s, p, m = setups.kh3d(24)   # periodic copies on every axis
+    elif problem == "polytrope262k":
+        s, p, m = setups.polytrope3d(1 << 18, rho_floor=1e-2)
+        p.enable_fmm = 0
+        p.max_neighbors = 512
     else:
         s, p, m = setups.polytrope3d(20000)
         p.enable_fmm = 0
@@ -87,12 +91,8 @@ def test_mixed_matches_fp64(problem):
     normwise = np.abs(AMX - A64).max() / np.abs(A64).max()
     print(problem, "accel rel err max", e.max(), "median", np.median(e),
           "normwise", normwise, "rho", rho_err.max())
-    if problem in ("sod", "kh"):
-        # lattices: interior accelerations cancel to ~0, so the bound is
-        # normwise there
-        assert normwise <= ACCEL_TOL, normwise
-    else:
-        assert e.max() <= ACCEL_TOL, e.max()
+    assert e.max() <= ACCEL_TOL, (e.max(), np.median(e), normwise)
+    assert np.abs(r64["dedt"]).max() > 0
     dedt = np.abs(rmx["dedt"] - r64["dedt"]).max() / np.abs(r64["dedt"]).max()
     assert dedt <= DEDT_TOL, dedt
 
