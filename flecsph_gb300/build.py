@@ -40,10 +40,17 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
+def _tuning_defines():
+    """-D flags from $FSPH_NVCC_DEFINES ("NAME=VALUE NAME2=VALUE2"): launch-shape
+    knobs of the kernels (FSPH_ACCEL_FF_BLOCKS), for tuning runs; empty for
+    the default build."""
+    return ["-D" + d for d in os.environ.get("FSPH_NVCC_DEFINES", "").split() if d]
+
+
 def _compile(src, extra, verbose):
     obj = os.path.join(BUILD, src.replace(".cu", ".o"))
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xptxas", "-v" if verbose else "-O3", *extra, "-c",
+           "-Xptxas", "-v" if verbose else "-O3", *_tuning_defines(), *extra, "-c",
            os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -489,9 +489,11 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;
   ok &= dalloc(c, &c->K.fph, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.fpl, N) == cudaSuccess;
-  ok &= dalloc(c, &c->K.fm, N) == cudaSuccess;
-  ok &= dalloc(c, &c->K.fA, N) == cudaSuccess;
-  ok &= dalloc(c, &c->K.fscale, 2) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fmA, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fscale, 3) == cudaSuccess;
+  // (c->mixed is set further down: decide from the parameters)
+  if(p->precision_mode == FSPH_PRECISION_MIXED)
+    ok &= dalloc(c, &c->K.ahyd, 3 * N) == cudaSuccess;
   c->periodic = p->periodic_boundary_x || p->periodic_boundary_y ||
                 p->periodic_boundary_z;
   if(c->periodic) {
@@ -559,6 +561,7 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   if(!c || !v || v->n < 2 || v->n > c->cap || !v->x || !v->y ||
      (c->p.dimension == 3 && !v->z) || !v->m || !v->h || !v->id)
     return FSPH_ERR_ARG;
+  c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -606,6 +609,7 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
 fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
   if(!c || !v || !c->uploaded || v->n != c->n)
     return FSPH_ERR_ARG;
+  c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -767,6 +771,7 @@ fsph_status fsph_get_range(fsph_ctx * c, double * range) {
 fsph_status fsph_update_iteration(fsph_ctx * c) {
   if(!c || !c->uploaded)
     return FSPH_ERR_STATE;
+  c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -851,6 +856,7 @@ fsph_status fsph_compute_alpha(fsph_ctx * c) {
     c->last_error = "compute_alpha needs sph_viscosity = visc_cullen";
     return FSPH_ERR_STATE;
   }
+  c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -866,6 +872,7 @@ fsph_status fsph_compute_alpha(fsph_ctx * c) {
 static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
+  c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -900,6 +907,11 @@ fsph_status fsph_density_pressure_soundspeed(fsph_ctx * c) {
   return density_impl(c, true);
 }
 
+static bool wendland(int k) {
+  return k == FSPH_KERNEL_WENDLAND_C2 || k == FSPH_KERNEL_WENDLAND_C4 ||
+         k == FSPH_KERNEL_WENDLAND_C6;
+}
+
 static fsph_status accel_impl(fsph_ctx * c, int kick, int fused_vsig = 0) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
@@ -912,6 +924,9 @@ static fsph_status accel_impl(fsph_ctx * c, int kick, int fused_vsig = 0) {
     CK(launch_accel_mixed(L, c->P, c->pp, c->Ls, c->K, kick, c->d_time, fused_vsig));
   else
     CK(launch_accel_fp64(L, c->P, c->pp, c->Ls, kick, c->d_time));
+  // the float-float pass (Wendland kernels) leaves the pressure-only
+  // acceleration in K.ahyd for the de/dt pass
+  c->ahyd_ok = c->mixed && c->K.ahyd && wendland(c->pp.kernel);
   return FSPH_OK;
 }
 
@@ -941,7 +956,8 @@ fsph_status fsph_dedt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
-    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, 0, c->d_time, c->d_status));
+    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, 0, c->d_time, c->d_status,
+      c->ahyd_ok ? 1 : 0));
   else
     CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
   return FSPH_OK;
@@ -964,9 +980,12 @@ static fsph_status energy_then(fsph_ctx * c, bool thermo, int op) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(thermo)
-    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status));
+    CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status,
+      c->ahyd_ok ? 1 : 0));
   else
     CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, op));
+  // the pressure update of `op` changes P/rho^2
+  c->ahyd_ok = false;
   return FSPH_OK;
 }
 
@@ -997,6 +1016,12 @@ fsph_status fsph_add_short_range_repulsion(fsph_ctx * c) {
 static fsph_status elem(fsph_ctx * c, int op, int phase) {
   if(!c || !c->uploaded)
     return FSPH_ERR_STATE;
+  // every update of positions, P/rho^2, v_half, alpha or h outdates the
+  // pressure-only acceleration the de/dt pass would reuse
+  if(op != OP_KICK_V && op != OP_KICK_E && op != OP_KICK_U &&
+     op != OP_SET_TOTAL_ENERGY && op != OP_DRAG_ACC && op != OP_DRAG_DEDT &&
+     op != OP_DRAG_DUDT && op != OP_CHECK_NANS && op != OP_CHECK_NEGATIVITY)
+    c->ahyd_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;

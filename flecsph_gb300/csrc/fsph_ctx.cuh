@@ -47,6 +47,10 @@ struct fsph_ctx {
   int64_t iteration = 0;
   unsigned permute_skip = 0;  // fields the next permute may leave behind
   bool tree_ok = false;
+  // K.ahyd holds the pressure-only acceleration of the current positions,
+  // P/rho^2, v_half and alpha (set by the float-float acceleration pass,
+  // cleared by every call that changes one of them)
+  bool ahyd_ok = false;
   bool uploaded = false;
   long long launches = 0;
   // timers

@@ -126,9 +126,14 @@ struct Packed {
   // h is in the same units.
   float4 * fph;     // {X_h, Y_h, Z_h, h_h}
   float4 * fpl;     // {X_l, Y_l, Z_l, h_l}
-  float2 * fm;      // {m_h, m_l}
-  float2 * fA;      // {(P/rho^2)_h, (P/rho^2)_l}
-  double * fscale;  // device [2]: E, 1 / E
+  float4 * fmA;     // {m_h, m_l, (P/rho^2)_h, (P/rho^2)_l}: m packed with the
+                    // positions, P/rho^2 by the density pass (two 8-byte halves)
+  double * fscale;  // device [3]: E, 1 / E, 1 if every h is equal (else 0)
+  // pressure-only hydro acceleration of the float-float pass,
+  // -sum_b m_b (P_a/rho_a^2 + P_b/rho_b^2) grad W, as three FP64 arrays of
+  // stride n: the de/dt pass rewrites its pressure terms with it while
+  // positions, P/rho^2, v_half and alpha are unchanged
+  double * ahyd;
 };
 
 // Multipole of a radix-tree node (FP64): mass, centre of mass, traceless
@@ -250,7 +255,7 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   int then_op);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st);
+  const DevTime * t, DevStatus * st, int use_ahyd);
 
 // ---- fsph_gravity.cu ----
 cudaError_t launch_gravity(const Launch & L, const Particles & P,

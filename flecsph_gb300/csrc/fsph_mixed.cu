@@ -37,6 +37,8 @@ __global__ void k_pack_pos(Particles P, int dim,
     if(blockIdx.x == 0) {
       K.fscale[0] = E;
       K.fscale[1] = s_iE;
+      // h_min == h_max: the pair passes take h_ab = h_a throughout
+      K.fscale[2] = rbits[6] == rbits[7] ? 1.0 : 0.0;
     }
   }
   __syncthreads();
@@ -67,7 +69,7 @@ __global__ void k_pack_pos(Particles P, int dim,
   K.fpl[i] = make_float4(xl[0], xl[1], xl[2], xl[3]);
   const double m = P.f[F_M][i];
   const float mh = (float)m;
-  K.fm[i] = make_float2(mh, (float)(m - (double)mh));
+  ((float2 *)K.fmA)[2 * i] = make_float2(mh, (float)(m - (double)mh));
 }
 
 // PACK_AV_IN: {c_s, sign(div v)} for the Cullen & Dehnen alpha pass;
@@ -97,7 +99,7 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
     const double A = P.f[F_P][i] / (rho * rho);
     K.thermo[i] = make_float4((float)rho, (float)A, (float)cs, (float)cs);
     const float Ah = (float)A;
-    K.fA[i] = make_float2(Ah, (float)(A - (double)Ah));
+    ((float2 *)K.fmA)[2 * i + 1] = make_float2(Ah, (float)(A - (double)Ah));
   }
   if(what & PACK_AV_IN) {
     // signnum_c of the reference (viscosity.h:63-67), taken in FP64
@@ -232,15 +234,15 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
 
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st) {
+  const DevTime * t, DevStatus * st, int use_ahyd) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
     PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
-    run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st);
+    run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st, use_ahyd);
   else
-    run_dedt_mixed<false>(L, P, pp, Ls, K, then_op, t, st);
+    run_dedt_mixed<false>(L, P, pp, Ls, K, then_op, t, st, use_ahyd);
   return cudaGetLastError();
 }
 

@@ -28,8 +28,8 @@ void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
 
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st) {
-  run_dedt_mixed<true>(L, P, pp, Ls, K, then_op, t, st);
+  const DevTime * t, DevStatus * st, int use_ahyd) {
+  run_dedt_mixed<true>(L, P, pp, Ls, K, then_op, t, st, use_ahyd);
 }
 
 // viscosity::compute_alpha with A_trigger and compute_xi (viscosity.h:

@@ -664,6 +664,42 @@ __device__ __forceinline__ ffloat ff_ipow(ffloat ih) {
   return ff_mul(i4, ih);  // P == 5
 }
 
+// The density sum of one particle: sum_b m_b wpoly(t_ab) / h_ab^D, or, with
+// UNI (every h equal), sum_b m_b wpoly(t_ab), the particle's 1/h^D applied
+// once afterwards.
+template<int D, int K, bool UNI>
+__device__ __forceinline__ ffloat density_ff_sum(const Packed & Kp, const int * lp,
+  int cnt, const float4 & pa, const float4 & la, const ffloat & iha,
+  const ffloat & ihDa) {
+  ffloat sum = ff_make(0.f, 0.f);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const float4 pb = Kp.fph[b], lb = Kp.fpl[b];
+      const float2 mb = ((const float2 *)Kp.fmA)[2 * b];
+      const FFGeom<D> g = ff_geom<D>(pa, la, pb, lb);
+      ffloat ih = iha, ihD = ihDa;
+      if(!UNI && (pb.w != pa.w || lb.w != la.w)) {
+        ih = ff_rcp_scaled(ff_add(ff_make(pa.w, la.w), ff_make(pb.w, lb.w)), 2.f);
+        ihD = ff_ipow<D>(ih);
+      }
+      const ffloat q = ff_mul(g.r, ih);
+      const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
+      ffloat w = ff_mul(ff_wpoly<K>(t), ff_make(mb.x, mb.y));
+      if(!UNI)
+        w = ff_mul(w, ihD);
+      if(!(q.h < 1.f) || j0 + u >= cnt)
+        w = ff_make(0.f, 0.f);
+      ff_acc(sum, w);
+    }
+  }
+  if(UNI)
+    sum = ff_mul(sum, ihDa);
+  return sum;
+}
+
 template<int D, int K, bool CULL>
 __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   PhysParams pp, Lists Ls, Packed Kp, double * cs_new, DevStatus * st,
@@ -676,42 +712,25 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   const ffloat ihDa = ff_ipow<D>(iha);
   const int cnt = Ls.cnt[a];
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
-  ffloat sum = ff_make(0.f, 0.f);
+  const ffloat sum = Kp.fscale[2] != 0.0
+                       ? density_ff_sum<D, K, true>(Kp, lp, cnt, pa, la, iha, ihDa)
+                       : density_ff_sum<D, K, false>(Kp, lp, cnt, pa, la, iha, ihDa);
   double gsum[3] = {0.0, 0.0, 0.0};
-  double pa64[3] = {0.0, 0.0, 0.0}, h_a = 0.0;
   if(CULL) {
+    // m_b grad_a W_ab for compute_divv, in FP64 (see k_density_mixed)
+    double pa64[3] = {0.0, 0.0, 0.0};
     for(int d = 0; d < D; ++d)
       pa64[d] = P.f[F_X + d][a];
-    h_a = P.f[F_H][a];
-  }
-  for(int j0 = 0; j0 < cnt; j0 += 4) {
-    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
-#pragma unroll
-    for(int u = 0; u < 4; ++u) {
-      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
-      const float4 pb = Kp.fph[b], lb = Kp.fpl[b];
-      const float2 mb = Kp.fm[b];
-      const FFGeom<D> g = ff_geom<D>(pa, la, pb, lb);
-      ffloat ih = iha, ihD = ihDa;
-      if(pb.w != pa.w || lb.w != la.w) {
-        ih = ff_rcp_scaled(ff_add(ff_make(pa.w, la.w), ff_make(pb.w, lb.w)), 2.f);
-        ihD = ff_ipow<D>(ih);
-      }
-      const ffloat q = ff_mul(g.r, ih);
-      const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
-      ffloat w = ff_mul(ff_mul(ff_wpoly<K>(t), ihD), ff_make(mb.x, mb.y));
-      if(!(q.h < 1.f) || j0 + u >= cnt)
-        w = ff_make(0.f, 0.f);
-      ff_acc(sum, w);
-      if(CULL) {
-        double pos_ab[3] = {0.0, 0.0, 0.0}, DiW[3];
-        for(int d = 0; d < D; ++d)
-          pos_ab[d] = pa64[d] - P.f[F_X + d][b];
-        kgrad<D, K>(pos_ab, .5 * (h_a + P.f[F_H][b]), DiW, pp);
-        const double mbd = P.f[F_M][b];
-        for(int d = 0; d < D; ++d)
-          gsum[d] += mbd * DiW[d];
-      }
+    const double h_a = P.f[F_H][a];
+    for(int j = 0; j < cnt; ++j) {
+      const int b = lp[slot_off(j)];
+      double pos_ab[3] = {0.0, 0.0, 0.0}, DiW[3];
+      for(int d = 0; d < D; ++d)
+        pos_ab[d] = pa64[d] - P.f[F_X + d][b];
+      kgrad<D, K>(pos_ab, .5 * (h_a + P.f[F_H][b]), DiW, pp);
+      const double mbd = P.f[F_M][b];
+      for(int d = 0; d < D; ++d)
+        gsum[d] += mbd * DiW[d];
     }
   }
   const double iE = Kp.fscale[1];
@@ -742,7 +761,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   const double A = Pa / (rho * rho);
   Kp.thermo[a] = make_float4((float)rho, (float)A, (float)cs, (float)P.f[F_CS][a]);
   const float Ah = (float)A;
-  Kp.fA[a] = make_float2(Ah, (float)(A - (double)Ah));
+  ((float2 *)Kp.fmA)[2 * a + 1] = make_float2(Ah, (float)(A - (double)Ah));
   if(CULL) {
     double div_v = 0.0;
     for(int d = 0; d < D; ++d)
@@ -756,29 +775,25 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
 // Acceleration with the pressure-gradient sum in float-float:
 //   a_a = -sum_b m_b (P_a/rho_a^2 + P_b/rho_b^2 + Pi_ab) grad_a W_ab
 // and, with VSIG, the signal speed of the density pass (FP32, as
-// k_vsig_mixed).
-template<int D, int K, bool VSIG, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
-  PhysParams pp, Lists Ls, Packed Kp, int kick, const DevTime * tm) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if(a >= P.n)
-    return;
-  const float eps = (float)pp.eps, alpha = (float)pp.alpha, beta = (float)pp.beta;
-  const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
-  const float4 pa = Kp.fph[a], la = Kp.fpl[a];
-  const float2 Aa2 = Kp.fA[a];
-  const ffloat Aa = ff_make(Aa2.x, Aa2.y);
-  const ffloat iha = ff_rcp_scaled(ff_make(pa.w, la.w), 1.f);
-  const ffloat ihPa = ff_ipow<D + 2>(iha);
-  const float4 vha = Kp.vhm[a];
-  const float4 ta = Kp.thermo[a];
-  const int cnt = Ls.cnt[a];
-  float4 va = make_float4(0.f, 0.f, 0.f, 0.f);
-  if(VSIG)
-    va = Kp.vel[a];
-  float vsig = 0.f;
+// k_vsig_mixed).  With UNI (every h equal) 1/h^(D+2) multiplies the
+// finished sums instead of every pair.  The viscous part is also summed on
+// its own in FP32 (Kahan) so that the pass can leave the pressure-only
+// acceleration for the de/dt pass.
+struct AccelFFState {
+  ffloat sx, sy, sz;     // the whole pair sum (pressure and viscosity)
+  float vx, vy, vz;      // its viscous part
+  float vsig;
+};
+
+template<int D, int K, bool VSIG, bool CULL, bool UNI>
+__device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
+  int cnt, int a, const float4 & pa, const float4 & la, const ffloat & iha,
+  const ffloat & ihPa, const ffloat & Aa, const float4 & vha, const float4 & ta,
+  const float4 & va, float eps, float alpha, float beta, float alpha_a,
+  AccelFFState & out) {
   ffloat sx = ff_make(0.f, 0.f), sy = sx, sz = sx;
-  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  float vx = 0.f, vy = 0.f, vz = 0.f, cvx = 0.f, cvy = 0.f, cvz = 0.f;
+  float vsig = 0.f;
   for(int j0 = 0; j0 < cnt; j0 += 4) {
     const int4 q4 = *(const int4 *)(lp + (j0 << 5));
 #pragma unroll 2
@@ -787,7 +802,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
       const float4 pb = Kp.fph[b], lb = Kp.fpl[b];
       const FFGeom<D> g = ff_geom<D>(pa, la, pb, lb);
       ffloat ih = iha, ihP = ihPa;
-      if(pb.w != pa.w || lb.w != la.w) {
+      if(!UNI && (pb.w != pa.w || lb.w != la.w)) {
         ih = ff_rcp_scaled(ff_add(ff_make(pa.w, la.w), ff_make(pb.w, lb.w)), 2.f);
         ihP = ff_ipow<D + 2>(ih);
       }
@@ -795,8 +810,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
       const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
       const float4 vhb = Kp.vhm[b];
       const float4 tb = Kp.thermo[b];
-      const float2 mb = Kp.fm[b];
-      const float2 Ab = Kp.fA[b];
+      const float4 mAb = Kp.fmA[b];
       // viscosity in FP32 (the position unit cancels in mu)
       const float hab = 0.5f * (pa.w + pb.w);
       const float dotp = (vha.x - vhb.x) * g.dxr[0] + (vha.y - vhb.y) * g.dxr[1] +
@@ -805,10 +819,18 @@ __global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
       const float rho_ab = 0.5f * (ta.x + tb.x);
       const float c_ab = 0.5f * (ta.z + tb.z);
       const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
-      ffloat S = ff_add_f(ff_add(Aa, ff_make(Ab.x, Ab.y)), Pi);
-      S = ff_mul(ff_mul(ff_mul(S, ff_make(mb.x, mb.y)), ihP), ff_gpoly<K>(t));
-      if(!(q.h < 1.f))
+      const ffloat gp = ff_gpoly<K>(t);
+      ffloat S = ff_add_f(ff_add(Aa, ff_make(mAb.z, mAb.w)), Pi);
+      S = ff_mul(ff_mul(S, ff_make(mAb.x, mAb.y)), gp);
+      float V = mAb.x * Pi * gp.h;
+      if(!UNI) {
+        S = ff_mul(S, ihP);
+        V *= ihP.h;
+      }
+      if(!(q.h < 1.f)) {
         S = ff_make(0.f, 0.f);
+        V = 0.f;
+      }
       if(VSIG) {
         const float4 vb = Kp.vel[b];
         const float dotv = ((va.x - vb.x) * g.dxr[0] + (va.y - vb.y) * g.dxr[1] +
@@ -820,16 +842,78 @@ __global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
       // padding slots and the self pair have dx = 0 and add nothing
       ff_acc(sx, ff_mul(S, g.dx[0]));
       ff_acc(sy, ff_mul(S, g.dx[1]));
-      if(D == 3)
+      kahan(vx, cvx, V * g.dxr[0]);
+      kahan(vy, cvy, V * g.dxr[1]);
+      if(D == 3) {
         ff_acc(sz, ff_mul(S, g.dx[2]));
+        kahan(vz, cvz, V * g.dxr[2]);
+      }
     }
   }
+  if(UNI) {
+    sx = ff_mul(sx, ihPa);
+    sy = ff_mul(sy, ihPa);
+    sz = ff_mul(sz, ihPa);
+  }
+  const float ihs = UNI ? ihPa.h : 1.f;
+  out.sx = sx;
+  out.sy = sy;
+  out.sz = sz;
+  out.vx = (vx - cvx) * ihs;
+  out.vy = (vy - cvy) * ihs;
+  out.vz = (vz - cvz) * ihs;
+  out.vsig = vsig;
+}
+
+// Resident blocks of 256 per SM the acceleration pass is compiled for.  2
+// gives it up to 128 registers; 3 caps it at 80 for 24 warps to hide the
+// neighbour gathers, which measured slower on Sedov 128^3 (2.23 against
+// 1.94 ms per pass: the spills and the lost unrolling cost more than the
+// extra warps gain).
+#ifndef FSPH_ACCEL_FF_BLOCKS
+#define FSPH_ACCEL_FF_BLOCKS 2
+#endif
+
+template<int D, int K, bool VSIG, bool CULL>
+__global__ void __launch_bounds__(MIX_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
+  Particles P, PhysParams pp, Lists Ls, Packed Kp, int kick, const DevTime * tm) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const float eps = (float)pp.eps, alpha = (float)pp.alpha, beta = (float)pp.beta;
+  const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
+  const float4 pa = Kp.fph[a], la = Kp.fpl[a];
+  const float2 Aa2 = ((const float2 *)Kp.fmA)[2 * a + 1];
+  const ffloat Aa = ff_make(Aa2.x, Aa2.y);
+  const ffloat iha = ff_rcp_scaled(ff_make(pa.w, la.w), 1.f);
+  const ffloat ihPa = ff_ipow<D + 2>(iha);
+  const float4 vha = Kp.vhm[a];
+  const float4 ta = Kp.thermo[a];
+  const int cnt = Ls.cnt[a];
+  float4 va = make_float4(0.f, 0.f, 0.f, 0.f);
+  if(VSIG)
+    va = Kp.vel[a];
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  AccelFFState r;
+  if(Kp.fscale[2] != 0.0)
+    accel_ff_sum<D, K, VSIG, CULL, true>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, vha,
+      ta, va, eps, alpha, beta, alpha_a, r);
+  else
+    accel_ff_sum<D, K, VSIG, CULL, false>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, vha,
+      ta, va, eps, alpha, beta, alpha_a, r);
   const double iE = Kp.fscale[1];
   const double iE2 = iE * iE;
   // a = -gconst / E^(D+1) * sum
   const double scale = -ff_gconst<D, K>() * (D == 3 ? iE2 * iE2 : iE2 * iE);
-  double acc[3] = {scale * ff_to_double(sx), scale * ff_to_double(sy),
-    D == 3 ? scale * ff_to_double(sz) : 0.0};
+  double acc[3] = {scale * ff_to_double(r.sx), scale * ff_to_double(r.sy),
+    D == 3 ? scale * ff_to_double(r.sz) : 0.0};
+  if(Kp.ahyd) {
+    // pressure-only hydro acceleration: the whole sum less its viscous part
+    const double av[3] = {scale * (double)r.vx, scale * (double)r.vy,
+      scale * (double)r.vz};
+    for(int d = 0; d < D; ++d)
+      Kp.ahyd[(size_t)d * P.n + a] = acc[d] - av[d];
+  }
   if(pp.has_eacc) {  // acc_a += external_force::acceleration (:404)
     const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
     double ext[3];
@@ -846,7 +930,96 @@ __global__ void __launch_bounds__(MIX_THREADS, 2) k_accel_ff(Particles P,
   }
   P.f[F_GPOT][a] = 0.0;
   if(VSIG)
-    P.f[F_VSIG][a] = (double)vsig;
+    P.f[F_VSIG][a] = (double)r.vsig;
+}
+
+// de/dt through the pressure-only acceleration of the float-float pass.
+// With a^P_a = -sum_b m_b (A_a + A_b) grad W_ab (A = P/rho^2), the
+// reference's
+//   de/dt_a = -sum_b m_b (A_a v_b + A_b v_a + Pi_ab (v_a + v_b) / 2) . grad W_ab
+//             + g_a . v_a                      (default_physics.h:502-566)
+// is, exactly (A_a v_b + A_b v_a = (A_a + A_b) v_a + A_a (v_b - v_a)),
+//   de/dt_a = v_a . a^P_a
+//             - sum_b m_b (A_a (v_b - v_a) + Pi_ab (v_a + v_b) / 2) . grad W_ab
+//             + g_a . v_a.
+// The pressure terms, which cancel on lattices and in equilibrium, are then
+// those of a^P (float-float, less an FP32 viscous part); the remaining sum,
+// over velocity differences and the viscosity, stays FP32.  Valid while
+// positions, P/rho^2, v_half and alpha are those of the acceleration pass
+// (the caller tracks that).
+template<int D, int K, bool CULL>
+__global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_ahyd(Particles P,
+  PhysParams pp, Lists Ls, Packed Kp, int then_op, const DevTime * tm,
+  DevStatus * st) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if(a >= P.n)
+    return;
+  const float s0 = Kp.qscale[0], s1 = Kp.qscale[1], s2 = D == 3 ? Kp.qscale[2] : 0.f;
+  const float eps = (float)pp.eps, alpha = (float)pp.alpha, beta = (float)pp.beta;
+  const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
+  const int4 qa = Kp.qpos[a];
+  const float ha = __int_as_float(qa.w);
+  const float4 vha = Kp.vhm[a];
+  const float4 va = Kp.velp[a];  // .w = P_a / rho_a^2
+  const float2 ra = Kp.rc[a];
+  const int cnt = Ls.cnt[a];
+  float sum = 0.f, comp = 0.f;
+  const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; ++u) {
+      const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
+      const int4 qb = Kp.qpos[b];
+      const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
+      const float hab = 0.5f * (ha + __int_as_float(qb.w));
+      const float ih = 1.0f / hab;
+      const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
+      const float4 vhb = Kp.vhm[b];
+      const float4 vb = Kp.velp[b];
+      const float2 rb = Kp.rc[b];
+      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
+                         (vha.z - vhb.z) * g.dz;
+      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
+        0.5f * (ra.y + rb.y), mu);
+      const float vbad = f * ((vb.x - va.x) * g.dx + (vb.y - va.y) * g.dy +
+                              (vb.z - va.z) * g.dz);
+      const float vsd = f * ((va.x + vb.x) * g.dx + (va.y + vb.y) * g.dy +
+                             (va.z + vb.z) * g.dz);
+      kahan(sum, comp, vhb.w * (va.w * vbad + 0.5f * Pi * vsd));
+    }
+  }
+  double gv = 0, vah = 0;
+  for(int d = 0; d < D; ++d) {
+    gv += P.f[F_GAX + d][a] * P.f[F_VX + d][a];
+    vah += P.f[F_VX + d][a] * Kp.ahyd[(size_t)d * P.n + a];
+  }
+  const double dedt = vah - ((double)sum - (double)comp) + gv;
+  P.f[F_DEDT][a] = dedt;
+  if(then_op) {
+    // recompute_pressure_soundspeed_thermokinetic (default_physics.h:169-182)
+    // and, with the kick, leapfrog_kick_e (integration.h:94-98)
+    const double dt = tm->dt;
+    double vv = 0, vda = 0;
+    for(int d = 0; d < D; ++d) {
+      const double v = P.f[F_VX + d][a];
+      vv += v * v;
+      vda += v * P.f[F_AX + d][a];
+    }
+    const double e = P.f[F_E][a];
+    const double eint = e - .5 * vv - ext_potential_of<D>(pp, P.f, a);
+    if(!(eint > 0))
+      raise_status(st, FSPH_ERR_NEG_ENERGY, a);
+    P.f[F_U][a] = eint;
+    double Pn, cs;
+    eos_p_cs(pp, P.f[F_RHO][a], eint + 0.5 * dt * (dedt - vda), P.f[F_K][a],
+      P.f[F_YE][a], P.f[F_P][a], P.f[F_CS][a], Pn, cs);
+    P.f[F_P][a] = Pn;
+    P.f[F_CS][a] = cs;
+    if(then_op == OP_RECOMPUTE_KICK_E)
+      P.f[F_E][a] = e + 0.5 * dt * dedt;
+  }
 }
 
 // ------------------------------------------------------------ dispatch --
@@ -948,8 +1121,11 @@ inline void run_dudt_mixed(const Launch & L, const Particles & P,
 template<bool CULL>
 inline void run_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st) {
-  MIX_DISPATCH(k_dedt_mixed, CULL, P, pp, Ls, K, then_op, t, st);
+  const DevTime * t, DevStatus * st, int use_ahyd) {
+  if(use_ahyd && wendland_kernel(pp.kernel))
+    FF_DISPATCH(k_dedt_ahyd, CULL, P, pp, Ls, K, then_op, t, st);
+  else
+    MIX_DISPATCH(k_dedt_mixed, CULL, P, pp, Ls, K, then_op, t, st);
 }
 
 template<bool CULL>
@@ -1016,7 +1192,7 @@ void run_dudt_mixed_cullen(const Launch & L, const Particles & P,
   int then_op);
 void run_dedt_mixed_cullen(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st);
+  const DevTime * t, DevStatus * st, int use_ahyd);
 void run_alpha_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 
