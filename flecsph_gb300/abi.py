@@ -301,3 +301,27 @@ def make_view(state, n=None, fields=None):
         assert a.dtype == np.uint64 and a.flags.c_contiguous
         v.key = a.ctypes.data_as(C.POINTER(C.c_uint64))
     return v
+
+
+def make_view_tensors(batch, n=None, fields=None):
+    """fsph_soa_view over torch tensors (host or device memory; the caller
+    keeps them alive): float64 fields, int64 id, int64 key bits."""
+    import torch
+    if n is None:
+        n = int(batch["x"].shape[0])
+    v = SoAView()
+    v.n = n
+    for f in DOUBLE_FIELDS:
+        if fields is not None and f not in fields:
+            continue
+        t = batch.get(f)
+        if t is None:
+            continue
+        assert t.dtype == torch.float64 and t.is_contiguous() and t.shape[0] == n, f
+        setattr(v, f, C.cast(C.c_void_p(t.data_ptr()), _DP))
+    for f, ct in (("id", C.c_int64), ("key", C.c_uint64)):
+        if f in batch and (fields is None or f in fields):
+            t = batch[f]
+            assert t.dtype == torch.int64 and t.is_contiguous() and t.shape[0] == n, f
+            setattr(v, f, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ct)))
+    return v

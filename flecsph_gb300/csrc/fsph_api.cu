@@ -236,8 +236,8 @@ bool params_supported(const fsph_params * p, std::string * why) {
       }
   }
   if(p->enable_fmm && (p->dimension != 3 || p->gravity_order < 1 ||
-                        p->gravity_order > 2 || !(p->fmm_macangle > 0))) {
-    *why = "gravity needs 3D, gravity_order 1 or 2 and fmm_macangle > 0";
+                        p->gravity_order > 2 || !(p->fmm_macangle >= 0))) {
+    *why = "gravity needs 3D, gravity_order 1 or 2 and fmm_macangle >= 0";
     return false;
   }
   if(p->max_neighbors < 8 || p->max_neighbors > 4096) {
@@ -540,6 +540,8 @@ void fsph_destroy(fsph_ctx * c) {
     cudaStreamSynchronize(c->io.stream);
   for(void * p : c->allocs)
     cudaFree(p);
+  if(c->let_buf)
+    cudaFree(c->let_buf);
   for(auto & e : c->events)
     if(e)
       cudaEventDestroy(e);
@@ -557,7 +559,10 @@ void fsph_destroy(fsph_ctx * c) {
   delete c;
 }
 
-fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
+// The view's arrays are host memory (kind cudaMemcpyHostToDevice) or device
+// memory of the context's device (cudaMemcpyDeviceToDevice).
+static fsph_status upload_impl(fsph_ctx * c, const fsph_soa_view * v,
+  cudaMemcpyKind kind) {
   if(!c || !v || v->n < 2 || v->n > c->cap || !v->x || !v->y ||
      (c->p.dimension == 3 && !v->z) || !v->m || !v->h || !v->id)
     return FSPH_ERR_ARG;
@@ -568,9 +573,14 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   const int n = (int)v->n;
   if(c->periodic) {
     // the copies are told apart by id: the real particles must hold 0..n-1
+    std::vector<long long> ids((size_t)n);
+    if(kind == cudaMemcpyHostToDevice)
+      std::memcpy(ids.data(), v->id, sizeof(long long) * n);
+    else
+      CK(cudaMemcpy(ids.data(), v->id, sizeof(long long) * n, cudaMemcpyDeviceToHost));
     std::vector<char> seen((size_t)n, 0);
     for(int i = 0; i < n; ++i) {
-      const long long id = v->id[i];
+      const long long id = ids[i];
       if(id < 0 || id >= n || seen[(size_t)id]) {
         c->last_error = "periodic boundaries need the ids 0 .. n-1";
         return FSPH_ERR_ARG;
@@ -587,13 +597,11 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
     v->vsig, v->dt, v->divv, v->ddivvdt, v->Ye};
   for(int k = 0; k < NF; ++k) {
     if(src[k])
-      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
-        cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n, kind, c->stream));
     else
       CK(cudaMemsetAsync(c->P.f[k], 0, sizeof(double) * n, c->stream));
   }
-  CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n,
-    cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n, kind, c->stream));
   CK(cudaMemsetAsync(c->P.key, 0, sizeof(unsigned long long) * n, c->stream));
   DevTime t;
   init_time(&c->p, &t);
@@ -606,7 +614,16 @@ fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
   return FSPH_OK;
 }
 
-fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
+fsph_status fsph_upload(fsph_ctx * c, const fsph_soa_view * v) {
+  return upload_impl(c, v, cudaMemcpyHostToDevice);
+}
+
+fsph_status fsph_upload_device(fsph_ctx * c, const fsph_soa_view * v) {
+  return upload_impl(c, v, cudaMemcpyDeviceToDevice);
+}
+
+static fsph_status upload_fields_impl(fsph_ctx * c, const fsph_soa_view * v,
+  cudaMemcpyKind kind) {
   if(!c || !v || !c->uploaded || v->n != c->n)
     return FSPH_ERR_ARG;
   c->ahyd_ok = false;
@@ -620,12 +637,18 @@ fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
     v->vsig, v->dt, v->divv, v->ddivvdt, v->Ye};
   for(int k = 0; k < NF; ++k)
     if(src[k])
-      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n,
-        cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->P.f[k], src[k], sizeof(double) * n, kind, c->stream));
   if(v->id)
-    CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n,
-      cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->P.id, v->id, sizeof(long long) * n, kind, c->stream));
   return FSPH_OK;
+}
+
+fsph_status fsph_upload_fields(fsph_ctx * c, const fsph_soa_view * v) {
+  return upload_fields_impl(c, v, cudaMemcpyHostToDevice);
+}
+
+fsph_status fsph_upload_fields_device(fsph_ctx * c, const fsph_soa_view * v) {
+  return upload_fields_impl(c, v, cudaMemcpyDeviceToDevice);
 }
 
 fsph_status fsph_host_register(void * ptr, int64_t bytes) {
@@ -689,7 +712,8 @@ fsph_status fsph_sync(fsph_ctx * c) {
   return FSPH_OK;
 }
 
-fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
+static fsph_status download_impl(fsph_ctx * c, fsph_soa_view * v,
+  cudaMemcpyKind kind) {
   if(!c || !v || v->n != c->n || !c->uploaded)
     return FSPH_ERR_ARG;
   fsph_status s = fsph_sync(c);
@@ -705,17 +729,23 @@ fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
       if(c->p.dimension == 2)
         continue;
     if(dst[k])
-      CK(cudaMemcpyAsync(dst[k], c->P.f[k], sizeof(double) * n,
-        cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(dst[k], c->P.f[k], sizeof(double) * n, kind, c->stream));
   }
   if(v->id)
-    CK(cudaMemcpyAsync(v->id, c->P.id, sizeof(long long) * n,
-      cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(v->id, c->P.id, sizeof(long long) * n, kind, c->stream));
   if(v->key)
-    CK(cudaMemcpyAsync(v->key, c->P.key, sizeof(unsigned long long) * n,
-      cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(v->key, c->P.key, sizeof(unsigned long long) * n, kind,
+      c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return FSPH_OK;
+}
+
+fsph_status fsph_download(fsph_ctx * c, fsph_soa_view * v) {
+  return download_impl(c, v, cudaMemcpyDeviceToHost);
+}
+
+fsph_status fsph_download_device(fsph_ctx * c, fsph_soa_view * v) {
+  return download_impl(c, v, cudaMemcpyDeviceToDevice);
 }
 
 fsph_status fsph_get_time(fsph_ctx * c, double * dt, double * tt,
@@ -772,6 +802,7 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   if(!c || !c->uploaded)
     return FSPH_ERR_STATE;
   c->ahyd_ok = false;
+  c->grav_nodes_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -1122,6 +1153,79 @@ fsph_status fsph_gravitation(fsph_ctx * c) {
   Phase ph(c, FSPH_TIMER_GRAVITY);
   CK(launch_gravity(L, c->P, c->pp, c->T, c->grav, c->d_range, c->p.fmm_macangle,
     c->p.gravity_order, c->mixed ? 1 : 0, c->d_status, c->nsm));
+  c->grav_nodes_ok = c->n >= 2;
+  return FSPH_OK;
+}
+
+static fsph_status let_reserve(fsph_ctx * c, long long records) {
+  if(records <= c->let_cap)
+    return FSPH_OK;
+  if(c->let_buf) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->let_buf);
+    c->let_buf = nullptr;
+    c->let_cap = 0;
+  }
+  CK(cudaMalloc((void **)&c->let_buf, sizeof(double) * 10 * (size_t)records));
+  c->let_cap = records;
+  return FSPH_OK;
+}
+
+fsph_status fsph_gravity_export(fsph_ctx * c, const double * box_lo,
+  const double * box_hi, double theta, double * cells, int64_t capacity,
+  int64_t * count) {
+  if(!c || !box_lo || !box_hi || !count || capacity < 0 || (capacity > 0 && !cells) ||
+     !(theta >= 0.0))
+    return FSPH_ERR_ARG;
+  if(!c->grav_nodes_ok) {
+    c->last_error = "gravity_export needs fsph_gravitation after the last tree build";
+    return FSPH_ERR_STATE;
+  }
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  // a walk emits at most every node and every particle once
+  const long long most = 2ll * c->n;
+  s = let_reserve(c, most);
+  if(s)
+    return s;
+  if(!c->let_count)
+    CK(dalloc(c, &c->let_count, 1));
+  Launch L = c->L();
+  CK(launch_let_export(L, c->P, c->p.dimension, c->T, c->grav, box_lo, box_hi, theta,
+    c->p.gravity_order, c->let_buf, most, c->let_count, c->d_status));
+  unsigned long long got = 0;
+  CK(cudaMemcpyAsync(&got, c->let_count, sizeof(got), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  s = fsph_sync(c);
+  if(s)
+    return s;
+  *count = (int64_t)got;
+  const long long take = (long long)got < capacity ? (long long)got : capacity;
+  if(take > 0)
+    CK(cudaMemcpy(cells, c->let_buf, sizeof(double) * 10 * (size_t)take, cudaMemcpyDefault));
+  return FSPH_OK;
+}
+
+fsph_status fsph_gravity_import(fsph_ctx * c, const double * cells, int64_t ncell) {
+  if(!c || ncell < 0 || (ncell > 0 && !cells))
+    return FSPH_ERR_ARG;
+  if(!c->uploaded)
+    return FSPH_ERR_STATE;
+  fsph_status s = set_device(c);
+  if(s)
+    return s;
+  if(ncell == 0)
+    return FSPH_OK;
+  s = let_reserve(c, ncell);
+  if(s)
+    return s;
+  Launch L = c->L();
+  Phase ph(c, FSPH_TIMER_GRAVITY);
+  CK(cudaMemcpyAsync(c->let_buf, cells, sizeof(double) * 10 * (size_t)ncell,
+    cudaMemcpyDefault, c->stream));
+  CK(launch_let_apply(L, c->P, c->p.dimension, c->let_buf, ncell,
+    c->p.gravitational_constant, c->mixed ? 1 : 0));
   return FSPH_OK;
 }
 

@@ -37,6 +37,12 @@ struct fsph_ctx {
   fsph::Packed K{};
   bool mixed = false;
   fsph::GravBuffers grav{};  // allocated when enable_fmm
+  bool grav_nodes_ok = false;  // grav.gn holds the multipoles of the current tree
+  // multi-rank gravity: exported / imported cell records (10 doubles each),
+  // grown on demand, freed with the context
+  double * let_buf = nullptr;
+  long long let_cap = 0;
+  unsigned long long * let_count = nullptr;
   // periodic boundaries: real particles hold ids [0, nreal)
   bool periodic = false;
   long long nreal = 0;

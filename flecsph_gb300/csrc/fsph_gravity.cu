@@ -423,6 +423,201 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
   }
 }
 
+// ------------------------------------------- multi-rank gravity (LET) --
+// A locally essential tree for a run decomposed over ranks.  The reference
+// shares top-tree branches and fetches remote subtrees during its FMM walk
+// (tree_topology.h:1142-1542,1550-1744); here a rank exports, for every
+// other rank's bounding box, the cells of its own tree that are far enough
+// for that whole box (r_max < theta * d(centre of mass, box), the test the
+// walk applies to a group's box) as multipoles, and the particles of the
+// cells that are not, as point masses; the receiving rank adds their field
+// to its particles (k_let_apply) after its own tree walk.  Cell record, 10
+// doubles: {m, c_x, c_y, c_z, Q_xx, Q_yy, Q_zz, Q_xy, Q_xz, Q_yz} (Q
+// traceless about c; zero for a point mass).
+#define LET_REC 10
+
+// One warp walks the tree (k_grav_nodes must have filled G.gn since the
+// last tree build) against the box [blo, bhi], in FP64.
+__global__ void k_let_export(Particles P, int dim, Tree T, GravBuffers G,
+  double3 blo, double3 bhi, double th2, int order, double * cells,
+  long long cap, unsigned long long * count, DevStatus * st) {
+  __shared__ int stack[GW_STACK];
+  const int lane = threadIdx.x;
+  const unsigned lt = lanemask_lt_g();
+  const double lo[3] = {blo.x, blo.y, blo.z}, hi[3] = {bhi.x, bhi.y, bhi.z};
+  int sptr = 1;
+  if(lane == 0)
+    stack[0] = 0;
+  __syncwarp();
+  while(sptr > 0) {
+    const int k = sptr < 32 ? sptr : 32;
+    const bool act = lane < k;
+    const int node = act ? stack[sptr - 1 - lane] : 0;
+    __syncwarp();
+    sptr -= k;
+    bool acc = false, open = false, leaf = false;
+    int code = 0;
+    if(act) {
+      if(node < 0)
+        leaf = true;
+      else {
+        const GravNode & g = G.gn[node];
+        double dd = 0.0;
+        for(int d = 0; d < dim; ++d) {
+          const double e = fmax(0.0, fmax(lo[d] - g.c[d], g.c[d] - hi[d]));
+          dd += e * e;
+        }
+        acc = dd > 0.0 && g.rmax * g.rmax < th2 * dd;
+        open = !acc;
+        code = T.qbox[2 * node + 1].w;
+      }
+    }
+    const unsigned bo = __ballot_sync(GFULL, open);
+    const int npush = 2 * __popc(bo);
+    if(sptr + npush > GW_STACK) {
+      if(lane == 0 && atomicCAS(&st->code, 0, (int)FSPH_ERR_STACK_OVERFLOW) == 0)
+        st->index = -1;
+      return;
+    }
+    if(open) {
+      const int pos = sptr + 2 * __popc(bo & lt);
+      const int split = code >> 2;
+      stack[pos] = (code & 1) ? ~(split + 1) : split + 1;
+      stack[pos + 1] = (code & 2) ? ~split : split;
+    }
+    sptr += npush;
+    if(acc || leaf) {
+      const unsigned long long slot = atomicAdd(count, 1ull);
+      if(slot < (unsigned long long)cap) {
+        double * r = cells + LET_REC * slot;
+        if(acc) {
+          const GravNode & g = G.gn[node];
+          r[0] = g.m;
+          for(int d = 0; d < 3; ++d)
+            r[1 + d] = g.c[d];
+          for(int q = 0; q < 6; ++q)
+            r[4 + q] = order >= 2 ? g.q[q] : 0.0;
+        }
+        else {
+          const int j = ~node;
+          r[0] = P.f[F_M][j];
+          r[1] = P.f[F_X][j];
+          r[2] = P.f[F_Y][j];
+          r[3] = dim == 3 ? P.f[F_Z][j] : 0.0;
+          for(int q = 0; q < 6; ++q)
+            r[4 + q] = 0.0;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Field of ncell cells on every particle, added to g-acceleration and
+// potential: the multipole terms of the walk (monopole + traceless
+// quadrupole), staged through shared memory in chunks.  FP64 mode in FP64;
+// the mixed path in FP32 relative to a reference point per block (the
+// block's first particle), with Kahan sums.  A cell at a particle's own
+// position (distance 0) adds nothing.
+#define LET_CHUNK 128
+template<bool MIXED>
+__global__ void __launch_bounds__(256) k_let_apply(Particles P, int dim,
+  const double * cells, long long ncell, double Gc) {
+  typedef typename std::conditional<MIXED, float, double>::type R;
+  __shared__ R sc[LET_CHUNK][LET_REC];
+  __shared__ double sref[3];
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = P.n;
+  if(threadIdx.x == 0) {
+    const int r = blockIdx.x * blockDim.x;
+    for(int d = 0; d < 3; ++d)
+      sref[d] = (MIXED && d < dim) ? P.f[F_X + d][r] : 0.0;
+  }
+  __syncthreads();
+  R xa[3] = {0, 0, 0};
+  if(a < n)
+    for(int d = 0; d < dim; ++d)
+      xa[d] = (R)(P.f[F_X + d][a] - sref[d]);
+  R s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
+  for(long long c0 = 0; c0 < ncell; c0 += LET_CHUNK) {
+    const int m = (int)(ncell - c0 < LET_CHUNK ? ncell - c0 : LET_CHUNK);
+    __syncthreads();
+    for(int t = threadIdx.x; t < m * LET_REC; t += blockDim.x) {
+      const int k = t / LET_REC, f = t % LET_REC;
+      double v = cells[LET_REC * (c0 + k) + f];
+      if(f >= 1 && f <= 3)
+        v -= sref[f - 1];
+      sc[k][f] = (R)v;
+    }
+    __syncthreads();
+    if(a >= n)
+      continue;
+    R p[4] = {0, 0, 0, 0};
+    for(int k = 0; k < m; ++k) {
+      const R mm = sc[k][0];
+      const R dx = xa[0] - sc[k][1], dy = xa[1] - sc[k][2];
+      const R dz = dim == 3 ? xa[2] - sc[k][3] : (R)0;
+      const R r2 = dx * dx + dy * dy + dz * dz;
+      if(!(r2 > (R)0))
+        continue;
+      const R ir = MIXED ? (R)rsqrtf((float)r2) : (R)rsqrt((double)r2);
+      const R ir2 = ir * ir, ir3 = ir * ir2;
+      R phi = -mm * ir;
+      R fx = -mm * ir3 * dx, fy = -mm * ir3 * dy, fz = -mm * ir3 * dz;
+      const R qxx = sc[k][4], qyy = sc[k][5], qzz = sc[k][6];
+      const R qxy = sc[k][7], qxz = sc[k][8], qyz = sc[k][9];
+      const R qdx = qxx * dx + qxy * dy + qxz * dz;
+      const R qdy = qxy * dx + qyy * dy + qyz * dz;
+      const R qdz = qxz * dx + qyz * dy + qzz * dz;
+      const R dqd = dx * qdx + dy * qdy + dz * qdz;
+      const R ir5 = ir3 * ir2, ir7 = ir5 * ir2;
+      phi += (R)-0.5 * dqd * ir5;
+      fx += qdx * ir5 - (R)2.5 * dqd * ir7 * dx;
+      fy += qdy * ir5 - (R)2.5 * dqd * ir7 * dy;
+      fz += qdz * ir5 - (R)2.5 * dqd * ir7 * dz;
+      p[0] += fx;
+      p[1] += fy;
+      p[2] += fz;
+      p[3] += phi;
+    }
+    for(int q = 0; q < 4; ++q)
+      kahan_g(s[q], c[q], p[q]);
+  }
+  if(a >= n)
+    return;
+  for(int d = 0; d < dim; ++d)
+    P.f[F_GAX + d][a] += ((double)s[d] - (double)c[d]) * Gc;
+  P.f[F_GPOT][a] += ((double)s[3] - (double)c[3]) * Gc;
+}
+
+cudaError_t launch_let_export(const Launch & L, const Particles & P, int dim,
+  const Tree & T, const GravBuffers & G, const double * blo, const double * bhi,
+  double theta, int order, double * cells, long long cap,
+  unsigned long long * count, DevStatus * st) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), L.stream);
+  if(e != cudaSuccess)
+    return e;
+  const double3 lo = make_double3(blo[0], blo[1], dim == 3 ? blo[2] : 0.0);
+  const double3 hi = make_double3(bhi[0], bhi[1], dim == 3 ? bhi[2] : 0.0);
+  k_let_export<<<1, 32, 0, L.stream>>>(P, dim, T, G, lo, hi, theta * theta, order,
+    cells, cap, count, st);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_let_apply(const Launch & L, const Particles & P, int dim,
+  const double * cells, long long ncell, double Gc, int mixed) {
+  if(P.n < 1 || ncell < 1)
+    return cudaSuccess;
+  const int nb = (P.n + 255) / 256;
+  if(mixed)
+    k_let_apply<true><<<nb, 256, 0, L.stream>>>(P, dim, cells, ncell, Gc);
+  else
+    k_let_apply<false><<<nb, 256, 0, L.stream>>>(P, dim, cells, ncell, Gc);
+  *L.counter += 1;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gravity(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, const GravBuffers & G,
   const unsigned long long * rbits, double theta, int order, int mixed,

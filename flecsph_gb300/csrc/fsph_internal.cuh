@@ -258,6 +258,12 @@ cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const DevTime * t, DevStatus * st, int use_ahyd);
 
 // ---- fsph_gravity.cu ----
+cudaError_t launch_let_export(const Launch & L, const Particles & P, int dim,
+  const Tree & T, const GravBuffers & G, const double * blo, const double * bhi,
+  double theta, int order, double * cells, long long cap,
+  unsigned long long * count, DevStatus * st);
+cudaError_t launch_let_apply(const Launch & L, const Particles & P, int dim,
+  const double * cells, long long ncell, double Gc, int mixed);
 cudaError_t launch_gravity(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, const GravBuffers & G,
   const unsigned long long * rbits, double theta, int order, int mixed,

@@ -100,6 +100,11 @@ def library():
     lib.fsph_mark_elapsed.argtypes = [C.c_void_p, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_double)]
     lib.fsph_measure_peak.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_double)]
+    for f in ("fsph_upload_device", "fsph_download_device", "fsph_upload_fields_device"):
+        getattr(lib, f).argtypes = [C.c_void_p, C.POINTER(SoAView)]
+    lib.fsph_gravity_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                        C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    lib.fsph_gravity_import.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
     _lib = lib
     return lib
 
@@ -193,6 +198,72 @@ class BodySystem:
 
     def download_into(self, view):
         self._check(self.lib.fsph_download(self.ctx, C.byref(view)), "download")
+
+    # -- device-resident data (torch tensors on this context's device) ------
+    @staticmethod
+    def _tensors_ready(batch):
+        """The library's stream does not wait for torch's: finish the work
+        that wrote these tensors before the library reads them."""
+        import torch
+        for t in batch.values() if isinstance(batch, dict) else [batch]:
+            if torch.is_tensor(t) and t.is_cuda:
+                torch.cuda.current_stream(t.device).synchronize()
+                return
+
+    def read_bodies_device(self, batch):
+        """fsph_upload_device from a dict of device tensors (float64 fields,
+        int64 id)."""
+        from .abi import make_view_tensors
+        self._tensors_ready(batch)
+        self._check(self.lib.fsph_upload_device(self.ctx, C.byref(make_view_tensors(batch))),
+                    "upload_device")
+
+    def download_device(self, fields=None, device=None):
+        """Current state as a dict of tensors on `device` (fsph_download_device)."""
+        import torch
+        from .abi import DOUBLE_FIELDS, make_view_tensors
+        n = self.count()[0]
+        keep = fields or (DOUBLE_FIELDS + ["id"])
+        out = {f: torch.empty(n, dtype=torch.int64 if f in ("id", "key") else torch.float64,
+                              device=device) for f in keep}
+        self._check(self.lib.fsph_download_device(self.ctx, C.byref(make_view_tensors(out, n))),
+                    "download_device")
+        return out
+
+    def upload_fields_device(self, batch):
+        """fsph_upload_fields_device, then a sync so `batch` may be freed."""
+        from .abi import make_view_tensors
+        n = self.count()[0]
+        self._tensors_ready(batch)
+        self._check(self.lib.fsph_upload_fields_device(
+            self.ctx, C.byref(make_view_tensors(batch, n))), "upload_fields_device")
+        self.sync()
+
+    def gravity_export(self, box_lo, box_hi, theta, device=None):
+        """Cell records (tensor [k, 10] float64) of this context's tree for a
+        remote box (fsph_gravity_export)."""
+        import torch
+        lo = np.ascontiguousarray(box_lo, np.float64)
+        hi = np.ascontiguousarray(box_hi, np.float64)
+        cnt = C.c_int64(0)
+        self._check(self.lib.fsph_gravity_export(self.ctx, lo.ctypes.data, hi.ctypes.data,
+                                                 float(theta), None, 0, C.byref(cnt)),
+                    "gravity_export")
+        out = torch.empty((cnt.value, 10), dtype=torch.float64, device=device)
+        if cnt.value:
+            self._check(self.lib.fsph_gravity_export(
+                self.ctx, lo.ctypes.data, hi.ctypes.data, float(theta), out.data_ptr(),
+                cnt.value, C.byref(cnt)), "gravity_export")
+        return out
+
+    def gravity_import(self, cells):
+        """Add the field of cell records (tensor [k, 10] float64, host or
+        device) to every particle held (fsph_gravity_import)."""
+        cells = cells.contiguous()
+        self._tensors_ready(cells)
+        self._check(self.lib.fsph_gravity_import(self.ctx, cells.data_ptr(),
+                                                 int(cells.shape[0])), "gravity_import")
+        self.sync()
 
     def step_io(self, vin, vout):
         """One iteration with its host copies (fsph_step_io): the non-NULL

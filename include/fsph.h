@@ -137,7 +137,7 @@ typedef struct fsph_params {
   double out_screen_dt;              /* [339] 0 */
   double out_scalar_dt;              /* [350] 0 */
   double out_h5data_dt;              /* [366] 0 */
-  double fmm_macangle;               /* [542] 0.0 */
+  double fmm_macangle;               /* [542] 0.0 (0: every pair summed directly) */
   double gravitational_constant;     /* [628] 1 */
   double box_length;                 /* [258] 3.0 */
   double box_width;                  /* [262] 1.0 */
@@ -293,6 +293,18 @@ fsph_status fsph_download(fsph_ctx * ctx, fsph_soa_view * host);
  * the uploaded count) into the current particle order, keeping time,
  * iteration and tree state: the per-step input path of a host-side driver. */
 fsph_status fsph_upload_fields(fsph_ctx * ctx, const fsph_soa_view * host);
+/* The same three copies with the view's arrays in DEVICE memory of the
+ * context's device (for instance another library's tensors): device to
+ * device on the context's stream, the stream synchronised before
+ * fsph_upload_device and fsph_download_device return.  The context's stream
+ * does not wait for other streams: work that writes the arrays must be
+ * complete before the call (synchronise the producing stream), and with
+ * fsph_upload_fields_device the arrays must stay unchanged until the
+ * context synchronises.  A multi-rank driver moves its exchanged particles
+ * in and out this way without host staging. */
+fsph_status fsph_upload_device(fsph_ctx * ctx, const fsph_soa_view * dev);
+fsph_status fsph_download_device(fsph_ctx * ctx, fsph_soa_view * dev);
+fsph_status fsph_upload_fields_device(fsph_ctx * ctx, const fsph_soa_view * dev);
 /* Page-lock (pin) / release a host buffer so the copies above run at full
  * link speed.  Thin wrappers over cudaHostRegister/cudaHostUnregister. */
 fsph_status fsph_host_register(void * ptr, int64_t bytes);
@@ -361,6 +373,28 @@ fsph_status fsph_compute_average_smoothinglength(fsph_ctx * ctx);
 /* gravitation_fmm(): multipole tree gravity, order params.gravity_order,
  * opening angle params.fmm_macangle; adds into g-acceleration/potential. */
 fsph_status fsph_gravitation(fsph_ctx * ctx);
+/* Gravity over ranks (a locally essential tree).  The reference shares
+ * top-tree branches between MPI ranks and fetches remote subtrees in its
+ * FMM walk (tree_topology.h:1142-1542,1550-1744).  Here each rank, after
+ * fsph_gravitation on its own particles, exports for every other rank's
+ * bounding box [box_lo, box_hi] (dimension doubles each) the cells of its
+ * tree that are far enough for that whole box (r_max < theta * distance of
+ * the centre of mass to the box) and the particles of the cells that are
+ * not, as records of 10 doubles {m, c_x, c_y, c_z, Q_xx, Q_yy, Q_zz, Q_xy,
+ * Q_xz, Q_yz} (traceless quadrupole about c, zero for a particle and with
+ * gravity_order 1).  *count receives the number of records; at most
+ * `capacity` are copied to `cells` (host or device memory; NULL with
+ * capacity 0 to query).  Synchronous.  FSPH_ERR_STATE unless
+ * fsph_gravitation ran after the last fsph_update_iteration. */
+fsph_status fsph_gravity_export(fsph_ctx * ctx, const double * box_lo,
+  const double * box_hi, double theta, double * cells, int64_t capacity,
+  int64_t * count);
+/* Adds the field of `ncell` such records (host or device memory, from the
+ * other ranks; device records must be complete, as above) to the
+ * g-acceleration and potential of every particle the context holds:
+ * monopole plus quadrupole terms, G = gravitational_constant; a record at a
+ * particle's own position adds nothing to it. */
+fsph_status fsph_gravity_import(fsph_ctx * ctx, const double * cells, int64_t ncell);
 /* physics::advance_time() */
 fsph_status fsph_advance_time(fsph_ctx * ctx);
 

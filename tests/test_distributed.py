@@ -20,11 +20,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 from flecsph_gb300 import setups  # noqa: E402
 from flecsph_gb300.abi import DOUBLE_FIELDS  # noqa: E402
 from flecsph_gb300.distributed import (Comm, FIELDS, global_range,  # noqa: E402
-                                       halo_destinations, morton_keys)
+                                       halo_destinations, morton_keys, to_numpy,
+                                       to_tensors)
 
 
 class OracleEngine:
-    """The CPU oracle with the engine surface DistributedSystem needs."""
+    """The CPU oracle with the engine surface DistributedSystem needs
+    (host tensors in and out)."""
 
     def __init__(self, params):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -32,27 +34,81 @@ class OracleEngine:
         self.o = pyoracle.Oracle("port", params, threads=1)
         self.time = (params.initial_dt, params.initial_time, params.initial_iteration)
 
-    def upload(self, state):
-        self.o.upload(state)
+    def upload(self, batch):
+        self.o.upload(to_numpy(batch))
 
     def set_time(self, dt, t, it):
         self.time = (dt, t, it)
         self.o.set_time(dt, t, it)
 
-    def refresh(self, state):
+    def refresh(self, batch):
         # the oracle has no field-only upload: reload and rebuild the same tree
-        self.o.upload(state)
+        self.o.upload(to_numpy(batch))
         self.o.set_time(*self.time)
         self.o.update_iteration()
 
     def download(self):
-        return self.o.download()
+        return to_tensors(self.o.download(), "cpu")
 
     def neighbors(self):
         return self.o.neighbors()
 
     def __getattr__(self, name):
         return getattr(self.o, name)
+
+
+class DirectGravityEngine:
+    """Gravity of a rank's own particles by direct FP64 summation, with the
+    export/import surface of the gravity engine: at theta = 0 no cell is
+    far enough, so the export is every particle as a point mass, and the
+    distributed field must be the global direct sum."""
+
+    def __init__(self, G=1.0):
+        self.G = G
+
+    def upload(self, batch):
+        self.s = to_numpy(batch)
+
+    def set_time(self, *a):
+        pass
+
+    def update_iteration(self):
+        pass
+
+    def _field(self, src_x, src_m):
+        x = np.stack([self.s[k] for k in ("x", "y", "z")], 1)
+        d = x[:, None, :] - src_x[None, :, :]
+        r2 = (d ** 2).sum(-1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ir = np.where(r2 > 0, 1.0 / np.sqrt(r2), 0.0)
+        a = -self.G * ((src_m[None, :] * ir ** 3)[..., None] * d).sum(1)
+        phi = -self.G * (src_m[None, :] * ir).sum(1)
+        return a, phi
+
+    def gravitation(self):
+        x = np.stack([self.s[k] for k in ("x", "y", "z")], 1)
+        a, phi = self._field(x, self.s["m"])
+        for k, f in enumerate(("gax", "gay", "gaz")):
+            self.s[f] = self.s[f] + a[:, k]
+        self.s["gpot"] = self.s["gpot"] + phi
+
+    def gravity_export(self, lo, hi, theta):
+        import torch
+        assert theta == 0.0
+        rec = np.zeros((len(self.s["m"]), 10))
+        rec[:, 0] = self.s["m"]
+        rec[:, 1], rec[:, 2], rec[:, 3] = self.s["x"], self.s["y"], self.s["z"]
+        return torch.from_numpy(rec)
+
+    def gravity_import(self, cells):
+        c = cells.numpy()
+        a, phi = self._field(c[:, 1:4], c[:, 0])
+        for k, f in enumerate(("gax", "gay", "gaz")):
+            self.s[f] = self.s[f] + a[:, k]
+        self.s["gpot"] = self.s["gpot"] + phi
+
+    def download(self):
+        return to_tensors(self.s, "cpu")
 
 
 def _problem():
@@ -81,9 +137,9 @@ def _rank_main(rank, world, port, outdir, steps):
     ds.read_bodies(local)
     ds.update_iteration()
     # lists of own particles, as id sets
-    st = ds.e.download()
+    st = to_numpy(ds.e.download())
     off, idx = ds.e.neighbors()
-    own = np.isin(st["id"], ds.own_ids)
+    own = np.isin(st["id"], ds.own_ids.numpy())
     lists = {int(st["id"][a]): np.sort(st["id"][idx[off[a]:off[a + 1]]])
              for a in np.nonzero(own)[0]}
     nb_ids = np.array(sorted(lists))
@@ -177,11 +233,12 @@ def test_steps_match_one_rank(rank_run, oracle_port):
 
 
 def test_keys_and_halo_single_rank_helpers(oracle_port):
-    """Host Morton keys equal the oracle's; with one rank nothing is a ghost."""
+    """Tensor Morton keys equal the oracle's; with one rank nothing is a ghost."""
     s, p = _problem()
     comm = Comm(None)
-    lo, hi = global_range(comm, s, 3)
-    keys = morton_keys(s, lo, hi, 3)
+    b = to_tensors(s, "cpu")
+    lo, hi = global_range(comm, b, 3)
+    keys = morton_keys(b, lo, hi, 3).numpy().view(np.uint64)
     o = oracle_port.Oracle("port", p)
     o.upload(s)
     o.update_iteration()
@@ -189,4 +246,78 @@ def test_keys_and_halo_single_rank_helpers(oracle_port):
     order = np.argsort(st["id"])
     mine = np.argsort(s["id"])
     assert np.array_equal(keys[mine], st["key"][order])
-    assert all(len(x) == 0 for x in halo_destinations(comm, s, 3))
+    assert all(len(x) == 0 for x in halo_destinations(comm, b, 3))
+
+
+def test_keys_2d_match_oracle(oracle_port):
+    """The 2D key layout (marker at bit 62) as well."""
+    s, p, m = setups.sod2d(60, 12)
+    s = setups.shuffled(s, 4)
+    b = to_tensors(s, "cpu")
+    lo, hi = global_range(Comm(None), b, 2)
+    keys = morton_keys(b, lo, hi, 2).numpy().view(np.uint64)
+    o = oracle_port.Oracle("port", p)
+    o.upload(s)
+    o.update_iteration()
+    st = o.download()
+    assert np.array_equal(keys[np.argsort(s["id"])], st["key"][np.argsort(st["id"])])
+
+
+def _grav_rank_main(rank, world, port, outdir):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from flecsph_gb300.distributed import DistributedSystem
+    comm = Comm(dist)
+    s, p = _grav_problem()
+    share = np.random.Generator(np.random.PCG64(6)).integers(0, world, len(s["x"]))
+    local = {f: s[f][share == rank] for f in FIELDS}
+    ds = DistributedSystem(OracleEngine(p), p, comm, gravity=DirectGravityEngine())
+    ds.read_bodies(local)
+    ds.update_iteration()
+    ds.e.eos_init()
+    ds.e.density_pressure_soundspeed()
+    ds.e.save_velocityhalf()
+    ds.refresh_ghosts()
+    ds.e.acceleration()
+    ds.gravitation()
+    out = ds.own_state()
+    np.savez(os.path.join(outdir, f"g{rank}.npz"), cells=ds.cells_received,
+             **{"s_" + f: out[f] for f in ("id", "gax", "gay", "gaz", "gpot")})
+    dist.destroy_process_group()
+
+
+def _grav_problem():
+    s, p, m = setups.polytrope3d(1500, seed=3)
+    p.enable_fmm = 1
+    p.fmm_macangle = 0.0
+    p.max_neighbors = 1024
+    p.adaptive_timestep = 0
+    return s, p
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_gravity_over_ranks_is_the_global_sum(world, tmp_path):
+    """Gravity of a decomposed run (own tree walk + cells from the other
+    ranks, here at theta = 0, i.e. every remote particle): equal to the
+    direct sum over all particles to rounding."""
+    import torch.multiprocessing as mp
+    mp.start_processes(_grav_rank_main, args=(world, _free_port(), str(tmp_path)),
+                       nprocs=world, join=True, start_method="spawn")
+    ranks = [dict(np.load(os.path.join(tmp_path, f"g{r}.npz"))) for r in range(world)]
+    s, p = _grav_problem()
+    x = np.stack([s[k] for k in ("x", "y", "z")], 1)
+    d = x[:, None, :] - x[None, :, :]
+    r2 = (d ** 2).sum(-1)
+    with np.errstate(divide="ignore"):
+        ir = np.where(r2 > 0, 1 / np.sqrt(r2), 0.0)
+    a = -((s["m"][None, :] * ir ** 3)[..., None] * d).sum(1)
+    ids = np.concatenate([r["s_id"] for r in ranks])
+    got = np.concatenate([np.stack([r["s_gax"], r["s_gay"], r["s_gaz"]], 1) for r in ranks])
+    o = np.argsort(ids)
+    ref = a[np.argsort(s["id"])]
+    assert np.array_equal(np.sort(ids), np.sort(s["id"]))
+    err = np.abs(got[o] - ref).max() / np.abs(ref).max()
+    assert err <= 1e-12, err
+    assert all(int(r["cells"]) > 0 for r in ranks)
