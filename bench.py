@@ -24,8 +24,9 @@ timed steps in both precisions; `polytrope` -- the n=1 polytrope with tree
 gravity (quadrupole, theta 0.5), 4M particles by default, with the gravity
 error of 64 sampled blocks of sinks against direct FP64 summation over all
 sources on the host cores; `ensemble` -- 256 independent 2D problems (Sod and
-Noh, log-uniform sizes 2k-200k) stepped as CUDA graphs, against the same
-members stepped one by one.
+Noh, log-uniform sizes 2k-200k, about 12.4M particles) stepped as CUDA
+graphs with the lane count and walk-group size chosen by
+fsph_ensemble_tune_shape, against the same members stepped one by one.
 
 `--impl reference` times the reference algorithm on the host cores instead
 (the CPU oracle: the reference compiled from its sources where those exist
@@ -422,9 +423,10 @@ def ensemble_arm(args):
     ens.step(1 + args.warmup)
     ens.sync()
     res = {}
+    gsize = 32
     for mode in ("one_by_one", "graphs"):
         if mode == "graphs":
-            lanes, _ = ens.tune(2)
+            lanes, gsize, _ = ens.tune_shape(2)
         else:
             ens.set_lanes(0)
             lanes = 0
@@ -454,7 +456,8 @@ def ensemble_arm(args):
         "config": {"workload": f"ensemble2d_{len(probs)}_sod_noh",
                    "problems": len(probs), "n_particles_total": ntot,
                    "n_min": min(sizes), "n_max": max(sizes), "precision": "mixed",
-                   "lanes": g["lanes"], "timing": "host wall clock around K steps "
+                   "lanes": g["lanes"], "group_size": gsize,
+                   "timing": "host wall clock around K steps "
                    "with a device sync on both sides (many streams)"},
         "one_by_one": {"value": world * ntot * K / res["one_by_one"]["seconds"],
                        "ms_per_step": 1e3 * res["one_by_one"]["seconds"] / K},

@@ -105,7 +105,7 @@ class Params(C.Structure):
         ("precision_mode", C.c_int32),
         ("max_neighbors", C.c_int32),
         ("gravity_order", C.c_int32),
-        ("reserved_pad", C.c_int32),
+        ("group_size", C.c_int32),
         ("sph_viscosity_alpha_max", C.c_double),
         ("sph_viscosity_l", C.c_double),
         ("sph_viscosity_delta", C.c_double),
@@ -227,7 +227,7 @@ class Params(C.Structure):
     def as_dict(self):
         out = {}
         for name, _ in self._fields_:
-            if name in ("reserved", "reserved_pad", "reserved_pad2"):
+            if name in ("reserved", "reserved_pad2"):
                 continue
             v = getattr(self, name)
             out[name] = list(v) if name == "external_force" else v

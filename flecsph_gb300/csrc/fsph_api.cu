@@ -240,6 +240,10 @@ bool params_supported(const fsph_params * p, std::string * why) {
     *why = "gravity needs 3D, gravity_order 1 or 2 and fmm_macangle >= 0";
     return false;
   }
+  if(p->group_size < 0 || p->group_size > 32) {
+    *why = "group_size out of [0, 32]";
+    return false;
+  }
   if(p->max_neighbors < 8 || p->max_neighbors > 4096) {
     *why = "max_neighbors out of [8, 4096]";
     return false;
@@ -849,7 +853,8 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   {
     Phase ph(c, FSPH_TIMER_TREE);
     CK(launch_pack_positions(L, c->P, c->pp, c->d_range, c->K));
-    CK(launch_build_tree(L, c->P, c->pp, c->T, GROUP_MAX, c->d_range, c->K.qpos,
+    CK(launch_build_tree(L, c->P, c->pp, c->T,
+      c->p.group_size > 0 ? c->p.group_size : GROUP_MAX, c->d_range, c->K.qpos,
       c->mixed ? 0 : 1));
   }
   {

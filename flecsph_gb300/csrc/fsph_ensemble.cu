@@ -19,7 +19,8 @@
 //     iteration, launch count) to where that iteration leaves it.
 // Members are spread over lanes (one stream each) by particle count, largest
 // first onto the least loaded lane; fsph_ensemble_tune times a few steps per
-// lane count and keeps the fastest.
+// lane count and keeps the fastest, fsph_ensemble_tune_shape does so for each
+// walk-group size (8, 16, 32 particles per warp) as well.
 //
 // Periodic members (their copy count is read back every iteration) and
 // members with timers on run eagerly, member by member.  Any host-visible
@@ -479,6 +480,57 @@ fsph_status fsph_ensemble_tune(fsph_ensemble * e, int32_t steps_per_trial,
     return s;
   if(lanes_chosen)
     *lanes_chosen = best_l;
+  if(ms_per_step)
+    *ms_per_step = best;
+  return FSPH_OK;
+}
+
+fsph_status fsph_ensemble_set_group_size(fsph_ensemble * e, int32_t group_size) {
+  if(!e || group_size < 0 || group_size > 32)
+    return FSPH_ERR_ARG;
+  ECK(cudaSetDevice(e->device));
+  for(auto s : e->lane_stream)
+    ECK(cudaStreamSynchronize(s));
+  for(auto & mb : e->m) {
+    ECK(cudaStreamSynchronize(mb.c->stream));
+    mb.c->p.group_size = group_size;
+  }
+  // the captured iterations hold the old group size
+  drop_graphs(e);
+  return FSPH_OK;
+}
+
+fsph_status fsph_ensemble_tune_shape(fsph_ensemble * e, int32_t steps_per_trial,
+  int32_t * lanes_chosen, int32_t * group_size_chosen, double * ms_per_step) {
+  if(!e || steps_per_trial < 1)
+    return FSPH_ERR_ARG;
+  const int sizes[] = {8, 16, 32};
+  double best = 1e300;
+  int best_l = e->lanes, best_g = 32;
+  for(int g : sizes) {
+    fsph_status s = fsph_ensemble_set_group_size(e, g);
+    if(s)
+      return s;
+    int32_t l = 0;
+    double ms = 0;
+    s = fsph_ensemble_tune(e, steps_per_trial, &l, &ms);
+    if(s)
+      return s;
+    if(ms < best) {
+      best = ms;
+      best_l = l;
+      best_g = g;
+    }
+  }
+  fsph_status s = fsph_ensemble_set_group_size(e, best_g);
+  if(!s)
+    s = set_lanes(e, best_l);
+  if(s)
+    return s;
+  if(lanes_chosen)
+    *lanes_chosen = best_l;
+  if(group_size_chosen)
+    *group_size_chosen = best_g;
   if(ms_per_step)
     *ms_per_step = best;
   return FSPH_OK;

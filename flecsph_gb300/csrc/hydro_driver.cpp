@@ -142,6 +142,7 @@ bool set_param(fsph_params & p, const std::string & kv) {
   else if(k == "pressure_updates_number") p.pressure_updates_number = (int32_t)v;
   else if(k == "initial_iteration") p.initial_iteration = (int64_t)std::atoll(kv.c_str() + eq + 1);
   else if(k == "initial_time") p.initial_time = v;
+  else if(k == "group_size") p.group_size = (int32_t)v;
   else
     return false;
   return true;

@@ -267,11 +267,12 @@ def noh2d(n1d=100, gamma=5.0 / 3.0, eta=1.5, P0=1e-6):
     return s, params, dict(problem="noh2d", n=n, dx=dx)
 
 
-def ensemble2d(nproblems=256, nmin=2000, nmax=200000, seed=2024):
+def ensemble2d(nproblems=256, nmin=2000, nmax=200000, seed=2020):
     """Many independent 2D problems: particle counts log-uniform in
     [nmin, nmax] (seeded), alternately a Sod tube (10:1 lattice) and a Noh
     disc, all in mixed precision.  Returns a list of (state, params, meta);
-    the actual counts follow from the lattices (recorded in meta)."""
+    the actual counts follow from the lattices (recorded in meta).  With
+    the default seed the 256 problems hold about 12.4M particles."""
     rng = np.random.Generator(np.random.PCG64(seed))
     target = np.exp(rng.uniform(math.log(nmin), math.log(nmax), nproblems))
     out = []

@@ -83,6 +83,9 @@ def library():
     lib.fsph_ensemble_set_lanes.argtypes = [C.c_void_p, C.c_int32]
     lib.fsph_ensemble_tune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_double)]
+    lib.fsph_ensemble_set_group_size.argtypes = [C.c_void_p, C.c_int32]
+    lib.fsph_ensemble_tune_shape.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     lib.fsph_ensemble_last_error.restype = C.c_char_p
     lib.fsph_ensemble_last_error.argtypes = [C.c_void_p]
     lib.fsph_ensemble_destroy.argtypes = [C.c_void_p]
@@ -369,6 +372,19 @@ class Ensemble:
 
     def set_lanes(self, lanes):
         self._check(self.lib.fsph_ensemble_set_lanes(self.ens, lanes), "ensemble_set_lanes")
+
+    def set_group_size(self, group_size):
+        self._check(self.lib.fsph_ensemble_set_group_size(self.ens, group_size),
+                    "set_group_size")
+
+    def tune_shape(self, steps_per_trial=2):
+        """Lanes and walk-group size (fsph_ensemble_tune_shape): returns
+        (lanes, group_size, ms_per_step)."""
+        l, g, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+        self._check(self.lib.fsph_ensemble_tune_shape(self.ens, steps_per_trial, C.byref(l),
+                                                      C.byref(g), C.byref(ms)),
+                    "tune_shape")
+        return l.value, g.value, ms.value
 
     def tune(self, steps_per_trial=3):
         lanes, ms = C.c_int32(0), C.c_double(0)

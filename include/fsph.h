@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FSPH_ABI_VERSION 5
+#define FSPH_ABI_VERSION 6
 
 /* Status codes.  They replace the reference's assert()/mpi_assert() aborts
  * (default_physics.h:134-143,215-226,636-651,661-691,918-979;
@@ -159,7 +159,9 @@ typedef struct fsph_params {
   int32_t precision_mode;            /* enum fsph_precision, default FP64 */
   int32_t max_neighbors;             /* neighbour-list capacity per particle, default 256 */
   int32_t gravity_order;             /* multipole order of fsph_gravitation: 1 or 2 (default 2) */
-  int32_t reserved_pad;
+  int32_t group_size;                /* particles per group of the neighbour and
+                                        gravity walks (one warp each): 1..32,
+                                        0 = 32 */
   /* Cullen & Dehnen adaptive viscosity (visc_cullen), param:: names */
   double sph_viscosity_alpha_max;    /* [516] 1.0 */
   double sph_viscosity_l;            /* [523] 0.05 */
@@ -486,6 +488,12 @@ fsph_status fsph_ensemble_set_lanes(fsph_ensemble * ens, int32_t lanes);
  * member meanwhile) and keeps the fastest. */
 fsph_status fsph_ensemble_tune(fsph_ensemble * ens, int32_t steps_per_trial,
   int32_t * lanes_chosen, double * ms_per_step);
+/* Sets every member's walk-group size (fsph_params.group_size, 0..32). */
+fsph_status fsph_ensemble_set_group_size(fsph_ensemble * ens, int32_t group_size);
+/* fsph_ensemble_tune for each walk-group size 8, 16 and 32; keeps the
+ * fastest (lanes, group size) pair. */
+fsph_status fsph_ensemble_tune_shape(fsph_ensemble * ens, int32_t steps_per_trial,
+  int32_t * lanes_chosen, int32_t * group_size_chosen, double * ms_per_step);
 const char * fsph_ensemble_last_error(const fsph_ensemble * ens);
 void fsph_ensemble_destroy(fsph_ensemble * ens);
 

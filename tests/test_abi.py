@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_abi_version(lib):
     lib.fsph_abi_version.restype = C.c_int32
-    assert lib.fsph_abi_version() == 5
+    assert lib.fsph_abi_version() == 6
 
 
 def test_params_defaults_match_header(lib):
@@ -37,7 +37,7 @@ def test_params_defaults_match_header(lib):
     lib.fsph_params_default(C.byref(p))
     q = abi.Params.defaults()
     for name, _ in abi.Params._fields_:
-        if name in ("reserved", "reserved_pad", "reserved_pad2"):
+        if name in ("reserved", "reserved_pad2"):
             continue
         a, b = getattr(p, name), getattr(q, name)
         if name == "external_force":
