@@ -155,6 +155,17 @@ __device__ __forceinline__ void kahan_g(R & s, R & c, R t) {
   s = u;
 }
 
+// Terms of a flush are summed plainly in blocks of GW_SUB and each block is
+// added to the compensated total: a plain sum over a whole flush (up to 128
+// terms) let its rounding, a fraction of the sum of |terms|, dominate where
+// the terms cancel (at the centre of a self-gravitating body).
+#define GW_SUB 8
+template<class R>
+__device__ __forceinline__ void fold_g(R & s, R & c, R & part) {
+  kahan_g(s, c, part);
+  part = (R)0;
+}
+
 // Shared-memory list records, one broadcast 16-byte load per quarter:
 //   mixed cell     {m, c - g} {q0..q3} {q4, q5, -, -}             48 B
 //                  (g: the group's reference point, see the walk)
@@ -359,6 +370,12 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
           py += fy;
           pz += fz;
           pp += phi;
+          if((k & (GW_SUB - 1)) == GW_SUB - 1) {
+            fold_g(sx, cx, px);
+            fold_g(sy, cy, py);
+            fold_g(sz, cz, pz);
+            fold_g(sp, cp, pp);
+          }
         }
         kahan_g(sx, cx, px);
         kahan_g(sy, cy, py);
@@ -396,6 +413,12 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
           py -= w3 * dy;
           pz -= w3 * dz;
           pp -= w;
+          if((k & (GW_SUB - 1)) == GW_SUB - 1) {
+            fold_g(sx, cx, px);
+            fold_g(sy, cy, py);
+            fold_g(sz, cz, pz);
+            fold_g(sp, cp, pp);
+          }
         }
         kahan_g(sx, cx, px);
         kahan_g(sy, cy, py);

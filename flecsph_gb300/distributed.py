@@ -433,7 +433,7 @@ class DistributedSystem:
                 continue
             lo = boxes[s, :self.dim].cpu().numpy()
             hi = boxes[s, self.dim:2 * self.dim].cpu().numpy()
-            parts.append(g.gravity_export(lo, hi, self.p.fmm_macangle))
+            parts.append(g.gravity_export(lo, hi, self.p.fmm_macangle).to(self.dev))
         cells = self.comm.alltoallv(torch.cat(parts), [len(c) for c in parts])
         if cells.shape[0]:
             g.gravity_import(cells)
@@ -569,6 +569,9 @@ class GpuEngine:
 
     def download(self):
         return self.bs.download_device(fields=DOUBLE_FIELDS + ["id"], device=self.device)
+
+    def gravity_export(self, box_lo, box_hi, theta):
+        return self.bs.gravity_export(box_lo, box_hi, theta, device=self.device)
 
     def __getattr__(self, name):
         return getattr(self.bs, name)
