@@ -53,10 +53,15 @@ sys.path.insert(0, ROOT)
 # include/fsph_work.h (the one table both this file and the design notes
 # use), parsed from the header.
 HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of the walk, per particle,
-# from a 96^3 capture (lists 341 MB, well above L2; the mean of two
-# launches, 488.3 MB / 884,736): profiles/k_neighbors_traffic_sedov3d_96.md
-MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum per particle of the
+# dominant kernel of a phase, from 96^3 Sedov captures (884,736 particles;
+# lists and records well above L2): the walk, the mean of two launches
+# (488.3 MB, profiles/k_neighbors_traffic_sedov3d_96.md); the float-float
+# density and acceleration passes and the de/dt pass of the warm-up
+# iteration (521.1, 569.4 and 593.5 MB,
+# profiles/k_density_ff_accel_ff_dedt_ahyd_sedov3d_96.md)
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9, "density": 589.0, "accel": 643.6,
+                                 "energy": 670.8}
 
 
 def read_work_header(path=os.path.join(ROOT, "include", "fsph_work.h")):
@@ -502,6 +507,7 @@ def gpu_arm(args):
         modes = ["fp64"]
     elif args.precision == "mixed":
         modes = ["mixed"]
+    cmp_state = None
     for mode in modes:
         p.precision_mode = PRECISION_MIXED if mode == "mixed" else PRECISION_FP64
         bs = sph.BodySystem(p, cap, device=local)
@@ -533,8 +539,15 @@ def gpu_arm(args):
         results[mode] = dict(ms=ms, timers=timers, launches=launches, nb_mean=nb_mean,
                              clocks=clk.summary(), ntot=ntot,
                              drift=drift(cons0, cons1, s, state))
-        # the accelerations of one pass from the input state
-        bs.read_bodies(s)
+        # one pass of each precision from one common state: the FP64 run's
+        # state after its timed steps (velocities and the blast or shear
+        # developed, so the energy rates are not trivially zero), real
+        # particles only (periodic copies carry ids >= n)
+        if cmp_state is None:
+            full = bs.download()
+            real = full["id"] < n
+            cmp_state = {f: np.ascontiguousarray(full[f][real]) for f in s}
+        bs.read_bodies(cmp_state)
         bs.update_iteration()
         bs.eos_init()
         if p.thermokinetic_formulation:
@@ -653,8 +666,9 @@ def gpu_arm(args):
                                  "accel_normwise": pf["a"]["normwise"],
                                  "per_field": pf,
                                  "measured_on": "one pass of each precision from the "
-                                                "input state (density, acceleration, "
-                                                "energy rate, gravity); per particle "
+                                                "FP64 run's state after its timed steps "
+                                                "(density, acceleration, energy rate, "
+                                                "gravity); per particle "
                                                 "|d|/|ref| for rho, P, c_s and "
                                                 "|d|/max(|ref|, 1e-3 rms|ref|) for a, "
                                                 "de/dt (du/dt), g_acc"}
