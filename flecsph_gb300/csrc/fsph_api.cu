@@ -488,6 +488,9 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->K.mass, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.velp, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.rc, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fv1, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fv2, N) == cudaSuccess;
+  ok &= dalloc(c, &c->K.fdv, N) == cudaSuccess;
   if(c->pp.cullen)
     ok &= dalloc(c, &c->K.visc, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.qscale, 4) == cudaSuccess;

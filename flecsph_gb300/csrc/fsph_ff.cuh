@@ -88,6 +88,11 @@ __device__ __forceinline__ ffloat ff_mul_f(ffloat a, float b) {
   return ff_make(p, e);
 }
 
+// a * c for a power of two c: exact, word by word
+__device__ __forceinline__ ffloat ff_scale2(ffloat a, float c) {
+  return ff_make(__fmul_rn(a.h, c), __fmul_rn(a.l, c));
+}
+
 __device__ __forceinline__ ffloat ff_sqr(ffloat a) {
   const float p = __fmul_rn(a.h, a.h);
   float e = __fmaf_rn(a.h, a.h, -p);

@@ -80,12 +80,17 @@ __global__ void k_grav_nodes(Particles P, int dim, Tree T, GravBuffers G,
   if(i >= n)
     return;
   double r0[3] = {0.0, 0.0, 0.0}, rc[3] = {0.0, 0.0, 0.0}, step[3] = {0.0, 0.0, 0.0};
+  // one step of the tree's fixed point, E / 2^31 on every axis (E: the
+  // largest range extent enlarged by 2^-19, as the positions were packed)
+  double E = 0.0;
   for(int d = 0; d < dim; ++d) {
     const double lo = ord_dec_g(rbits[d]), hi = ord_dec_g(rbits[3 + d]);
     r0[d] = lo;
     rc[d] = 0.5 * (lo + hi);
-    step[d] = (hi - lo) * (1.0 / 2147483648.0);
+    E = fmax(E, hi - lo);
   }
+  for(int d = 0; d < dim; ++d)
+    step[d] = E * (1.0 + 0x1p-19) * 0x1p-31;
   {
     // this particle for the walk: position relative to the corner, hi + lo
     float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
@@ -319,11 +324,44 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
       }
       const bool flush_m = nm > GW_MCAP - 32 || (done && nm > 0);
       const bool flush_p = np > GW_PCAP - 32 || (done && np > 0);
-      if(mem && flush_m) {
-        // plain sums over one flush (<= GW_MCAP terms), compensated into the
-        // totals at its end
+      // n terms summed plainly in blocks of GW_SUB, each block folded into
+      // the compensated totals: unrolled whole in the FP32 walk; the FP64
+      // walk, whose terms take twice the registers, keeps one loop
+      auto sum_terms = [&](int n, auto term) {
         R px = 0, py = 0, pz = 0, pp = 0;
-        for(int k = 0; k < nm; ++k) {
+        if constexpr(MIXED) {
+          int k = 0;
+          for(; k + GW_SUB <= n; k += GW_SUB) {
+#pragma unroll
+            for(int u = 0; u < GW_SUB; ++u)
+              term(k + u, px, py, pz, pp);
+            fold_g(sx, cx, px);
+            fold_g(sy, cy, py);
+            fold_g(sz, cz, pz);
+            fold_g(sp, cp, pp);
+          }
+          for(; k < n; ++k)
+            term(k, px, py, pz, pp);
+        }
+        else {
+          for(int k = 0; k < n; ++k) {
+            term(k, px, py, pz, pp);
+            if((k & (GW_SUB - 1)) == GW_SUB - 1) {
+              fold_g(sx, cx, px);
+              fold_g(sy, cy, py);
+              fold_g(sz, cz, pz);
+              fold_g(sp, cp, pp);
+            }
+          }
+        }
+        fold_g(sx, cx, px);
+        fold_g(sy, cy, py);
+        fold_g(sz, cz, pz);
+        fold_g(sp, cp, pp);
+      };
+      if(mem && flush_m) {
+        // one cell's potential and acceleration (monopole + quadrupole)
+        auto cell = [&](int k, R & px, R & py, R & pz, R & pp) {
           R m, dx, dy, dz, qxx, qyy, qzz, qxy, qxz, qyz;
           if(MIXED) {
             const float4 r0 = mf[3 * k];
@@ -370,21 +408,13 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
           py += fy;
           pz += fz;
           pp += phi;
-          if((k & (GW_SUB - 1)) == GW_SUB - 1) {
-            fold_g(sx, cx, px);
-            fold_g(sy, cy, py);
-            fold_g(sz, cz, pz);
-            fold_g(sp, cp, pp);
-          }
-        }
-        kahan_g(sx, cx, px);
-        kahan_g(sy, cy, py);
-        kahan_g(sz, cz, pz);
-        kahan_g(sp, cp, pp);
+        };
+        sum_terms(nm, cell);
       }
       if(mem && flush_p) {
-        R px = 0, py = 0, pz = 0, pp = 0;
-        for(int k = 0; k < np; ++k) {
+        // one particle's potential and acceleration; the particle itself
+        // drops out (fmm.h:136-137)
+        auto part = [&](int k, R & px, R & py, R & pz, R & pp) {
           int j;
           R m, dx, dy, dz;
           if(MIXED) {
@@ -404,7 +434,6 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
             dz = za - p1.x;
           }
           const R r2 = dx * dx + dy * dy + dz * dz;
-          // the particle itself drops out (fmm.h:136-137)
           const R ir = j == a ? (R)0
                               : (MIXED ? (R)rsqrtf((float)r2) : (R)rsqrt((double)r2));
           const R w = m * ir;
@@ -413,17 +442,8 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gravity_walk(Particles P,
           py -= w3 * dy;
           pz -= w3 * dz;
           pp -= w;
-          if((k & (GW_SUB - 1)) == GW_SUB - 1) {
-            fold_g(sx, cx, px);
-            fold_g(sy, cy, py);
-            fold_g(sz, cz, pz);
-            fold_g(sp, cp, pp);
-          }
-        }
-        kahan_g(sx, cx, px);
-        kahan_g(sy, cy, py);
-        kahan_g(sz, cz, pz);
-        kahan_g(sp, cp, pp);
+        };
+        sum_terms(np, part);
       }
       __syncwarp();
       if(flush_m)

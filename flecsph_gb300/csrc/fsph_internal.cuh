@@ -111,14 +111,26 @@ struct Tree {
 struct Packed {
   int4 * qpos;      // {qx, qy, qz, float bits of h}
   float4 * vhm;     // {vh_x, vh_y, vh_z, m}
-  float4 * vel;     // {v_x, v_y, v_z, 0}
+  float4 * vel;     // {v_x, v_y, v_z, c_s before the density pass}
   float4 * thermo;  // {rho, P/rho^2, c_s (new), c_s (previous)}
   float * mass;     // m alone, for the density pass (4 B per pair instead of 16)
   float4 * velp;    // de/dt pass: {v_x, v_y, v_z, P/rho^2}
+  // Records of the float-float acceleration pass and of the energy passes
+  // that carry v_half's low words (v - (float)v): a velocity difference
+  // taken as (high - high) + (low - low) keeps ~2^-24 of itself however
+  // large v is beside it (in a shear flow v_a - v_b is ~1e-3 of v, where
+  // FP32 records alone leave ~1e-5 of it).  v itself is v_half + (v -
+  // v_half), the second term in FP32: it is the step's kick, small beside
+  // v.  Filled four floats a record: the acceleration pass reads six
+  // 16-byte records a pair (fph, fpl, fmA, fv1, fv2, vel), the energy passes
+  // four (qpos, fv1, fv2, fdv).
+  float4 * fv1;     // {vh_x, vh_y, vh_z high words, rho}
+  float4 * fv2;     // {vh_x, vh_y, vh_z low words, c_s (of the density pass)}
+  float4 * fdv;     // energy passes: {v - v_half (FP32), m}
   float2 * rc;      // de/dt pass: {rho, c_s} (56 B per pair with qpos, vhm, velp)
   float2 * visc;    // Cullen & Dehnen: {c_s, sign(div v)} in the alpha pass,
                     // {alpha, 0} in the pair passes
-  float * qscale;   // device [3]: range extent / 2^31 per axis
+  float * qscale;   // device [3]: one fixed-point step per axis, E / 2^31 (E: the largest range extent enlarged by 2^-19)
   // Float-float records of the density and acceleration passes (Wendland
   // kernels).  Positions are X = 1 + (x - lo) / E with E the largest range
   // extent (slightly enlarged), so every X lies in [1, 2): the high words

@@ -18,47 +18,48 @@ __device__ __forceinline__ double ord_dec_m(unsigned long long u) {
 // ------------------------------------------------------------- packing --
 __global__ void k_pack_pos(Particles P, int dim,
   const unsigned long long * rbits, Packed K) {
-  // any monotone mapping shared by all particles will do: multiply by the
-  // reciprocal, computed once per block (FP64 division is costly here)
-  __shared__ double s_lo[3], s_inv[3], s_iE;
-  if(threadIdx.x < dim) {
-    const int d = threadIdx.x;
-    const double lo = ord_dec_m(rbits[d]), hi = ord_dec_m(rbits[3 + d]);
-    s_lo[d] = lo;
-    s_inv[d] = 2147483648.0 / (hi - lo);
-  }
+  // Every position as one 48-bit fixed-point word per axis,
+  //   F = round((x - lo) / E * 2^48),  E = the largest range extent
+  //   enlarged by 2^-19 (so F < 2^48 - 2^28),
+  // from which both packed forms follow by integer operations:
+  //   float-float X = 1 + F / 2^48 in [1, 2): the high word takes F's top
+  //     23 bits (exactly), the low word the other 25 (rounded to 24 bits);
+  //   the walk's 31-bit fixed point q = F / 2^17 rounded to nearest, one
+  //     step = E / 2^31 on every axis.
+  // Three FP64 operations per axis (subtract, scale, convert): this kernel
+  // runs on GB300's FP64 pipe, where divisions and splits cost most.
+  __shared__ double s_lo[3], s_sc, s_iE;
+  if(threadIdx.x < dim)
+    s_lo[threadIdx.x] = ord_dec_m(rbits[threadIdx.x]);
   if(threadIdx.x == 0) {
-    // float-float positions: X = 1 + (x - lo) / E in [1, 2 - 2^-20]
     double E = 0.0;
     for(int d = 0; d < dim; ++d)
       E = fmax(E, ord_dec_m(rbits[3 + d]) - ord_dec_m(rbits[d]));
     E *= 1.0 + 0x1p-19;
     s_iE = 1.0 / E;
+    s_sc = s_iE * 0x1p48;
     if(blockIdx.x == 0) {
       K.fscale[0] = E;
       K.fscale[1] = s_iE;
       // h_min == h_max: the pair passes take h_ab = h_a throughout
       K.fscale[2] = rbits[6] == rbits[7] ? 1.0 : 0.0;
+      for(int d = 0; d < 3; ++d)
+        K.qscale[d] = d < dim ? (float)(E * 0x1p-31) : 0.f;
     }
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i < 3 && i < dim) {
-    double ext = ord_dec_m(rbits[3 + i]) - ord_dec_m(rbits[i]);
-    K.qscale[i] = (float)(ext / 2147483648.0);
-  }
   if(i >= P.n)
     return;
+  const long long fmax48 = (1LL << 48) - (1LL << 28);
   int q[3] = {0, 0, 0};
   float xh[4] = {1.f, 1.f, 1.f, 0.f}, xl[4] = {0.f, 0.f, 0.f, 0.f};
   for(int d = 0; d < dim; ++d) {
-    double t = (P.f[F_X + d][i] - s_lo[d]) * s_inv[d];
-    t = fmin(fmax(t, 0.0), 2147483647.0);
-    q[d] = __double2int_rn(t);
-    const double X = fmin(fmax(1.0 + (P.f[F_X + d][i] - s_lo[d]) * s_iE, 1.0),
-      2.0 - 0x1p-20);
-    xh[d] = (float)X;
-    xl[d] = (float)(X - (double)xh[d]);
+    long long F = __double2ll_rn((P.f[F_X + d][i] - s_lo[d]) * s_sc);
+    F = F < 0 ? 0 : F > fmax48 ? fmax48 : F;
+    q[d] = (int)((F + (1LL << 16)) >> 17);
+    xh[d] = __int_as_float(0x3f800000 | (int)(F >> 25));
+    xl[d] = (float)(int)(F & ((1LL << 25) - 1)) * 0x1p-48f;
   }
   const double h = P.f[F_H][i];
   const double hX = h * s_iE;
@@ -85,15 +86,35 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= P.n)
     return;
+  // FP32 high word and low word of an FP64 velocity component
+  auto hl = [&](int f, float & h, float & l) {
+    const double v = P.f[f][i];
+    h = (float)v;
+    l = (float)(v - (double)h);
+  };
+  // the .w slots of fv1 and fv2 (rho, c_s) are written apart from their
+  // velocity words: by the density pass, or here from the FP64 state
+  float * w1 = (float *)&K.fv1[i];
+  float * w2 = (float *)&K.fv2[i];
   if(what & PACK_VHM) {
     const float m = (float)P.f[F_M][i];
-    K.vhm[i] = make_float4((float)P.f[F_VHX][i], (float)P.f[F_VHY][i],
-      dim == 3 ? (float)P.f[F_VHZ][i] : 0.f, m);
+    float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+    for(int d = 0; d < dim; ++d)
+      hl(F_VHX + d, h[d], l[d]);
+    K.vhm[i] = make_float4(h[0], h[1], h[2], m);
+    for(int d = 0; d < 3; ++d) {
+      w1[d] = h[d];
+      w2[d] = l[d];
+    }
     K.mass[i] = m;
   }
   if(what & PACK_VEL)
     K.vel[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
-      dim == 3 ? (float)P.f[F_VZ][i] : 0.f, 0.f);
+      dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)P.f[F_CS][i]);
+  if(what & (PACK_THERMO | PACK_DEDT)) {
+    w1[3] = (float)P.f[F_RHO][i];
+    w2[3] = (float)P.f[F_CS][i];
+  }
   if(what & PACK_THERMO) {
     const double rho = P.f[F_RHO][i], cs = P.f[F_CS][i];
     const double A = P.f[F_P][i] / (rho * rho);
@@ -114,6 +135,10 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
     K.velp[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)(P.f[F_P][i] / (rho * rho)));
     K.rc[i] = make_float2((float)rho, (float)P.f[F_CS][i]);
+    float dv[3] = {0.f, 0.f, 0.f};
+    for(int d = 0; d < dim; ++d)
+      dv[d] = (float)(P.f[F_VX + d][i] - P.f[F_VHX + d][i]);
+    K.fdv[i] = make_float4(dv[0], dv[1], dv[2], (float)P.f[F_M][i]);
   }
 }
 

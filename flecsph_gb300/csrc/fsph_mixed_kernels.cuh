@@ -198,20 +198,38 @@ __device__ __forceinline__ float gfac(float r, float h, float inv_h,
 
 // viscosity_function (viscosity.h:128-158): Monaghan's constant alpha and
 // beta, or Cullen & Dehnen's Pi with alpha_ab = (alpha_a + alpha_b) / 2
-// (default_physics.h:388).
+// (default_physics.h:388).  The FP32 pair terms divide with __fdividef
+// (two ulps, no special-case path): they carry FP32 rounding in any case.
 template<bool CULL>
 __device__ __forceinline__ float visc_pi_f(float alpha, float beta, float alpha_a,
   const Packed & Kp, int b, float rho_ab, float c_ab, float mu) {
   if(CULL) {
     const float al = 0.5f * (alpha_a + Kp.visc[b].x);
-    return -al * (c_ab - 2.f * mu) * mu / rho_ab;
+    return __fdividef(-al * (c_ab - 2.f * mu) * mu, rho_ab);
   }
-  return (-alpha * c_ab + beta * mu) * mu / rho_ab;
+  return __fdividef((-alpha * c_ab + beta * mu) * mu, rho_ab);
 }
 
 struct PairGeom {
   float dx, dy, dz, r2;
 };
+
+// (vh_a - vh_b) . d from the high words (fv1) and low words (fv2) of
+// v_half: the high-word and low-word differences are one rounding each, so
+// the difference keeps ~2^-24 of itself
+__device__ __forceinline__ float vdiff_dot(const float4 & ah, const float4 & al,
+  const float4 & bh, const float4 & bl, float dx, float dy, float dz) {
+  return ((ah.x - bh.x) + (al.x - bl.x)) * dx + ((ah.y - bh.y) + (al.y - bl.y)) * dy +
+         ((ah.z - bh.z) + (al.z - bl.z)) * dz;
+}
+
+// (v_a - v_b) . d with v = v_half + (v - v_half) (fv1, fv2, fdv)
+__device__ __forceinline__ float vel_diff_dot(const float4 & h1a, const float4 & h2a,
+  const float4 & dva, const float4 & h1b, const float4 & h2b, const float4 & dvb,
+  float dx, float dy, float dz) {
+  return vdiff_dot(h1a, h2a, h1b, h2b, dx, dy, dz) +
+         ((dva.x - dvb.x) * dx + (dva.y - dvb.y) * dy + (dva.z - dvb.z) * dz);
+}
 
 template<int D>
 __device__ __forceinline__ PairGeom geom(const int4 & qa, const int4 & qb,
@@ -262,7 +280,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_density_mixed(Particles P,
       const float mb = Kp.mass[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
-      const float ih = 1.0f / hab;
+      const float ih = __fdividef(1.f, hab);
       const float r = sqrtf(g.r2);
       const float w = mb * wfun<D, K>(r, hab, ih, pp);
       kahan(sum, comp, j0 + u < cnt ? w : 0.f);
@@ -351,14 +369,14 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_accel_mixed(Particles P,
       const int4 qb = Kp.qpos[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
-      const float ih = 1.0f / hab;
+      const float ih = __fdividef(1.f, hab);
       const float r = sqrtf(g.r2);
       const float f = gfac<D, K>(r, hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
       const float4 tb = Kp.thermo[b];
       const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
                          (vha.z - vhb.z) * g.dz;
-      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float mu = dotp < 0.f ? __fdividef(hab * dotp, g.r2 + eps * hab * hab) : 0.f;
       const float rho_ab = 0.5f * (ta.x + tb.x);
       const float c_ab = 0.5f * (ta.z + tb.z);
       const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
@@ -406,8 +424,15 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_accel_mixed(Particles P,
 // The same records as the de/dt pass ({v, .} and {rho, c_s}: 56 B per pair);
 // then_op (OP_RECOMPUTE or OP_RECOMPUTE_KICK_U, else 0) applies the
 // element-wise update that follows du/dt in the driver to the particle.
+// Resident blocks of 256 per SM of the du/dt and de/dt (through a^P)
+// passes: 3 gives them 80 registers, enough for four pairs' records in
+// flight with the velocities' low words and no spills.
+#ifndef FSPH_ENERGY_BLOCKS
+#define FSPH_ENERGY_BLOCKS 3
+#endif
+
 template<int D, int K, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS, 4) k_dudt_mixed(Particles P,
+__global__ void __launch_bounds__(MIX_THREADS, FSPH_ENERGY_BLOCKS) k_dudt_mixed(Particles P,
   PhysParams pp, Lists Ls, Packed Kp, const DevTime * tm, int then_op) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
@@ -422,9 +447,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dudt_mixed(Particles P,
   const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
   const int4 qa = Kp.qpos[a];
   const float ha = __int_as_float(qa.w);
-  const float4 vha = Kp.vhm[a];
-  const float4 va = Kp.velp[a];
-  const float2 ra = Kp.rc[a];
+  const float4 h1a = Kp.fv1[a], h2a = Kp.fv2[a], dva = Kp.fdv[a];
   const int cnt = Ls.cnt[a];
   float dp = 0.f, cp = 0.f, dv = 0.f, cv = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
@@ -437,20 +460,16 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dudt_mixed(Particles P,
       const int4 qb = Kp.qpos[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
-      const float ih = 1.0f / hab;
+      const float ih = __fdividef(1.f, hab);
       const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
-      const float4 vhb = Kp.vhm[b];
-      const float4 vb = Kp.velp[b];
-      const float2 rb = Kp.rc[b];
-      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
-                         (vha.z - vhb.z) * g.dz;
-      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
-        0.5f * (ra.y + rb.y), mu);
-      const float vdw = f * ((va.x - vb.x) * g.dx + (va.y - vb.y) * g.dy +
-                             (va.z - vb.z) * g.dz);
-      kahan(dp, cp, vhb.w * vdw);
-      kahan(dv, cv, vhb.w * vdw * Pi);
+      const float4 h1b = Kp.fv1[b], h2b = Kp.fv2[b], dvb = Kp.fdv[b];
+      const float dotp = vdiff_dot(h1a, h2a, h1b, h2b, g.dx, g.dy, g.dz);
+      const float mu = dotp < 0.f ? __fdividef(hab * dotp, g.r2 + eps * hab * hab) : 0.f;
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (h1a.w + h1b.w),
+        0.5f * (h2a.w + h2b.w), mu);
+      const float vdw = f * vel_diff_dot(h1a, h2a, dva, h1b, h2b, dvb, g.dx, g.dy, g.dz);
+      kahan(dp, cp, dvb.w * vdw);
+      kahan(dv, cv, dvb.w * vdw * Pi);
     }
   }
   const double sp = (double)dp - (double)cp, sv = (double)dv - (double)cv;
@@ -503,14 +522,14 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_mixed(Particles P,
       const int4 qb = Kp.qpos[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
-      const float ih = 1.0f / hab;
+      const float ih = __fdividef(1.f, hab);
       const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
       const float4 vhb = Kp.vhm[b];
       const float4 vb = Kp.velp[b];
       const float2 rb = Kp.rc[b];
       const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
                          (vha.z - vhb.z) * g.dz;
-      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
+      const float mu = dotp < 0.f ? __fdividef(hab * dotp, g.r2 + eps * hab * hab) : 0.f;
       const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
         0.5f * (ra.y + rb.y), mu);
       const float vad = f * (va.x * g.dx + va.y * g.dy + va.z * g.dz);
@@ -576,12 +595,12 @@ __device__ __forceinline__ ffloat ff_wpoly(ffloat t) {
   const ffloat t2 = ff_sqr(t);
   const ffloat t4 = ff_sqr(t2);
   if(K == FSPH_KERNEL_WENDLAND_C2)
-    return ff_mul(t4, ff_cadd(5.f, ff_mul_f(t, -4.f)));
+    return ff_mul(t4, ff_cadd(5.f, ff_scale2(t, -4.f)));
   if(K == FSPH_KERNEL_WENDLAND_C4) {
     const ffloat p = ff_cadd(56.f, ff_mul(ff_cadd(-88.f, ff_mul_f(t, 35.f)), t));
     return ff_mul(ff_mul(t4, t2), p);
   }
-  const ffloat a1 = ff_cadd(121.f, ff_mul_f(t, -32.f));
+  const ffloat a1 = ff_cadd(121.f, ff_scale2(t, -32.f));
   const ffloat a2 = ff_cadd(-154.f, ff_mul(a1, t));
   const ffloat p = ff_cadd(66.f, ff_mul(a2, t));
   return ff_mul(ff_sqr(t4), p);
@@ -595,7 +614,7 @@ __device__ __forceinline__ ffloat ff_gpoly(ffloat t) {
   const ffloat t4 = ff_sqr(t2);
   if(K == FSPH_KERNEL_WENDLAND_C4)
     return ff_mul(ff_mul(t4, t), ff_cadd(6.f, ff_mul_f(t, -5.f)));
-  const ffloat b1 = ff_cadd(-39.f, ff_mul_f(t, 16.f));
+  const ffloat b1 = ff_cadd(-39.f, ff_scale2(t, 16.f));
   const ffloat p = ff_cadd(24.f, ff_mul(b1, t));
   return ff_mul(ff_mul(ff_mul(t4, t2), t), p);
 }
@@ -760,6 +779,8 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   cs_new[a] = cs;
   const double A = Pa / (rho * rho);
   Kp.thermo[a] = make_float4((float)rho, (float)A, (float)cs, (float)P.f[F_CS][a]);
+  ((float *)&Kp.fv1[a])[3] = (float)rho;
+  ((float *)&Kp.fv2[a])[3] = (float)cs;
   const float Ah = (float)A;
   ((float2 *)Kp.fmA)[2 * a + 1] = make_float2(Ah, (float)(A - (double)Ah));
   if(CULL) {
@@ -772,23 +793,24 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   }
 }
 
-// Acceleration with the pressure-gradient sum in float-float:
+// Acceleration
 //   a_a = -sum_b m_b (P_a/rho_a^2 + P_b/rho_b^2 + Pi_ab) grad_a W_ab
-// and, with VSIG, the signal speed of the density pass (FP32, as
-// k_vsig_mixed).  With UNI (every h equal) 1/h^(D+2) multiplies the
-// finished sums instead of every pair.  The viscous part is also summed on
-// its own in FP32 (Kahan) so that the pass can leave the pressure-only
-// acceleration for the de/dt pass.
+// as two sums: the pressure terms, which cancel, in float-float, and the
+// viscous terms (Pi is FP32) in FP32 with Kahan compensation; with VSIG,
+// also the signal speed of the density pass (FP32, as k_vsig_mixed).  With
+// UNI (every h equal) 1/h^(D+2) multiplies the finished sums instead of
+// every pair.  The pressure sum alone is the pressure-only acceleration the
+// de/dt pass takes.
 struct AccelFFState {
-  ffloat sx, sy, sz;     // the whole pair sum (pressure and viscosity)
-  float vx, vy, vz;      // its viscous part
+  ffloat sx, sy, sz;     // the pressure sum
+  float vx, vy, vz;      // the viscous sum
   float vsig;
 };
 
 template<int D, int K, bool VSIG, bool CULL, bool UNI>
 __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
   int cnt, int a, const float4 & pa, const float4 & la, const ffloat & iha,
-  const ffloat & ihPa, const ffloat & Aa, const float4 & vha, const float4 & ta,
+  const ffloat & ihPa, const ffloat & Aa, const float4 & h1a, const float4 & h2a,
   const float4 & va, float eps, float alpha, float beta, float alpha_a,
   AccelFFState & out) {
   ffloat sx = ff_make(0.f, 0.f), sy = sx, sz = sx;
@@ -808,20 +830,18 @@ __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
       }
       const ffloat q = ff_mul(g.r, ih);
       const ffloat t = ff_cadd(1.f, ff_make(-q.h, -q.l));
-      const float4 vhb = Kp.vhm[b];
-      const float4 tb = Kp.thermo[b];
+      const float4 h1b = Kp.fv1[b], h2b = Kp.fv2[b];  // v_half, rho, c_s
       const float4 mAb = Kp.fmA[b];
       // viscosity in FP32 (the position unit cancels in mu)
       const float hab = 0.5f * (pa.w + pb.w);
-      const float dotp = (vha.x - vhb.x) * g.dxr[0] + (vha.y - vhb.y) * g.dxr[1] +
-                         (vha.z - vhb.z) * g.dxr[2];
-      const float mu = dotp < 0.f ? hab * dotp / (g.r2f + eps * hab * hab) : 0.f;
-      const float rho_ab = 0.5f * (ta.x + tb.x);
-      const float c_ab = 0.5f * (ta.z + tb.z);
+      const float dotp = vdiff_dot(h1a, h2a, h1b, h2b, g.dxr[0], g.dxr[1], g.dxr[2]);
+      const float mu = dotp < 0.f ? __fdividef(hab * dotp, g.r2f + eps * hab * hab) : 0.f;
+      const float rho_ab = 0.5f * (h1a.w + h1b.w);
+      const float c_ab = 0.5f * (h2a.w + h2b.w);
       const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, rho_ab, c_ab, mu);
       const ffloat gp = ff_gpoly<K>(t);
-      ffloat S = ff_add_f(ff_add(Aa, ff_make(mAb.z, mAb.w)), Pi);
-      S = ff_mul(ff_mul(S, ff_make(mAb.x, mAb.y)), gp);
+      ffloat S = ff_mul(ff_mul(ff_add(Aa, ff_make(mAb.z, mAb.w)), ff_make(mAb.x, mAb.y)),
+        gp);
       float V = mAb.x * Pi * gp.h;
       if(!UNI) {
         S = ff_mul(S, ihP);
@@ -832,11 +852,11 @@ __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
         V = 0.f;
       }
       if(VSIG) {
-        const float4 vb = Kp.vel[b];
+        const float4 vb = Kp.vel[b];  // .w: c_s before the density pass
         const float dotv = ((va.x - vb.x) * g.dxr[0] + (va.y - vb.y) * g.dxr[1] +
                              (va.z - vb.z) * g.dxr[2]) * rsqrtf(g.r2f);
-        const float cb = b > a ? tb.z : tb.w;
-        const float cand = fmaxf(ta.z, cb) - fminf(dotv, 0.f);
+        const float cb = b > a ? h2b.w : vb.w;
+        const float cand = fmaxf(h2a.w, cb) - fminf(dotv, 0.f);
         vsig = fmaxf(vsig, (b != a && g.r2f > 0.f) ? cand : 0.f);
       }
       // padding slots and the self pair have dx = 0 and add nothing
@@ -873,9 +893,12 @@ __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
 #ifndef FSPH_ACCEL_FF_BLOCKS
 #define FSPH_ACCEL_FF_BLOCKS 2
 #endif
+#ifndef FSPH_ACCEL_FF_THREADS
+#define FSPH_ACCEL_FF_THREADS MIX_THREADS
+#endif
 
 template<int D, int K, bool VSIG, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
+__global__ void __launch_bounds__(FSPH_ACCEL_FF_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
   Particles P, PhysParams pp, Lists Ls, Packed Kp, int kick, const DevTime * tm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if(a >= P.n)
@@ -887,8 +910,7 @@ __global__ void __launch_bounds__(MIX_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
   const ffloat Aa = ff_make(Aa2.x, Aa2.y);
   const ffloat iha = ff_rcp_scaled(ff_make(pa.w, la.w), 1.f);
   const ffloat ihPa = ff_ipow<D + 2>(iha);
-  const float4 vha = Kp.vhm[a];
-  const float4 ta = Kp.thermo[a];
+  const float4 h1a = Kp.fv1[a], h2a = Kp.fv2[a];
   const int cnt = Ls.cnt[a];
   float4 va = make_float4(0.f, 0.f, 0.f, 0.f);
   if(VSIG)
@@ -896,23 +918,23 @@ __global__ void __launch_bounds__(MIX_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   AccelFFState r;
   if(Kp.fscale[2] != 0.0)
-    accel_ff_sum<D, K, VSIG, CULL, true>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, vha,
-      ta, va, eps, alpha, beta, alpha_a, r);
+    accel_ff_sum<D, K, VSIG, CULL, true>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
+      h2a, va, eps, alpha, beta, alpha_a, r);
   else
-    accel_ff_sum<D, K, VSIG, CULL, false>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, vha,
-      ta, va, eps, alpha, beta, alpha_a, r);
+    accel_ff_sum<D, K, VSIG, CULL, false>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
+      h2a, va, eps, alpha, beta, alpha_a, r);
   const double iE = Kp.fscale[1];
   const double iE2 = iE * iE;
   // a = -gconst / E^(D+1) * sum
   const double scale = -ff_gconst<D, K>() * (D == 3 ? iE2 * iE2 : iE2 * iE);
-  double acc[3] = {scale * ff_to_double(r.sx), scale * ff_to_double(r.sy),
+  const double ap[3] = {scale * ff_to_double(r.sx), scale * ff_to_double(r.sy),
     D == 3 ? scale * ff_to_double(r.sz) : 0.0};
+  double acc[3] = {ap[0] + scale * (double)r.vx, ap[1] + scale * (double)r.vy,
+    D == 3 ? ap[2] + scale * (double)r.vz : 0.0};
   if(Kp.ahyd) {
-    // pressure-only hydro acceleration: the whole sum less its viscous part
-    const double av[3] = {scale * (double)r.vx, scale * (double)r.vy,
-      scale * (double)r.vz};
+    // the pressure-only hydro acceleration for the de/dt pass
     for(int d = 0; d < D; ++d)
-      Kp.ahyd[(size_t)d * P.n + a] = acc[d] - av[d];
+      Kp.ahyd[(size_t)d * P.n + a] = ap[d];
   }
   if(pp.has_eacc) {  // acc_a += external_force::acceleration (:404)
     const double pos[3] = {P.f[F_X][a], P.f[F_Y][a], D == 3 ? P.f[F_Z][a] : 0.0};
@@ -948,7 +970,7 @@ __global__ void __launch_bounds__(MIX_THREADS, FSPH_ACCEL_FF_BLOCKS) k_accel_ff(
 // positions, P/rho^2, v_half and alpha are those of the acceleration pass
 // (the caller tracks that).
 template<int D, int K, bool CULL>
-__global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_ahyd(Particles P,
+__global__ void __launch_bounds__(MIX_THREADS, FSPH_ENERGY_BLOCKS) k_dedt_ahyd(Particles P,
   PhysParams pp, Lists Ls, Packed Kp, int then_op, const DevTime * tm,
   DevStatus * st) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -959,9 +981,8 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_ahyd(Particles P,
   const float alpha_a = CULL ? Kp.visc[a].x : 0.f;
   const int4 qa = Kp.qpos[a];
   const float ha = __int_as_float(qa.w);
-  const float4 vha = Kp.vhm[a];
-  const float4 va = Kp.velp[a];  // .w = P_a / rho_a^2
-  const float2 ra = Kp.rc[a];
+  const float4 h1a = Kp.fv1[a], h2a = Kp.fv2[a], dva = Kp.fdv[a];
+  const float Aa = Kp.fmA[a].z;  // P_a / rho_a^2 (high word)
   const int cnt = Ls.cnt[a];
   float sum = 0.f, comp = 0.f;
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
@@ -973,21 +994,19 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_dedt_ahyd(Particles P,
       const int4 qb = Kp.qpos[b];
       const PairGeom g = geom<D>(qa, qb, s0, s1, s2);
       const float hab = 0.5f * (ha + __int_as_float(qb.w));
-      const float ih = 1.0f / hab;
+      const float ih = __fdividef(1.f, hab);
       const float f = gfac<D, K>(sqrtf(g.r2), hab, ih, pp);
-      const float4 vhb = Kp.vhm[b];
-      const float4 vb = Kp.velp[b];
-      const float2 rb = Kp.rc[b];
-      const float dotp = (vha.x - vhb.x) * g.dx + (vha.y - vhb.y) * g.dy +
-                         (vha.z - vhb.z) * g.dz;
-      const float mu = dotp < 0.f ? hab * dotp / (g.r2 + eps * hab * hab) : 0.f;
-      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (ra.x + rb.x),
-        0.5f * (ra.y + rb.y), mu);
-      const float vbad = f * ((vb.x - va.x) * g.dx + (vb.y - va.y) * g.dy +
-                              (vb.z - va.z) * g.dz);
-      const float vsd = f * ((va.x + vb.x) * g.dx + (va.y + vb.y) * g.dy +
-                             (va.z + vb.z) * g.dz);
-      kahan(sum, comp, vhb.w * (va.w * vbad + 0.5f * Pi * vsd));
+      const float4 h1b = Kp.fv1[b], h2b = Kp.fv2[b], dvb = Kp.fdv[b];
+      const float dotp = vdiff_dot(h1a, h2a, h1b, h2b, g.dx, g.dy, g.dz);
+      const float mu = dotp < 0.f ? __fdividef(hab * dotp, g.r2 + eps * hab * hab) : 0.f;
+      const float Pi = visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b, 0.5f * (h1a.w + h1b.w),
+        0.5f * (h2a.w + h2b.w), mu);
+      // v_b - v_a and v_a + v_b, v = v_half + (v - v_half)
+      const float vbad = f * vel_diff_dot(h1b, h2b, dvb, h1a, h2a, dva, g.dx, g.dy, g.dz);
+      const float vsd = f * (((h1a.x + h1b.x) + (dva.x + dvb.x)) * g.dx +
+                             ((h1a.y + h1b.y) + (dva.y + dvb.y)) * g.dy +
+                             ((h1a.z + h1b.z) + (dva.z + dvb.z)) * g.dz);
+      kahan(sum, comp, dvb.w * (Aa * vbad + 0.5f * Pi * vsd));
     }
   }
   double gv = 0, vah = 0;
@@ -1132,7 +1151,7 @@ template<bool CULL>
 inline void run_accel_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
   const DevTime * t, int fused_vsig) {
-  const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
+  int threads = MIX_THREADS;
   void (*fn)(Particles, PhysParams, Lists, Packed, int, const DevTime *) = nullptr;
 #define PICK(D, KK)                                                            \
   fn = fused_vsig ? k_accel_mixed<D, KK, true, CULL> : k_accel_mixed<D, KK, false, CULL>
@@ -1174,9 +1193,10 @@ inline void run_accel_mixed(const Launch & L, const Particles & P,
       else if(pp.kernel == FSPH_KERNEL_WENDLAND_C4) PICK(2, FSPH_KERNEL_WENDLAND_C4);
       else PICK(2, FSPH_KERNEL_WENDLAND_C6);
     }
+    threads = FSPH_ACCEL_FF_THREADS;
   }
 #undef PICK
-  fn<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp, Ls, K, kick, t);
+  fn<<<(P.n + threads - 1) / threads, threads, 0, L.stream>>>(P, pp, Ls, K, kick, t);
   *L.counter += 1;
 }
 

@@ -195,8 +195,15 @@ cudaError_t launch_range_keys(const Launch & L, const Particles & P,
 // histogram per tile, one exclusive scan over [digit][tile], then a stable
 // scatter in which each tile ranks its keys with warp match/ballot.
 #define RS_THREADS 256
+#ifndef RS_ITEMS
 #define RS_ITEMS 16
+#endif
 #define RS_TILE (RS_THREADS * RS_ITEMS)
+// resident scatter blocks per SM (each holds its tile, 12 B a key, in
+// shared memory)
+#ifndef RS_SCATTER_BLOCKS
+#define RS_SCATTER_BLOCKS 3
+#endif
 
 size_t radix_hist_entries(int n) {
   size_t nb = ((size_t)n + RS_TILE - 1) / RS_TILE;
@@ -265,18 +272,27 @@ __global__ void __launch_bounds__(1024) k_scan_rows(unsigned * hist, int nb,
     tot[d] = run;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
+// Stable scatter of one tile.  Warp w owns the tile's items
+// [w * 32 * RS_ITEMS, (w + 1) * 32 * RS_ITEMS) and ranks them within their
+// digits with a warp-private count per digit (match/ballot per round of 32
+// keys, no block barrier); one scan per digit over the warps then gives
+// every key its place in the tile sorted by digit (tile order kept), the
+// tile is placed there in shared memory and written out in that order, so
+// the keys of one digit leave the tile as one run of consecutive addresses.
+#define RS_DYN_SMEM ((size_t)RS_TILE * 12)
+__global__ void __launch_bounds__(RS_THREADS, RS_SCATTER_BLOCKS) k_radix_scatter(
   const unsigned long long * kin, const int * vin, unsigned long long * kout,
   int * vout, int n, int shift, const unsigned * offs) {
-  __shared__ unsigned base[256];
-  __shared__ unsigned running[256];
+  extern __shared__ __align__(16) unsigned char rs_dyn[];
+  unsigned long long * skey = (unsigned long long *)rs_dyn;
+  int * sval = (int *)(rs_dyn + (size_t)RS_TILE * 8);
+  __shared__ unsigned base[256];   // where the tile's run of each digit goes
+  __shared__ unsigned toff[256];   // where each digit starts in the sorted tile
   __shared__ unsigned wcnt[RS_THREADS / 32][256];
   __shared__ unsigned wtot[RS_THREADS / 32];
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-  // digit base = sum of the totals of smaller digits (block-wide scan of
-  // the 256 row totals) + this tile's offset within its digit row
-  {
-    const unsigned v = offs[256 * gridDim.x + t];
+  // exclusive block scan of one value per thread (256 threads)
+  auto block_scan = [&](unsigned v) {
     unsigned x = v;
     for(int o = 1; o < 32; o <<= 1) {
       unsigned y = __shfl_up_sync(FULL, x, o);
@@ -289,66 +305,90 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
     unsigned pre = 0;
     for(int k = 0; k < w; ++k)
       pre += wtot[k];
-    base[t] = pre + x - v + offs[t * gridDim.x + blockIdx.x];
-  }
-  running[t] = 0;
+    __syncthreads();
+    return pre + x - v;
+  };
+  // digit base = sum of the totals of smaller digits + this tile's offset
+  // within its digit row
+  base[t] = block_scan(offs[256 * gridDim.x + t]) + offs[t * gridDim.x + blockIdx.x];
   for(int k = 0; k < RS_THREADS / 32; ++k)
     wcnt[k][t] = 0;
-  // the tile's keys and values into registers first: all loads in flight
-  // at once instead of one dependent load per ranking round
+  // this warp's keys into registers first: all loads in flight (the
+  // values follow when the keys are placed)
   const int tile = blockIdx.x * RS_TILE;
+  const int wbase = tile + w * 32 * RS_ITEMS;
   unsigned long long kreg[RS_ITEMS];
-  int vreg[RS_ITEMS];
 #pragma unroll
   for(int r = 0; r < RS_ITEMS; ++r) {
-    const int i = tile + r * RS_THREADS + t;
+    const int i = wbase + r * 32 + lane;
     kreg[r] = i < n ? kin[i] : 0ull;
-    vreg[r] = i < n ? vin[i] : 0;
   }
   __syncthreads();
   const unsigned lt = lanemask_lt();
+  unsigned * cnt = wcnt[w];
+  unsigned rk[RS_ITEMS];  // digit << 16 | rank within the digit in this warp
 #pragma unroll
   for(int r = 0; r < RS_ITEMS; ++r) {
-    int i = tile + r * RS_THREADS + t;
-    bool valid = i < n;
-    unsigned long long key = kreg[r];
-    int digit = valid ? (int)((key >> shift) & 255) : 256;
-    unsigned mask = __match_any_sync(FULL, digit);
-    int rank = __popc(mask & lt);
-    bool leader = (__ffs(mask) - 1) == lane;
-    if(valid && leader)
-      wcnt[w][digit] = __popc(mask);
-    __syncthreads();
-    if(valid) {
-      unsigned pre = running[digit];
-      for(int k = 0; k < w; ++k)
-        pre += wcnt[k][digit];
-      unsigned pos = base[digit] + pre + rank;
-      kout[pos] = key;
-      vout[pos] = vreg[r];
+    const bool valid = wbase + r * 32 + lane < n;
+    const int digit = valid ? (int)((kreg[r] >> shift) & 255) : 256;
+    const unsigned mask = __match_any_sync(FULL, digit);
+    const unsigned before = valid ? cnt[digit] : 0u;
+    __syncwarp();
+    if(valid && (__ffs(mask) - 1) == lane)
+      cnt[digit] = before + __popc(mask);
+    __syncwarp();
+    rk[r] = ((unsigned)(valid ? digit : 0) << 16) | (before + __popc(mask & lt));
+  }
+  __syncthreads();
+  // per digit (thread t): exclusive prefix over the warps, then the start of
+  // the digit in the sorted tile
+  unsigned run = 0;
+  for(int k = 0; k < RS_THREADS / 32; ++k) {
+    const unsigned c = wcnt[k][t];
+    wcnt[k][t] = run;
+    run += c;
+  }
+  toff[t] = block_scan(run);
+  __syncthreads();
+#pragma unroll
+  for(int r = 0; r < RS_ITEMS; ++r) {
+    const int i = wbase + r * 32 + lane;
+    if(i < n) {
+      const unsigned d = rk[r] >> 16;
+      const unsigned l = toff[d] + cnt[d] + (rk[r] & 0xffffu);
+      skey[l] = kreg[r];
+      sval[l] = vin[i];
     }
-    __syncthreads();
-    unsigned s = 0;
-    for(int k = 0; k < RS_THREADS / 32; ++k) {
-      s += wcnt[k][t];
-      wcnt[k][t] = 0;
-    }
-    running[t] += s;
-    __syncthreads();
+  }
+  __syncthreads();
+  const int ntile = n - tile < RS_TILE ? n - tile : RS_TILE;
+  for(int l = t; l < ntile; l += RS_THREADS) {
+    const unsigned long long key = skey[l];
+    const int d = (int)((key >> shift) & 255);
+    const unsigned pos = base[d] + ((unsigned)l - toff[d]);
+    kout[pos] = key;
+    vout[pos] = sval[l];
   }
 }
 
 cudaError_t radix_sort_pairs(const Launch & L, unsigned long long * keys,
   int * vals, unsigned long long * keys_tmp, int * vals_tmp, int n,
   unsigned * hist, int) {
+  static std::atomic<unsigned long long> attr_devices{0};
+  cudaError_t ae = once_per_device(&attr_devices, []() {
+    return cudaFuncSetAttribute(k_radix_scatter,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_DYN_SMEM);
+  });
+  if(ae != cudaSuccess)
+    return ae;
   int nb = (n + RS_TILE - 1) / RS_TILE;
   unsigned long long *ka = keys, *kb = keys_tmp;
   int *va = vals, *vb = vals_tmp;
   for(int shift = 0; shift < 64; shift += 8) {
     k_radix_hist<<<nb, RS_THREADS, 0, L.stream>>>(ka, n, shift, hist);
     k_scan_rows<<<256, 1024, 0, L.stream>>>(hist, nb, hist + (size_t)256 * nb);
-    k_radix_scatter<<<nb, RS_THREADS, 0, L.stream>>>(ka, va, kb, vb, n, shift,
-      hist);
+    k_radix_scatter<<<nb, RS_THREADS, RS_DYN_SMEM, L.stream>>>(ka, va, kb, vb, n,
+      shift, hist);
     *L.counter += 3;
     unsigned long long * tk = ka;
     ka = kb;
@@ -496,12 +536,16 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
     for(int d = 0; d < dim; ++d)
       rc[d] = 0.5 * (ord_dec(rbits[d]) + ord_dec(rbits[3 + d]));
   int p = T.leaf_parent[i];
-  // Leaves write nothing here, and each node's writes are fenced before the
-  // thread moves up, so one fence per level orders a node's data before the
-  // arrival count its parent's second thread reads it after (with __ldcg,
-  // from L2).
+  // Leaves write nothing here.  The arrival count at the parent is an
+  // acquire-release atomic at device scope: it publishes this thread's
+  // node data (release) to the sibling's thread, which reads it after its
+  // own arrival (acquire; the reads go through L2 with __ldcg), so no
+  // full fence is needed per level.
   while(p >= 0) {
-    if(atomicAdd(&T.counter[p], 1u) == 0)
+    unsigned prior;
+    asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
+                 : "=r"(prior) : "l"(T.counter + p) : "memory");
+    if(prior == 0)
       return;  // the sibling subtree is not finished yet
     if(T.gmom) {
       double S[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -598,7 +642,6 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       T.fbox2[2 * p] = make_float4(fl[0], fl[1], fl[2], 0.f);
       T.fbox2[2 * p + 1] = make_float4(fh[0], fh[1], fh[2], 0.f);
     }
-    __threadfence();
     p = T.parent[p];
   }
 }
@@ -713,6 +756,18 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
 #define NB_BLOCKS_PER_SM 20
 #endif
 #define NB_ORDERED_BLOCKS_PER_SM 8
+// The mixed walk comes in two variants, one for runs in which every h is
+// equal and one for varying h; both are launched and each returns at once
+// unless the device's range words select it.  The equal-h variant keeps
+// none of the reference node-test state (FP64 group box, reference group,
+// FP32 centre) and no candidate h, so it fits more warps per SM.
+#ifndef NB_UNI_BLOCKS_PER_SM
+#define NB_UNI_BLOCKS_PER_SM 24
+#endif
+#ifndef NB_UNI_CAND
+#define NB_UNI_CAND 256
+#endif
+enum { NB_MODE_UNI = 0, NB_MODE_VAR = 1, NB_MODE_ORDERED = 2 };
 
 __device__ __forceinline__ void warp_bitonic(unsigned long long * a, int m,
   int lane) {
@@ -895,14 +950,20 @@ __device__ __forceinline__ bool box_near(int4 glo, int4 ghi, float hg,
 // which the reference's breadth-first walk appends neighbours; when the
 // candidates of a group did not fit one chunk, every member's list is
 // sorted by the same key at the end.
-template<bool ORDERED>
+template<int MODE>
 __global__ void __launch_bounds__(NB_WARPS * 32,
-  ORDERED ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM) k_neighbors(Particles P,
-  Tree T, Lists Ls, DevStatus * st, int dim, const unsigned long long * rbits,
-  Packed K) {
+  MODE == NB_MODE_ORDERED ? NB_ORDERED_BLOCKS_PER_SM
+  : MODE == NB_MODE_UNI ? NB_UNI_BLOCKS_PER_SM : NB_BLOCKS_PER_SM) k_neighbors(
+  Particles P, Tree T, Lists Ls, DevStatus * st, int dim,
+  const unsigned long long * rbits, Packed K) {
+  constexpr bool ORDERED = MODE == NB_MODE_ORDERED;
+  constexpr bool UNI = MODE == NB_MODE_UNI;
+  if(!ORDERED && UNI != (rbits[6] == rbits[7]))
+    return;  // the other variant's run
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cap = ORDERED ? NB_CAND_ORDERED : NB_CAND;
+  constexpr int CAND = ORDERED ? NB_CAND_ORDERED : UNI ? NB_UNI_CAND : NB_CAND;
+  const int cap = CAND;
   unsigned long long * ckey = nullptr;
   float * cxs = nullptr;  // candidates as SoA: minus their position relative
   float * cys = nullptr;  // to the group box corner, h and particle index,
@@ -915,13 +976,14 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
     stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND_ORDERED * 8) + w * NB_STACK;
   }
   else {
-    float * base = (float *)smem + (size_t)w * 5 * NB_CAND;
+    constexpr int NA = UNI ? 4 : 5;  // arrays per candidate (no h with UNI)
+    float * base = (float *)smem + (size_t)w * NA * CAND;
     cxs = base;
-    cys = base + NB_CAND;
-    czs = base + 2 * NB_CAND;
-    chs = base + 3 * NB_CAND;
-    cidx = (int *)(base + 4 * NB_CAND);
-    stack = (int *)(smem + (size_t)NB_WARPS * NB_CAND * 20) + w * NB_STACK;
+    cys = base + CAND;
+    czs = base + 2 * CAND;
+    chs = UNI ? nullptr : base + 3 * CAND;
+    cidx = (int *)(base + (NA - 1) * CAND);
+    stack = (int *)(smem + (size_t)NB_WARPS * CAND * NA * 4) + w * NB_STACK;
   }
   const unsigned lt = lanemask_lt();
   const double * X = P.f[F_X];
@@ -930,7 +992,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
   const double * H = P.f[F_H];
   const int ngroups = *T.ngroups;
   const int maxnb = Ls.maxnb;
-  const bool nonuni = rbits[6] != rbits[7];
+  const bool nonuni = !UNI && rbits[6] != rbits[7];
   const float qs0 = K.qscale[0], qs1 = K.qscale[1], qs2 = dim == 3 ? K.qscale[2] : 0.f;
   const float qmax = fmaxf(qs0, fmaxf(qs1, qs2));
   const float hglob = (float)ord_dec(rbits[7]);
@@ -1037,7 +1099,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
           cxs[pos] = -((float)(ql.x - glo.x) * qs0);
           cys[pos] = -((float)(ql.y - glo.y) * qs1);
           czs[pos] = -((float)(ql.z - glo.z) * qs2);
-          chs[pos] = __int_as_float(ql.w);
+          if(!UNI)
+            chs[pos] = __int_as_float(ql.w);
           cidx[pos] = j;
         }
       }
@@ -1055,7 +1118,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
             cxs[ncand] = 1e30f;
             cys[ncand] = 1e30f;
             czs[ncand] = 1e30f;
-            chs[ncand] = 0.f;
+            if(!UNI)
+              chs[ncand] = 0.f;
             cidx[ncand] = -1;
           }
           __syncwarp();
@@ -1142,7 +1206,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
                 append(b);
             }
           }
-          else if(!nonuni) {
+          else if(UNI) {
             // every h is equal: r and the margin are constants of the group
             // and the predicate decides (ties included, see tie)
             const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay);
@@ -1179,7 +1243,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
               }
             }
           }
-          else {
+          else if(!UNI) {
             // two candidates per iteration with Blackwell's packed FP32x2
             // arithmetic
             const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay);
@@ -1272,30 +1336,40 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
   const unsigned long long * rbits, const Packed & K, int ordered) {
   const size_t smem_o = (size_t)NB_WARPS * NB_CAND_ORDERED * 8 +
                         (size_t)NB_WARPS * NB_STACK * 4;
-  const size_t smem_u = (size_t)NB_WARPS * NB_CAND * 20 +
+  const size_t smem_v = (size_t)NB_WARPS * NB_CAND * 20 +
+                        (size_t)NB_WARPS * NB_STACK * 4;
+  const size_t smem_u = (size_t)NB_WARPS * NB_UNI_CAND * 16 +
                         (size_t)NB_WARPS * NB_STACK * 4;
   static std::atomic<unsigned long long> attr_devices{0};
   cudaError_t ae = once_per_device(&attr_devices, [&]() {
-    cudaError_t e = cudaFuncSetAttribute(k_neighbors<true>,
+    cudaError_t e = cudaFuncSetAttribute(k_neighbors<NB_MODE_ORDERED>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_o);
     if(e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_neighbors<false>,
+      e = cudaFuncSetAttribute(k_neighbors<NB_MODE_VAR>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v);
+    if(e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_neighbors<NB_MODE_UNI>,
         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u);
     return e;
   });
   if(ae != cudaSuccess)
     return ae;
-  int blocks = nsm * (ordered ? NB_ORDERED_BLOCKS_PER_SM : NB_BLOCKS_PER_SM);
-  int maxb = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
-  if(blocks > maxb)
-    blocks = maxb > 0 ? maxb : 1;
-  if(ordered)
-    k_neighbors<true><<<blocks, NB_WARPS * 32, smem_o, L.stream>>>(P, T, Ls,
-      st, pp.dim, rbits, K);
-  else
-    k_neighbors<false><<<blocks, NB_WARPS * 32, smem_u, L.stream>>>(P, T, Ls,
-      st, pp.dim, rbits, K);
-  *L.counter += 1;
+  const int maxb0 = (P.n + NB_WARPS * 32 - 1) / (NB_WARPS * 32) * 8;
+  const int maxb = maxb0 > 0 ? maxb0 : 1;
+  auto grid = [&](int per_sm) { return nsm * per_sm < maxb ? nsm * per_sm : maxb; };
+  if(ordered) {
+    k_neighbors<NB_MODE_ORDERED><<<grid(NB_ORDERED_BLOCKS_PER_SM), NB_WARPS * 32,
+      smem_o, L.stream>>>(P, T, Ls, st, pp.dim, rbits, K);
+    *L.counter += 1;
+  }
+  else {
+    // both variants; the one the range words do not select returns at once
+    k_neighbors<NB_MODE_UNI><<<grid(NB_UNI_BLOCKS_PER_SM), NB_WARPS * 32, smem_u,
+      L.stream>>>(P, T, Ls, st, pp.dim, rbits, K);
+    k_neighbors<NB_MODE_VAR><<<grid(NB_BLOCKS_PER_SM), NB_WARPS * 32, smem_v,
+      L.stream>>>(P, T, Ls, st, pp.dim, rbits, K);
+    *L.counter += 2;
+  }
   return cudaGetLastError();
 }
 
@@ -1314,7 +1388,8 @@ cudaError_t launch_neighbors(const Launch & L, const Particles & P,
 #define NOALLOC_RANGE_BYTES 256
 #define NOALLOC_KEYS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 8)
 #define NOALLOC_VALS_BYTES ((size_t)FSPH_NOALLOC_SORT_MAX * 4)
-#define NOALLOC_HIST_BYTES ((size_t)(256 * (FSPH_NOALLOC_SORT_MAX / RS_TILE) + 256) * 4)
+#define NOALLOC_HIST_BYTES \
+  ((size_t)(256 * ((FSPH_NOALLOC_SORT_MAX + RS_TILE - 1) / RS_TILE) + 256) * 4)
 #define NOALLOC_TOTAL \
   (NOALLOC_RANGE_BYTES + NOALLOC_KEYS_BYTES + NOALLOC_VALS_BYTES + NOALLOC_HIST_BYTES)
 

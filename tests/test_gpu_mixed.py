@@ -10,7 +10,10 @@ pressure terms of interior particles cancel to ~1e-13 of one term in FP64
 and plain FP32 pair sums missed the bar by 100x; density within 1e-10
 relative (float-float density sum); de/dt (FP32 pair terms) within 1e-5
 normwise.  A smooth velocity field is added so that the viscosity and de/dt
-terms are exercised."""
+terms are exercised; one case adds a uniform velocity 100x larger than the
+field's differences between neighbours (velocity differences need the
+velocities' low words: FP32 records alone miss the bar), and one starts
+from a KH state evolved in FP64, where the shear layers have developed."""
 import numpy as np
 import pytest
 
@@ -54,11 +57,12 @@ def accel_err(a, b):
     return np.linalg.norm(A - B, axis=1) / np.maximum(mag, 1e-3 * rms)
 
 
-@pytest.mark.parametrize("problem", ["sod", "sedov", "polytrope", "polytrope262k", "kh"])
+@pytest.mark.parametrize("problem", ["sod", "sedov", "sedov_boost", "polytrope",
+                                     "polytrope262k", "kh"])
 def test_mixed_matches_fp64(problem):
     if problem == "sod":
         s, p, m = setups.sod3d(40, 10, 10)
-    elif problem == "sedov":
+    elif problem.startswith("sedov"):
         s, p, m = setups.sedov3d(32)
     elif problem == "kh":
         s, p, m = setups.kh3d(24)   # periodic copies on every axis
@@ -76,6 +80,9 @@ def test_mixed_matches_fp64(problem):
         s["vx"][:] = 0.05 * np.sin(two_pi * s["y"])
         s["vy"][:] = 0.05 * np.sin(two_pi * s["z"])
         s["vz"][:] = 0.05 * np.sin(two_pi * s["x"])
+    if problem == "sedov_boost":
+        for f, v0 in (("vx", 30.0), ("vy", -20.0), ("vz", 10.0)):
+            s[f] += v0
     r64, l64 = _run_passes(s, p, PRECISION_FP64)
     rmx, lmx = _run_passes(s, p, PRECISION_MIXED)
     assert np.array_equal(r64["id"], rmx["id"])
@@ -116,3 +123,35 @@ def test_mixed_steps_stay_close():
     assert abs(ta[0] - tb[0]) <= 1e-4 * ta[0]
     for f in ("x", "y", "z", "rho", "P", "e", "u", "vsig"):
         assert np.abs(a[f] - b[f]).max() <= 1e-6 * max(np.abs(a[f]).max(), 1e-30), f
+
+
+def test_mixed_on_evolved_kh():
+    """KH 3D (32^3, periodic) after 60 FP64 driver iterations: one pass of
+    each precision from that state; the acceleration within the bar for
+    every particle, de/dt reported and bounded."""
+    from flecsph_gb300 import build
+    from flecsph_gb300.sph import BodySystem, capacity_for
+    build.build()
+    s, p, m = setups.kh3d(32)
+    n = m["n"]
+    p.precision_mode = PRECISION_FP64
+    bs = BodySystem(p, capacity_for(p, n, s))
+    bs.read_bodies(s)
+    for _ in range(61):
+        bs.step()
+    full = bs.download()
+    bs.close()
+    real = full["id"] < n
+    st = {f: np.ascontiguousarray(full[f][real]) for f in s}
+    r64, _ = _run_passes(st, p, PRECISION_FP64)
+    rmx, _ = _run_passes(st, p, PRECISION_MIXED)
+    o64, omx = np.argsort(r64["id"]), np.argsort(rmx["id"])
+    r64 = {k: v[o64] for k, v in r64.items()}
+    rmx = {k: v[omx] for k, v in rmx.items()}
+    e = accel_err(rmx, r64)
+    r = r64["dedt"]
+    de = np.abs(rmx["dedt"] - r) / np.maximum(np.abs(r), 1e-3 * np.sqrt((r ** 2).mean()))
+    print("evolved KH accel max", e.max(), "median", np.median(e), "dedt max", de.max(),
+          "median", np.median(de))
+    assert e.max() <= ACCEL_TOL, (e.max(), np.median(e))
+    assert de.max() <= 1e-4, (de.max(), np.median(de))

@@ -82,8 +82,9 @@ def test_driver_steps_fp64(name):
 
 
 def test_sod3d_full_size_vs_oracle(oracle_port):
-    """Config 1 at its full size (80x20x20 = 32,000): three driver
-    iterations on the GPU against the C oracle."""
+    """The Sod tube at its full size (80x20x20 = 32,000 particles, FP64):
+    the initial driver iteration and ten leapfrog steps on the GPU against
+    the C oracle, every field after each."""
     from flecsph_gb300 import setups
     s, p, meta = setups.sod3d()
     s = setups.shuffled(s, 11)
@@ -91,7 +92,7 @@ def test_sod3d_full_size_vs_oracle(oracle_port):
     bs.read_bodies(s)
     o = oracle_port.Oracle("port", p, threads=8)
     o.upload(s)
-    for k in range(3):
+    for k in range(11):
         bs.step()
         o.step()
         g, r = bs.download(), o.download()
