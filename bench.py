@@ -152,6 +152,8 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true",
+                    help="skip the polytrope's direct-summation gravity check")
     return ap.parse_args()
 
 
@@ -472,6 +474,27 @@ def ensemble_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def one_pass(bs, state, p):
+    """One pass of every physics callback from `state`: density, pressure,
+    sound speed, acceleration, the energy rate and gravity."""
+    bs.read_bodies(state)
+    bs.update_iteration()
+    bs.eos_init()
+    if p.thermokinetic_formulation:
+        bs.set_total_energy()
+    bs.density_pressure_soundspeed()
+    bs.save_velocityhalf()
+    bs.acceleration()
+    if p.thermokinetic_formulation:
+        bs.dedt()
+    else:
+        bs.dudt()
+    if p.enable_fmm:
+        bs.gravitation()
+    return bs.download(fields=["ax", "ay", "az", "gax", "gay", "gaz", "rho", "P", "cs",
+                               "dedt", "dudt", "id"])
+
+
 def gpu_arm(args):
     rank, world, local = dist_info()
     dist = init_dist(world)
@@ -547,24 +570,18 @@ def gpu_arm(args):
             full = bs.download()
             real = full["id"] < n
             cmp_state = {f: np.ascontiguousarray(full[f][real]) for f in s}
-        bs.read_bodies(cmp_state)
-        bs.update_iteration()
-        bs.eos_init()
-        if p.thermokinetic_formulation:
-            bs.set_total_energy()
-        bs.density_pressure_soundspeed()
-        bs.save_velocityhalf()
-        bs.acceleration()
-        if p.thermokinetic_formulation:
-            bs.dedt()
-        else:
-            bs.dudt()
-        if p.enable_fmm:
-            bs.gravitation()
-        results[mode]["same_state"] = bs.download(
-            fields=["ax", "ay", "az", "gax", "gay", "gaz", "rho", "P", "cs", "dedt",
-                    "dudt", "id"])
-        if args.workload == "polytrope" and rank == 0 and mode == modes[-1]:
+        results[mode]["same_state"] = one_pass(bs, cmp_state, p)
+        if len(modes) == 2 and p.sph_viscosity == 0:
+            # the same pass without artificial viscosity: how much of the
+            # acceleration error is the FP32 viscosity's
+            visc = (p.sph_viscosity_alpha, p.sph_viscosity_beta)
+            p.sph_viscosity_alpha = p.sph_viscosity_beta = 0.0
+            b2 = sph.BodySystem(p, cap, device=local)
+            results[mode]["no_visc"] = one_pass(b2, cmp_state, p)
+            b2.close()
+            p.sph_viscosity_alpha, p.sph_viscosity_beta = visc
+        if (args.workload == "polytrope" and rank == 0 and mode == modes[-1]
+                and not args.no_check):
             results[mode]["gravity_check"] = gravity_check(bs, p)
         # end to end through the C ABI with pinned host buffers
         if not args.no_e2e:
@@ -672,6 +689,9 @@ def gpu_arm(args):
                                                 "|d|/|ref| for rho, P, c_s and "
                                                 "|d|/max(|ref|, 1e-3 rms|ref|) for a, "
                                                 "de/dt (du/dt), g_acc"}
+        if "no_visc" in results["mixed"]:
+            pv = per_field_errors(results["fp64"]["no_visc"], results["mixed"]["no_visc"], p)
+            line["mixed_vs_fp64"]["accel_without_viscosity"] = pv["a"]
         if p.enable_fmm:
             line["mixed_vs_fp64"]["gravity_rel_err_max"] = pf["g_acc"]["max"]
             line["mixed_vs_fp64"]["gravity_rel_err_median"] = pf["g_acc"]["median"]

@@ -801,6 +801,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
 // UNI (every h equal) 1/h^(D+2) multiplies the finished sums instead of
 // every pair.  The pressure sum alone is the pressure-only acceleration the
 // de/dt pass takes.
+// pairs of a four-slot list chunk the acceleration pass unrolls
+#ifndef FSPH_ACCEL_FF_UNROLL
+#define FSPH_ACCEL_FF_UNROLL 2
+#endif
+constexpr int accel_ff_unroll = FSPH_ACCEL_FF_UNROLL;
+
 struct AccelFFState {
   ffloat sx, sy, sz;     // the pressure sum
   float vx, vy, vz;      // the viscous sum
@@ -818,7 +824,7 @@ __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
   float vsig = 0.f;
   for(int j0 = 0; j0 < cnt; j0 += 4) {
     const int4 q4 = *(const int4 *)(lp + (j0 << 5));
-#pragma unroll 2
+#pragma unroll(accel_ff_unroll)
     for(int u = 0; u < 4; ++u) {
       const int b = u == 0 ? q4.x : u == 1 ? q4.y : u == 2 ? q4.z : q4.w;
       const float4 pb = Kp.fph[b], lb = Kp.fpl[b];

@@ -196,7 +196,7 @@ cudaError_t launch_range_keys(const Launch & L, const Particles & P,
 // scatter in which each tile ranks its keys with warp match/ballot.
 #define RS_THREADS 256
 #ifndef RS_ITEMS
-#define RS_ITEMS 16
+#define RS_ITEMS 18
 #endif
 #define RS_TILE (RS_THREADS * RS_ITEMS)
 // resident scatter blocks per SM (each holds its tile, 12 B a key, in
@@ -531,10 +531,12 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
   if(i >= P.n)
     return;
   const bool nonuni = refboxes || rbits[6] != rbits[7];
-  double rc[3] = {0.0, 0.0, 0.0};
-  if(T.gmom)
-    for(int d = 0; d < dim; ++d)
-      rc[d] = 0.5 * (ord_dec(rbits[d]) + ord_dec(rbits[3 + d]));
+  double rc[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0};
+  for(int d = 0; d < dim; ++d) {
+    r0[d] = ord_dec(rbits[d]);
+    if(T.gmom)
+      rc[d] = 0.5 * (r0[d] + ord_dec(rbits[3 + d]));
+  }
   int p = T.leaf_parent[i];
   // Leaves write nothing here.  The arrival count at the parent is an
   // acquire-release atomic at device scope: it publishes this thread's
@@ -635,9 +637,8 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       T.box2[p] = n2;
       float fl[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
       for(int d = 0; d < dim; ++d) {
-        const double r0 = ord_dec(rbits[d]);
-        fl[d] = __double2float_rd(n2.lo[d] - r0);
-        fh[d] = __double2float_ru(n2.hi[d] - r0);
+        fl[d] = __double2float_rd(n2.lo[d] - r0[d]);
+        fh[d] = __double2float_ru(n2.hi[d] - r0[d]);
       }
       T.fbox2[2 * p] = make_float4(fl[0], fl[1], fl[2], 0.f);
       T.fbox2[2 * p + 1] = make_float4(fh[0], fh[1], fh[2], 0.f);
