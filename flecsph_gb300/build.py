@@ -42,7 +42,8 @@ def nvcc():
 
 def _tuning_defines():
     """-D flags from $FSPH_NVCC_DEFINES ("NAME=VALUE NAME2=VALUE2"): launch-shape
-    knobs of the kernels (FSPH_ACCEL_FF_BLOCKS), for tuning runs; empty for
+    knobs of the kernels (FSPH_ACCEL_FF_BLOCKS, NB_UNI_BLOCKS_PER_SM, RS_ITEMS,
+    ...), for tuning runs; empty for
     the default build."""
     return ["-D" + d for d in os.environ.get("FSPH_NVCC_DEFINES", "").split() if d]
 

@@ -147,3 +147,102 @@ __device__ __forceinline__ ffloat ff_from_double(double x) {
 }
 
 }  // namespace fsph
+
+// ---- two float-float values at once (one per float2 lane) ------------------
+// The same operations on float2 words with Blackwell's packed FP32x2
+// instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn): two neighbours' pair
+// terms per instruction, which halves the issue slots of the float-float
+// passes' arithmetic (the FMA pipe's work stays the same).  a - b is
+// __ffma2_rn(b, -1, a): one rounding, as a subtraction.
+namespace fsph {
+
+struct ffloat2 {
+  float2 h, l;
+};
+
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2s(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, f2s(-1.f), a);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return f2(-a.x, -a.y); }
+
+__device__ __forceinline__ ffloat2 ff2_make(float2 h, float2 l) {
+  ffloat2 r;
+  r.h = h;
+  r.l = l;
+  return r;
+}
+__device__ __forceinline__ ffloat2 ff2_bcast(ffloat a) {
+  return ff2_make(f2s(a.h), f2s(a.l));
+}
+__device__ __forceinline__ ffloat ff2_lane(const ffloat2 & a, int k) {
+  return k == 0 ? ff_make(a.h.x, a.l.x) : ff_make(a.h.y, a.l.y);
+}
+
+__device__ __forceinline__ ffloat2 ff2_add(ffloat2 a, ffloat2 b) {
+  const float2 s = add2(a.h, b.h);
+  const float2 bb = sub2(s, a.h);
+  const float2 e = add2(sub2(a.h, sub2(s, bb)), sub2(b.h, bb));
+  return ff2_make(s, add2(e, add2(a.l, b.l)));
+}
+__device__ __forceinline__ ffloat2 ff2_cadd(float c, ffloat2 b) {
+  const float2 s = add2(f2s(c), b.h);
+  const float2 e = sub2(b.h, sub2(s, f2s(c)));
+  return ff2_make(s, add2(e, b.l));
+}
+__device__ __forceinline__ ffloat2 ff2_norm(ffloat2 a) {
+  const float2 s = add2(a.h, a.l);
+  return ff2_make(s, sub2(a.l, sub2(s, a.h)));
+}
+__device__ __forceinline__ ffloat2 ff2_mul(ffloat2 a, ffloat2 b) {
+  const float2 p = mul2(a.h, b.h);
+  float2 e = fma2(a.h, b.h, neg2(p));
+  e = fma2(a.h, b.l, e);
+  e = fma2(a.l, b.h, e);
+  return ff2_make(p, e);
+}
+__device__ __forceinline__ ffloat2 ff2_scale2(ffloat2 a, float c) {
+  return ff2_make(mul2(a.h, f2s(c)), mul2(a.l, f2s(c)));
+}
+__device__ __forceinline__ ffloat2 ff2_sqr(ffloat2 a) {
+  const float2 p = mul2(a.h, a.h);
+  float2 e = fma2(a.h, a.h, neg2(p));
+  e = fma2(add2(a.h, a.h), a.l, e);
+  return ff2_make(p, e);
+}
+__device__ __forceinline__ ffloat2 ff2_sqr_wide(ffloat2 a) {
+  const float2 p = mul2(a.h, a.h);
+  float2 e = fma2(a.h, a.h, neg2(p));
+  e = fma2(add2(a.h, a.h), a.l, e);
+  e = fma2(a.l, a.l, e);
+  return ff2_make(p, e);
+}
+// sqrt of a normalised a >= 0 (the rsqrt per lane)
+__device__ __forceinline__ ffloat2 ff2_sqrt(ffloat2 a) {
+  const float2 rs = f2(a.h.x > 0.f ? rsqrtf(a.h.x) : 0.f, a.h.y > 0.f ? rsqrtf(a.h.y) : 0.f);
+  const float2 r = mul2(a.h, rs);
+  const float2 d = add2(fma2(neg2(r), r, a.h), a.l);
+  return ff2_make(r, mul2(d, mul2(f2s(0.5f), rs)));
+}
+// c / a for a float constant c (the reciprocal per lane)
+__device__ __forceinline__ ffloat2 ff2_rcp_scaled(ffloat2 a, float c) {
+  const float2 r = f2(1.0f / a.h.x, 1.0f / a.h.y);
+  float2 e = fma2(neg2(a.h), r, f2s(1.0f));
+  e = fma2(neg2(a.l), r, e);
+  return ff2_make(mul2(f2s(c), r), mul2(f2s(c), mul2(e, r)));
+}
+__device__ __forceinline__ void ff2_acc(ffloat2 & s, ffloat2 t) {
+  const float2 n = add2(s.h, t.h);
+  const float2 bb = sub2(n, s.h);
+  const float2 e = add2(sub2(s.h, sub2(n, bb)), sub2(t.h, bb));
+  s.h = n;
+  s.l = add2(s.l, add2(e, t.l));
+}
+
+}  // namespace fsph

@@ -606,6 +606,24 @@ __device__ __forceinline__ ffloat ff_wpoly(ffloat t) {
   return ff_mul(ff_sqr(t4), p);
 }
 
+// ff_wpoly on two values at once (packed FP32x2)
+template<int K>
+__device__ __forceinline__ ffloat2 ff2_wpoly(ffloat2 t) {
+  const ffloat2 t2 = ff2_sqr(t);
+  const ffloat2 t4 = ff2_sqr(t2);
+  if(K == FSPH_KERNEL_WENDLAND_C2)
+    return ff2_mul(t4, ff2_cadd(5.f, ff2_scale2(t, -4.f)));
+  if(K == FSPH_KERNEL_WENDLAND_C4) {
+    const ffloat2 c35 = ff2_make(f2s(35.f), f2s(0.f));
+    const ffloat2 p = ff2_cadd(56.f, ff2_mul(ff2_cadd(-88.f, ff2_mul(t, c35)), t));
+    return ff2_mul(ff2_mul(t4, t2), p);
+  }
+  const ffloat2 a1 = ff2_cadd(121.f, ff2_scale2(t, -32.f));
+  const ffloat2 a2 = ff2_cadd(-154.f, ff2_mul(a1, t));
+  const ffloat2 p = ff2_cadd(66.f, ff2_mul(a2, t));
+  return ff2_mul(ff2_sqr(t4), p);
+}
+
 template<int K>
 __device__ __forceinline__ ffloat ff_gpoly(ffloat t) {
   const ffloat t2 = ff_sqr(t);
@@ -719,6 +737,64 @@ __device__ __forceinline__ ffloat density_ff_sum(const Packed & Kp, const int * 
   return sum;
 }
 
+// 1: the density pass takes two neighbours per step in packed FP32x2
+#ifndef FSPH_DENSITY_PAIRED
+#define FSPH_DENSITY_PAIRED 1
+#endif
+
+// density_ff_sum with two neighbours per step in packed FP32x2 (the list's
+// four-slot chunks hold two pairs of neighbours).  The two lanes keep their
+// own running sums, added at the end.
+template<int D, int K, bool UNI>
+__device__ __forceinline__ ffloat density_ff_sum2(const Packed & Kp, const int * lp,
+  int cnt, const float4 & pa, const float4 & la, const ffloat & iha,
+  const ffloat & ihDa) {
+  ffloat2 sum = ff2_make(f2s(0.f), f2s(0.f));
+  const ffloat2 ih1 = ff2_bcast(iha);
+  const float2 xa = f2s(pa.x), ya = f2s(pa.y), za = f2s(pa.z);
+  const float2 xal = f2s(la.x), yal = f2s(la.y), zal = f2s(la.z);
+  for(int j0 = 0; j0 < cnt; j0 += 4) {
+    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
+#pragma unroll
+    for(int u = 0; u < 4; u += 2) {
+      const int b0 = u == 0 ? q4.x : q4.z, b1 = u == 0 ? q4.y : q4.w;
+      const float4 p0 = Kp.fph[b0], p1 = Kp.fph[b1];
+      const float4 l0 = Kp.fpl[b0], l1 = Kp.fpl[b1];
+      const float2 m0 = ((const float2 *)Kp.fmA)[2 * b0];
+      const float2 m1 = ((const float2 *)Kp.fmA)[2 * b1];
+      // separations: exact high-word differences, low-word differences
+      const ffloat2 dx = ff2_make(sub2(xa, f2(p0.x, p1.x)), sub2(xal, f2(l0.x, l1.x)));
+      const ffloat2 dy = ff2_make(sub2(ya, f2(p0.y, p1.y)), sub2(yal, f2(l0.y, l1.y)));
+      ffloat2 r2 = ff2_add(ff2_sqr_wide(dx), ff2_sqr_wide(dy));
+      if(D == 3) {
+        const ffloat2 dz = ff2_make(sub2(za, f2(p0.z, p1.z)), sub2(zal, f2(l0.z, l1.z)));
+        r2 = ff2_add(r2, ff2_sqr_wide(dz));
+      }
+      const ffloat2 r = ff2_sqrt(ff2_norm(r2));
+      ffloat2 ih = ih1;
+      if(!UNI)
+        ih = ff2_rcp_scaled(ff2_add(ff2_make(f2s(pa.w), f2s(la.w)),
+                                    ff2_make(f2(p0.w, p1.w), f2(l0.w, l1.w))), 2.f);
+      const ffloat2 q = ff2_mul(r, ih);
+      const ffloat2 t = ff2_cadd(1.f, ff2_make(neg2(q.h), neg2(q.l)));
+      ffloat2 w = ff2_mul(ff2_wpoly<K>(t), ff2_make(f2(m0.x, m1.x), f2(m0.y, m1.y)));
+      if(!UNI) {
+        // 1 / h_ab^D per lane
+        const ffloat2 i2 = ff2_sqr(ih);
+        w = ff2_mul(w, D == 3 ? ff2_mul(i2, ih) : i2);
+      }
+      const bool k0 = q.h.x < 1.f && j0 + u < cnt, k1 = q.h.y < 1.f && j0 + u + 1 < cnt;
+      w.h = f2(k0 ? w.h.x : 0.f, k1 ? w.h.y : 0.f);
+      w.l = f2(k0 ? w.l.x : 0.f, k1 ? w.l.y : 0.f);
+      ff2_acc(sum, w);
+    }
+  }
+  ffloat s1 = ff_add(ff2_lane(sum, 0), ff2_lane(sum, 1));
+  if(UNI)
+    s1 = ff_mul(s1, ihDa);
+  return s1;
+}
+
 template<int D, int K, bool CULL>
 __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   PhysParams pp, Lists Ls, Packed Kp, double * cs_new, DevStatus * st,
@@ -731,9 +807,15 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   const ffloat ihDa = ff_ipow<D>(iha);
   const int cnt = Ls.cnt[a];
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
+#if FSPH_DENSITY_PAIRED
+  const ffloat sum = Kp.fscale[2] != 0.0
+                       ? density_ff_sum2<D, K, true>(Kp, lp, cnt, pa, la, iha, ihDa)
+                       : density_ff_sum2<D, K, false>(Kp, lp, cnt, pa, la, iha, ihDa);
+#else
   const ffloat sum = Kp.fscale[2] != 0.0
                        ? density_ff_sum<D, K, true>(Kp, lp, cnt, pa, la, iha, ihDa)
                        : density_ff_sum<D, K, false>(Kp, lp, cnt, pa, la, iha, ihDa);
+#endif
   double gsum[3] = {0.0, 0.0, 0.0};
   if(CULL) {
     // m_b grad_a W_ab for compute_divv, in FP64 (see k_density_mixed)
