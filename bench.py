@@ -58,10 +58,10 @@ HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
 # lists and records well above L2): the walk, the mean of two launches
 # (488.3 MB, profiles/k_neighbors_traffic_sedov3d_96.md); the float-float
 # density and acceleration passes and the de/dt pass of the warm-up
-# iteration (521.1, 569.4 and 593.5 MB,
+# iteration (567.6, 569.2 and 597.8 MB,
 # profiles/k_density_ff_accel_ff_dedt_ahyd_sedov3d_96.md)
-MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9, "density": 589.0, "accel": 643.6,
-                                 "energy": 670.8}
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9, "density": 641.6, "accel": 643.3,
+                                 "energy": 675.7}
 
 
 def read_work_header(path=os.path.join(ROOT, "include", "fsph_work.h")):

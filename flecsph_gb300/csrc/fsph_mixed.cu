@@ -92,29 +92,22 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
     h = (float)v;
     l = (float)(v - (double)h);
   };
-  // the .w slots of fv1 and fv2 (rho, c_s) are written apart from their
-  // velocity words: by the density pass, or here from the FP64 state
-  float * w1 = (float *)&K.fv1[i];
-  float * w2 = (float *)&K.fv2[i];
   if(what & PACK_VHM) {
+    // fv1, fv2: v_half's words with rho and c_s as they stand (after the
+    // density pass the state holds the new c_s; before it, the values are
+    // rewritten by the next packing before any pass reads them)
     const float m = (float)P.f[F_M][i];
     float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
     for(int d = 0; d < dim; ++d)
       hl(F_VHX + d, h[d], l[d]);
     K.vhm[i] = make_float4(h[0], h[1], h[2], m);
-    for(int d = 0; d < 3; ++d) {
-      w1[d] = h[d];
-      w2[d] = l[d];
-    }
+    K.fv1[i] = make_float4(h[0], h[1], h[2], (float)P.f[F_RHO][i]);
+    K.fv2[i] = make_float4(l[0], l[1], l[2], (float)P.f[F_CS][i]);
     K.mass[i] = m;
   }
   if(what & PACK_VEL)
     K.vel[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)P.f[F_CS][i]);
-  if(what & (PACK_THERMO | PACK_DEDT)) {
-    w1[3] = (float)P.f[F_RHO][i];
-    w2[3] = (float)P.f[F_CS][i];
-  }
   if(what & PACK_THERMO) {
     const double rho = P.f[F_RHO][i], cs = P.f[F_CS][i];
     const double A = P.f[F_P][i] / (rho * rho);
@@ -261,8 +254,11 @@ cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
   const DevTime * t, DevStatus * st, int use_ahyd) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
+  // through a^P, v_half, rho and c_s are those the acceleration pass packed
+  // (the caller's flag says so): only v - v_half is new
+  const int vhm = use_ahyd && wendland_kernel(pp.kernel) ? 0 : PACK_VHM;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
+    vhm | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
     run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st, use_ahyd);

@@ -49,7 +49,9 @@ def rel_err(a, b):
 
 @pytest.fixture(scope="module")
 def poly(oracle_port):
-    s, p, m = setups.polytrope3d(32768, seed=5)
+    # the 64k polytrope on which the tree walk and direct summation both
+    # cover every particle (the 4M run checks a 64k sample of sinks)
+    s, p, m = setups.polytrope3d(65536, seed=5)
     p.max_neighbors = 2048
     p.thermokinetic_formulation = 0   # e is not initialised for a bare call
     return s, p, _direct(oracle_port, s, p)
