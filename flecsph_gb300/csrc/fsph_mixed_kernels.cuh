@@ -38,14 +38,6 @@ __device__ __forceinline__ void kahan(float & sum, float & comp, float term) {
   sum = t;
 }
 
-// kahan on two running sums at once
-__device__ __forceinline__ void kahan2(float2 & sum, float2 & comp, float2 term) {
-  const float2 y = sub2(term, comp);
-  const float2 t = add2(sum, y);
-  comp = sub2(sub2(t, sum), y);
-  sum = t;
-}
-
 // ------------------------------------------------------- FP32 kernels --
 __device__ __forceinline__ float sig_cubic(int D) {
   return D == 2 ? 40.f / (7.f * FPI) : 8.f / FPI;
@@ -645,21 +637,6 @@ __device__ __forceinline__ ffloat ff_gpoly(ffloat t) {
   return ff_mul(ff_mul(ff_mul(t4, t2), t), p);
 }
 
-// ff_gpoly on two values at once (packed FP32x2)
-template<int K>
-__device__ __forceinline__ ffloat2 ff2_gpoly(ffloat2 t) {
-  const ffloat2 t2 = ff2_sqr(t);
-  if(K == FSPH_KERNEL_WENDLAND_C2)
-    return ff2_mul(t2, t);
-  const ffloat2 t4 = ff2_sqr(t2);
-  if(K == FSPH_KERNEL_WENDLAND_C4) {
-    const ffloat2 c5 = ff2_make(f2s(-5.f), f2s(0.f));
-    return ff2_mul(ff2_mul(t4, t), ff2_cadd(6.f, ff2_mul(t, c5)));
-  }
-  const ffloat2 b1 = ff2_cadd(-39.f, ff2_scale2(t, 16.f));
-  const ffloat2 p = ff2_cadd(24.f, ff2_mul(b1, t));
-  return ff2_mul(ff2_mul(ff2_mul(t4, t2), t), p);
-}
 
 // W = wconst / h^D * wpoly(t);  (dW/dr)/r = gconst / h^(D+2) * gpoly(t)
 template<int D, int K>
@@ -995,124 +972,6 @@ __device__ __forceinline__ void accel_ff_sum(const Packed & Kp, const int * lp,
   out.vsig = vsig;
 }
 
-// accel_ff_sum with two neighbours per step in packed FP32x2: float-float
-// geometry, kernel gradient and pressure products for both, the viscosity
-// and the signal speed per lane where they need a division, a maximum or
-// the Cullen alpha.  The two lanes' sums are added at the end.
-template<int D, int K, bool VSIG, bool CULL, bool UNI>
-__device__ __forceinline__ void accel_ff_sum2(const Packed & Kp, const int * lp,
-  int cnt, int a, const float4 & pa, const float4 & la, const ffloat & iha,
-  const ffloat & ihPa, const ffloat & Aa, const float4 & h1a, const float4 & h2a,
-  const float4 & va, float eps, float alpha, float beta, float alpha_a,
-  AccelFFState & out) {
-  ffloat2 sx = ff2_make(f2s(0.f), f2s(0.f)), sy = sx, sz = sx;
-  float2 vx = f2s(0.f), vy = vx, vz = vx, cvx = vx, cvy = vx, cvz = vx;
-  float vsig = 0.f;
-  const ffloat2 ih1 = ff2_bcast(iha), ihP1 = ff2_bcast(ihPa), Aa2 = ff2_bcast(Aa);
-  for(int j0 = 0; j0 < cnt; j0 += 4) {
-    const int4 q4 = *(const int4 *)(lp + (j0 << 5));
-#pragma unroll 1
-    for(int u = 0; u < 4; u += 2) {
-      const int b0 = u == 0 ? q4.x : q4.z, b1 = u == 0 ? q4.y : q4.w;
-      const float4 p0 = Kp.fph[b0], p1 = Kp.fph[b1];
-      const float4 l0 = Kp.fpl[b0], l1 = Kp.fpl[b1];
-      const ffloat2 dx = ff2_make(sub2(f2s(pa.x), f2(p0.x, p1.x)), sub2(f2s(la.x), f2(l0.x, l1.x)));
-      const ffloat2 dy = ff2_make(sub2(f2s(pa.y), f2(p0.y, p1.y)), sub2(f2s(la.y), f2(l0.y, l1.y)));
-      const ffloat2 dz = D == 3 ? ff2_make(sub2(f2s(pa.z), f2(p0.z, p1.z)),
-                                           sub2(f2s(la.z), f2(l0.z, l1.z)))
-                                : ff2_make(f2s(0.f), f2s(0.f));
-      ffloat2 r2 = ff2_add(ff2_sqr_wide(dx), ff2_sqr_wide(dy));
-      if(D == 3)
-        r2 = ff2_add(r2, ff2_sqr_wide(dz));
-      r2 = ff2_norm(r2);
-      const float2 r2f = r2.h;
-      const float2 dxr = add2(dx.h, dx.l), dyr = add2(dy.h, dy.l), dzr = add2(dz.h, dz.l);
-      const ffloat2 r = ff2_sqrt(r2);
-      ffloat2 ih = ih1, ihP = ihP1;
-      if(!UNI) {
-        ih = ff2_rcp_scaled(ff2_add(ff2_make(f2s(pa.w), f2s(la.w)),
-                                    ff2_make(f2(p0.w, p1.w), f2(l0.w, l1.w))), 2.f);
-        const ffloat2 i2 = ff2_sqr(ih), i4 = ff2_sqr(i2);
-        ihP = D == 3 ? ff2_mul(i4, ih) : i4;
-      }
-      const ffloat2 q = ff2_mul(r, ih);
-      const ffloat2 t = ff2_cadd(1.f, ff2_make(neg2(q.h), neg2(q.l)));
-      const float4 g0 = Kp.fv1[b0], g1 = Kp.fv1[b1];  // v_half, rho
-      const float4 k0 = Kp.fv2[b0], k1 = Kp.fv2[b1];  // low words, c_s
-      const float4 n0 = Kp.fmA[b0], n1 = Kp.fmA[b1];
-      // viscosity in FP32 (the position unit cancels in mu)
-      const float2 hab = mul2(f2s(0.5f), add2(f2s(pa.w), f2(p0.w, p1.w)));
-      const float2 dvx = add2(sub2(f2s(h1a.x), f2(g0.x, g1.x)), sub2(f2s(h2a.x), f2(k0.x, k1.x)));
-      const float2 dvy = add2(sub2(f2s(h1a.y), f2(g0.y, g1.y)), sub2(f2s(h2a.y), f2(k0.y, k1.y)));
-      const float2 dvz = add2(sub2(f2s(h1a.z), f2(g0.z, g1.z)), sub2(f2s(h2a.z), f2(k0.z, k1.z)));
-      const float2 dotp = fma2(dvz, dzr, fma2(dvy, dyr, mul2(dvx, dxr)));
-      const float2 den = fma2(mul2(f2s(eps), hab), hab, r2f);
-      const float2 num = mul2(hab, dotp);
-      const float2 mu = f2(dotp.x < 0.f ? __fdividef(num.x, den.x) : 0.f,
-                           dotp.y < 0.f ? __fdividef(num.y, den.y) : 0.f);
-      const float2 rho_ab = mul2(f2s(0.5f), add2(f2s(h1a.w), f2(g0.w, g1.w)));
-      const float2 c_ab = mul2(f2s(0.5f), add2(f2s(h2a.w), f2(k0.w, k1.w)));
-      const float2 Pi = f2(visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b0, rho_ab.x, c_ab.x, mu.x),
-                           visc_pi_f<CULL>(alpha, beta, alpha_a, Kp, b1, rho_ab.y, c_ab.y, mu.y));
-      const ffloat2 gp = ff2_gpoly<K>(t);
-      const ffloat2 m = ff2_make(f2(n0.x, n1.x), f2(n0.y, n1.y));
-      ffloat2 S = ff2_mul(ff2_mul(ff2_add(Aa2, ff2_make(f2(n0.z, n1.z), f2(n0.w, n1.w))), m), gp);
-      float2 V = mul2(mul2(m.h, Pi), gp.h);
-      if(!UNI) {
-        S = ff2_mul(S, ihP);
-        V = mul2(V, ihP.h);
-      }
-      const bool in0 = q.h.x < 1.f, in1 = q.h.y < 1.f;
-      S.h = f2(in0 ? S.h.x : 0.f, in1 ? S.h.y : 0.f);
-      S.l = f2(in0 ? S.l.x : 0.f, in1 ? S.l.y : 0.f);
-      V = f2(in0 ? V.x : 0.f, in1 ? V.y : 0.f);
-      if(VSIG) {
-        const float4 w0 = Kp.vel[b0], w1 = Kp.vel[b1];  // .w: c_s before the density pass
-        const float2 dwx = sub2(f2s(va.x), f2(w0.x, w1.x));
-        const float2 dwy = sub2(f2s(va.y), f2(w0.y, w1.y));
-        const float2 dwz = sub2(f2s(va.z), f2(w0.z, w1.z));
-        const float2 dv = fma2(dwz, dzr, fma2(dwy, dyr, mul2(dwx, dxr)));
-        const float d0 = dv.x * rsqrtf(r2f.x), d1 = dv.y * rsqrtf(r2f.y);
-        const float c0 = b0 > a ? k0.w : w0.w, c1 = b1 > a ? k1.w : w1.w;
-        const float e0 = fmaxf(h2a.w, c0) - fminf(d0, 0.f);
-        const float e1 = fmaxf(h2a.w, c1) - fminf(d1, 0.f);
-        vsig = fmaxf(vsig, (b0 != a && r2f.x > 0.f) ? e0 : 0.f);
-        vsig = fmaxf(vsig, (b1 != a && r2f.y > 0.f) ? e1 : 0.f);
-      }
-      // padding slots and the self pair have dx = 0 and add nothing
-      ff2_acc(sx, ff2_mul(S, dx));
-      ff2_acc(sy, ff2_mul(S, dy));
-      kahan2(vx, cvx, mul2(V, dxr));
-      kahan2(vy, cvy, mul2(V, dyr));
-      if(D == 3) {
-        ff2_acc(sz, ff2_mul(S, dz));
-        kahan2(vz, cvz, mul2(V, dzr));
-      }
-    }
-  }
-  ffloat ox = ff_add(ff2_lane(sx, 0), ff2_lane(sx, 1));
-  ffloat oy = ff_add(ff2_lane(sy, 0), ff2_lane(sy, 1));
-  ffloat oz = ff_add(ff2_lane(sz, 0), ff2_lane(sz, 1));
-  if(UNI) {
-    ox = ff_mul(ox, ihPa);
-    oy = ff_mul(oy, ihPa);
-    oz = ff_mul(oz, ihPa);
-  }
-  const float ihs = UNI ? ihPa.h : 1.f;
-  out.sx = ox;
-  out.sy = oy;
-  out.sz = oz;
-  out.vx = ((vx.x - cvx.x) + (vx.y - cvx.y)) * ihs;
-  out.vy = ((vy.x - cvy.x) + (vy.y - cvy.y)) * ihs;
-  out.vz = ((vz.x - cvz.x) + (vz.y - cvz.y)) * ihs;
-  out.vsig = vsig;
-}
-
-// 1: the acceleration pass takes two neighbours per step in packed FP32x2
-#ifndef FSPH_ACCEL_PAIRED
-#define FSPH_ACCEL_PAIRED 0
-#endif
-
 // Resident blocks of 256 per SM the acceleration pass is compiled for.  2
 // gives it up to 128 registers; 3 caps it at 80 for 24 warps to hide the
 // neighbour gathers, which measured slower on Sedov 128^3 (2.23 against
@@ -1145,21 +1004,12 @@ __global__ void __launch_bounds__(FSPH_ACCEL_FF_THREADS, FSPH_ACCEL_FF_BLOCKS) k
     va = Kp.vel[a];
   const int * lp = Ls.idx + list_slot(a, 0, Ls.maxnb);
   AccelFFState r;
-#if FSPH_ACCEL_PAIRED
-  if(Kp.fscale[2] != 0.0)
-    accel_ff_sum2<D, K, VSIG, CULL, true>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
-      h2a, va, eps, alpha, beta, alpha_a, r);
-  else
-    accel_ff_sum2<D, K, VSIG, CULL, false>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
-      h2a, va, eps, alpha, beta, alpha_a, r);
-#else
   if(Kp.fscale[2] != 0.0)
     accel_ff_sum<D, K, VSIG, CULL, true>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
       h2a, va, eps, alpha, beta, alpha_a, r);
   else
     accel_ff_sum<D, K, VSIG, CULL, false>(Kp, lp, cnt, a, pa, la, iha, ihPa, Aa, h1a,
       h2a, va, eps, alpha, beta, alpha_a, r);
-#endif
   const double iE = Kp.fscale[1];
   const double iE2 = iE * iE;
   // a = -gconst / E^(D+1) * sum
