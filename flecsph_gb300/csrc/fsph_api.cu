@@ -480,6 +480,7 @@ fsph_ctx * fsph_create(const fsph_params * p, int32_t device, int64_t capacity,
   ok &= dalloc(c, &c->T.edepth, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.group_first, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.group_last, N) == cudaSuccess;
+  ok &= dalloc(c, &c->T.group_start, N) == cudaSuccess;
   ok &= dalloc(c, &c->T.ngroups, 1) == cudaSuccess;
   ok &= dalloc(c, &c->K.qpos, N) == cudaSuccess;
   ok &= dalloc(c, &c->K.vhm, N) == cudaSuccess;
@@ -858,7 +859,7 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
     CK(launch_pack_positions(L, c->P, c->pp, c->d_range, c->K));
     CK(launch_build_tree(L, c->P, c->pp, c->T,
       c->p.group_size > 0 ? c->p.group_size : GROUP_MAX, c->d_range, c->K.qpos,
-      c->mixed ? 0 : 1));
+      c->K.qscale, c->mixed ? 0 : 1));
   }
   {
     // FP64 mode keeps each list in the reference's order so its sums round

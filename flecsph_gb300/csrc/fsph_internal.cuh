@@ -98,6 +98,7 @@ struct Tree {
   unsigned char * edepth;  // reference octree depth of each particle
   int * group_first;
   int * group_last;
+  int * group_start;       // per group: the node its mixed walk starts from
   int * ngroups;           // device scalar
   double * gmom;           // with gravity only (else null): per node the raw
                            // moments of mass about the range centre,
@@ -244,7 +245,7 @@ cudaError_t launch_permute(const Launch & L, const Particles & src,
 struct Packed;
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,
-  const unsigned long long * rbits, const int4 * qpos, int ordered);
+  const unsigned long long * rbits, const int4 * qpos, const float * qscale, int ordered);
 cudaError_t launch_neighbors(const Launch & L, const Particles & P,
   const PhysParams & pp, const Tree & T, Lists & Ls, DevStatus * st, int nsm,
   const unsigned long long * rbits, const Packed & K, int ordered);

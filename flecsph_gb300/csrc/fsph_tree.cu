@@ -647,8 +647,17 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
   }
 }
 
-// Groups: maximal subtrees with at most `gmax` particles.
-__global__ void k_groups(int n, Tree T, int gmax) {
+// Groups: maximal subtrees with at most `gmax` particles.  Each group also
+// gets the node its mixed walk starts from: the lowest ancestor whose
+// fixed-point box, less one step on every side, holds the group's box grown
+// by the largest reach (max h, with the walk's 1e-5 slack and two steps for
+// the quantisation).  A radix-tree node holds every particle whose key
+// shares its prefix, so its particles' box lies in that Morton cell; a
+// particle within reach lies in the grown box, hence a step inside the
+// node's box, hence in the cell and in the subtree: the walk below that
+// node finds every candidate the walk from the root finds.
+__global__ void k_groups(int n, Tree T, int gmax, int dim, const float * qscale,
+  const unsigned long long * rbits) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n)
     return;
@@ -664,6 +673,31 @@ __global__ void k_groups(int n, Tree T, int gmax) {
     int slot = atomicAdd(T.ngroups, 1);
     T.group_first[slot] = f;
     T.group_last[slot] = l;
+    // (a one-particle group walks from the root)
+    int v = 0;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if(g >= 0) {
+      const int4 glo = T.qbox[2 * g], ghi = T.qbox[2 * g + 1];
+      const int gl[3] = {glo.x, glo.y, glo.z}, gh[3] = {ghi.x, ghi.y, ghi.z};
+      const float R = (float)ord_dec(rbits[7]) * 1.00001f;
+      for(int d = 0; d < dim; ++d) {
+        const int r = (int)ceilf(R / qscale[d]) + 2;
+        lo[d] = gl[d] - r;
+        hi[d] = gh[d] + r;
+      }
+      v = T.parent[g];
+    }
+    while(v > 0) {
+      const int4 a = T.qbox[2 * v], b = T.qbox[2 * v + 1];
+      const int al[3] = {a.x, a.y, a.z}, bh[3] = {b.x, b.y, b.z};
+      bool in = true;
+      for(int d = 0; d < dim; ++d)
+        in = in && al[d] + 1 <= lo[d] && bh[d] - 1 >= hi[d];
+      if(in)
+        break;
+      v = T.parent[v];
+    }
+    T.group_start[slot] = v < 0 ? 0 : v;
   }
 }
 
@@ -709,7 +743,8 @@ __global__ void k_refgroups(const unsigned long long * K, int n, int dim,
 
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,
-  const unsigned long long * rbits, const int4 * qpos, int ordered) {
+  const unsigned long long * rbits, const int4 * qpos, const float * qscale,
+  int ordered) {
   const int n = P.n;
   cudaMemsetAsync(T.counter, 0, sizeof(unsigned) * (size_t)n, L.stream);
   cudaMemsetAsync(T.ngroups, 0, sizeof(int), L.stream);
@@ -717,7 +752,8 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   if(ordered)  // reference octree depths order the FP64 lists
     k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
   k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits, ordered);
-  k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max);
+  k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max, pp.dim, qscale,
+    rbits);
   k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits,
     ordered);
   *L.counter += 5;
@@ -1052,7 +1088,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
     bool chunked = false;
     bool refdone = false;  // varying h: this lane's list is already filtered
     if(lane == 0)
-      stack[0] = 0;
+      stack[0] = ORDERED ? 0 : T.qbox[2 * T.group_start[g] + 1].w;
     __syncwarp();
     while(sp > 0) {
       const int k = sp < 32 ? sp : 32;
@@ -1060,6 +1096,70 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
       int node = act ? stack[sp - 1 - lane] : 0;
       __syncwarp();
       sp -= k;
+      if(!ORDERED) {
+        // The stack holds the split codes of accepted nodes (split << 2 |
+        // left leaf << 1 | right leaf, as qbox's .w keeps them); a round
+        // tests both children of each -- nodes split and split + 1, whose
+        // boxes are adjacent in qbox, or a leaf's position -- pushes the
+        // accepted inner children's codes and stages the accepted leaves, so
+        // every level of the descent costs one round instead of two.
+        int4 cl[2], chh[2];
+        bool lf[2] = {false, false}, ca[2] = {false, false};
+        int split = 0;
+        if(act) {
+          const int code = node;
+          split = code >> 2;
+          lf[0] = (code & 2) != 0;
+          lf[1] = (code & 1) != 0;
+          for(int c = 0; c < 2; ++c) {
+            if(lf[c]) {
+              cl[c] = chh[c] = K.qpos[split + c];
+            }
+            else {
+              cl[c] = T.qbox[2 * (split + c)];
+              chh[c] = T.qbox[2 * (split + c) + 1];
+            }
+          }
+          for(int c = 0; c < 2; ++c)
+            ca[c] = box_near(glo, ghi, hg, cl[c], chh[c], __int_as_float(cl[c].w), qs0,
+              qs1, qs2);
+        }
+        const int cc[2] = {lf[0] ? ~split : chh[0].w, lf[1] ? ~(split + 1) : chh[1].w};
+        const unsigned bi0 = __ballot_sync(FULL, ca[0] && !lf[0]);
+        const unsigned bi1 = __ballot_sync(FULL, ca[1] && !lf[1]);
+        const unsigned bl0 = __ballot_sync(FULL, ca[0] && lf[0]);
+        const unsigned bl1 = __ballot_sync(FULL, ca[1] && lf[1]);
+        const int npush = __popc(bi0) + __popc(bi1);
+        if(sp + npush > NB_STACK) {
+          if(lane == 0 && atomicCAS(&st->code, 0, (int)FSPH_ERR_STACK_OVERFLOW) == 0)
+            st->index = gf;
+          break;
+        }
+        if(ca[0] && !lf[0])
+          stack[sp + __popc(bi0 & lt)] = cc[0];
+        if(ca[1] && !lf[1])
+          stack[sp + __popc(bi0) + __popc(bi1 & lt)] = cc[1];
+        sp += npush;
+        // a node's two leaves go side by side (lane order, left first): the
+        // lists keep the tree's index order, which the pair passes' gathers
+        // share between the lanes of a group
+        const int lfirst = ncand + __popc(bl0 & lt) + __popc(bl1 & lt);
+        for(int c = 0; c < 2; ++c) {
+          if(ca[c] && lf[c]) {
+            const int pos = lfirst + (c && ca[0] && lf[0] ? 1 : 0);
+            const int4 ql = cl[c];
+            // minus the position relative to the group box corner, in FP32
+            cxs[pos] = -((float)(ql.x - glo.x) * qs0);
+            cys[pos] = -((float)(ql.y - glo.y) * qs1);
+            czs[pos] = -((float)(ql.z - glo.z) * qs2);
+            if(!UNI)
+              chs[pos] = __int_as_float(ql.w);
+            cidx[pos] = ~cc[c];
+          }
+        }
+        ncand += __popc(bl0) + __popc(bl1);
+      }
+      else {
       bool acc = false;
       const bool leaf = node < 0;
       int4 ql = make_int4(0, 0, 0, 0);
@@ -1093,22 +1193,13 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
       if(acc && leaf) {
         const int j = ~node;
         const int pos = ncand + __popc(bl & lt);
-        if(ORDERED)
-          ckey[pos] = ((unsigned long long)T.edepth[j] << 32) | (unsigned)j;
-        else {
-          // minus the position relative to the group box corner, in FP32
-          cxs[pos] = -((float)(ql.x - glo.x) * qs0);
-          cys[pos] = -((float)(ql.y - glo.y) * qs1);
-          czs[pos] = -((float)(ql.z - glo.z) * qs2);
-          if(!UNI)
-            chs[pos] = __int_as_float(ql.w);
-          cidx[pos] = j;
-        }
+        ckey[pos] = ((unsigned long long)T.edepth[j] << 32) | (unsigned)j;
       }
       ncand += __popc(bl);
+      }
       __syncwarp();
       const bool last = (sp == 0);
-      if(ncand > cap - 33 || (last && ncand > 0)) {
+      if(ncand > cap - (ORDERED ? 33 : 65) || (last && ncand > 0)) {
         if(!last)
           chunked = true;
         if(ORDERED)
