@@ -55,12 +55,12 @@ sys.path.insert(0, ROOT)
 HBM_PEAK = 6815.2  # GB/s, MEASURED_PEAKS.json hbm_gbs
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per particle of the
 # dominant kernel of a phase, from 96^3 Sedov captures (884,736 particles;
-# lists and records well above L2): the walk, the mean of two launches
-# (488.3 MB, profiles/k_neighbors_traffic_sedov3d_96.md); the float-float
+# lists and records well above L2): the walk (459.4 MB,
+# profiles/k_neighbors_uni_sedov3d_96.md); the float-float
 # density and acceleration passes and the de/dt pass of the warm-up
 # iteration (567.6, 569.2 and 597.8 MB,
 # profiles/k_density_ff_accel_ff_dedt_ahyd_sedov3d_96.md)
-MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 551.9, "density": 641.6, "accel": 643.3,
+MEASURED_TRAFFIC_PER_PARTICLE = {"neighbors": 519.3, "density": 641.6, "accel": 643.3,
                                  "energy": 675.7}
 
 

@@ -73,11 +73,16 @@ __global__ void k_pack_pos(Particles P, int dim,
   ((float2 *)K.fmA)[2 * i] = make_float2(mh, (float)(m - (double)mh));
 }
 
+// PACK_VHM: {v_half, m} and m alone (the FP32 passes, the alpha pass);
+// PACK_VEL: {v, c_s before the density pass} (the signal speed);
 // PACK_AV_IN: {c_s, sign(div v)} for the Cullen & Dehnen alpha pass;
-// PACK_AV: {alpha, 0} for the pair passes that weight the viscosity by it.
-// PACK_DEDT: the de/dt pass's {v, P/rho^2} and {rho, c_s} records.
+// PACK_AV: {alpha, 0} for the pair passes that weight the viscosity by it;
+// PACK_DEDT: the FP32 de/dt pass's {v, P/rho^2} and {rho, c_s} records;
+// PACK_FV: v_half's high and low words with rho and c_s (the float-float
+// acceleration pass, the energy passes); PACK_FDV: {v - v_half, m} (the
+// energy passes).  Each pass packs only what its kernels read.
 enum { PACK_VHM = 1, PACK_VEL = 2, PACK_THERMO = 4, PACK_AV_IN = 8, PACK_AV = 16,
-       PACK_DEDT = 32 };
+       PACK_DEDT = 32, PACK_FV = 64, PACK_FDV = 128 };
 
 // Refresh the packed records a pass reads from the FP64 state, so every
 // pass sees the current v_half, v, rho, P and c_s whatever the caller did
@@ -92,18 +97,21 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
     h = (float)v;
     l = (float)(v - (double)h);
   };
-  if(what & PACK_VHM) {
-    // fv1, fv2: v_half's words with rho and c_s as they stand (after the
-    // density pass the state holds the new c_s; before it, the values are
-    // rewritten by the next packing before any pass reads them)
-    const float m = (float)P.f[F_M][i];
+  if(what & (PACK_VHM | PACK_FV)) {
     float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
     for(int d = 0; d < dim; ++d)
       hl(F_VHX + d, h[d], l[d]);
-    K.vhm[i] = make_float4(h[0], h[1], h[2], m);
-    K.fv1[i] = make_float4(h[0], h[1], h[2], (float)P.f[F_RHO][i]);
-    K.fv2[i] = make_float4(l[0], l[1], l[2], (float)P.f[F_CS][i]);
-    K.mass[i] = m;
+    if(what & PACK_VHM) {
+      const float m = (float)P.f[F_M][i];
+      K.vhm[i] = make_float4(h[0], h[1], h[2], m);
+      K.mass[i] = m;
+    }
+    if(what & PACK_FV) {
+      // rho and c_s as the state holds them: after the density pass, the
+      // new c_s
+      K.fv1[i] = make_float4(h[0], h[1], h[2], (float)P.f[F_RHO][i]);
+      K.fv2[i] = make_float4(l[0], l[1], l[2], (float)P.f[F_CS][i]);
+    }
   }
   if(what & PACK_VEL)
     K.vel[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
@@ -128,6 +136,8 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
     K.velp[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)(P.f[F_P][i] / (rho * rho)));
     K.rc[i] = make_float2((float)rho, (float)P.f[F_CS][i]);
+  }
+  if(what & PACK_FDV) {
     float dv[3] = {0.f, 0.f, 0.f};
     for(int d = 0; d < dim; ++d)
       dv[d] = (float)(P.f[F_VX + d][i] - P.f[F_VHX + d][i]);
@@ -184,9 +194,10 @@ cudaError_t launch_density_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
   DevStatus * st, const DevTime * tm) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
-  // masses for the density sum, velocities of this step for the signal speed
+  // velocities of this step for the signal speed; masses for the FP32
+  // density pass (the float-float one reads them from the position packing)
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_VEL);
+    wendland_kernel(pp.kernel) ? PACK_VEL : PACK_VHM | PACK_VEL);
   *L.counter += 1;
   if(pp.cullen)
     run_density_mixed_cullen(L, P, pp, Ls, K, cs_new, st, tm);
@@ -226,8 +237,9 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   // records are refreshed unless they come straight from the density pass
   // (fused signal speed needs their previous-sound-speed slot)
   const int av = pp.cullen ? PACK_AV : 0;
+  const int vh = wendland_kernel(pp.kernel) ? PACK_FV : PACK_VHM;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    (fused_vsig ? PACK_VHM : (PACK_VHM | PACK_THERMO)) | av);
+    (fused_vsig ? vh : (vh | PACK_THERMO)) | av);
   *L.counter += 1;
   if(pp.cullen)
     run_accel_mixed_cullen(L, P, pp, Ls, K, kick, t, fused_vsig);
@@ -241,7 +253,7 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   int then_op) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
+    PACK_FV | PACK_FDV | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
     run_dudt_mixed_cullen(L, P, pp, Ls, K, t, then_op);
@@ -256,9 +268,10 @@ cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   // through a^P, v_half, rho and c_s are those the acceleration pass packed
   // (the caller's flag says so): only v - v_half is new
-  const int vhm = use_ahyd && wendland_kernel(pp.kernel) ? 0 : PACK_VHM;
+  const int what = use_ahyd && wendland_kernel(pp.kernel) ? PACK_FDV
+                                                          : PACK_VHM | PACK_DEDT;
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    vhm | PACK_DEDT | (pp.cullen ? PACK_AV : 0));
+    what | (pp.cullen ? PACK_AV : 0));
   *L.counter += 1;
   if(pp.cullen)
     run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st, use_ahyd);
