@@ -474,6 +474,30 @@ def ensemble_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def link_gbs(nbytes=256 << 20, reps=4):
+    """Host<->device copy rate of this machine right after the e2e loop: one
+    256 MiB pinned buffer copied `reps` times each way (CUDA events), so that
+    the e2e figure can be read against the link it ran on."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    out = {}
+    with torch.cuda.stream(s):
+        for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+            dst.copy_(src, non_blocking=True)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(s)
+            e1.synchronize()
+            out[name] = round(reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    del h, d
+    return out
+
+
 def one_pass(bs, state, p):
     """One pass of every physics callback from `state`: density, pressure,
     sound speed, acceleration, the energy rate and gravity."""
@@ -611,9 +635,18 @@ def gpu_arm(args):
             e2e_ms = bs.elapsed_ms(2, 3)
             wall = time.perf_counter() - t0
             e2e_ms = max_over_ranks(dist, e2e_ms)
+            # the same registered host buffers copied alone, once each way
+            bs.mark(4)
+            bs.upload_fields(vin)
+            bs.mark(5)
+            bs.download_into(vout)
+            bs.mark(6)
+            copy_gbs = {"h2d": round(h2d / (bs.elapsed_ms(4, 5) * 1e-3) / 1e9, 1),
+                        "d2h": round(d2h / (bs.elapsed_ms(5, 6) * 1e-3) / 1e9, 1)}
             for a in regs:
                 sph.host_unregister(a)
-            results[mode]["e2e"] = dict(ms=e2e_ms, wall_s=wall, h2d=h2d, d2h=d2h)
+            results[mode]["e2e"] = dict(ms=e2e_ms, wall_s=wall, h2d=h2d, d2h=d2h,
+                                        link_gbs=link_gbs(), copy_gbs=copy_gbs)
         bs.close()
 
     if rank != 0:
@@ -698,7 +731,12 @@ def gpu_arm(args):
     if "e2e" in head:
         e = head["e2e"]
         line["e2e"] = {"value": world * n * K / (e["ms"] * 1e-3), "unit": "particle-steps/s",
-                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"]}
+                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
+                       "ms_per_step": e["ms"] / K,
+                       "wall_ms_per_step": 1e3 * e["wall_s"] / K,
+                       "copy_gbs": e["copy_gbs"], "link_gbs": e["link_gbs"],
+                       "host": {"cpus": len(os.sched_getaffinity(0)),
+                                "loadavg_1min": os.getloadavg()[0]}}
     if args.workload == "kh":
         line["drift"] = {m: results[m]["drift"] for m in results}
     if args.workload == "polytrope":

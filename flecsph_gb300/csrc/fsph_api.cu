@@ -575,6 +575,7 @@ static fsph_status upload_impl(fsph_ctx * c, const fsph_soa_view * v,
      (c->p.dimension == 3 && !v->z) || !v->m || !v->h || !v->id)
     return FSPH_ERR_ARG;
   c->ahyd_ok = false;
+  c->fv_ok = c->fdv_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -635,6 +636,7 @@ static fsph_status upload_fields_impl(fsph_ctx * c, const fsph_soa_view * v,
   if(!c || !v || !c->uploaded || v->n != c->n)
     return FSPH_ERR_ARG;
   c->ahyd_ok = false;
+  c->fv_ok = c->fdv_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -810,6 +812,7 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
   if(!c || !c->uploaded)
     return FSPH_ERR_STATE;
   c->ahyd_ok = false;
+  c->fv_ok = c->fdv_ok = false;
   c->grav_nodes_ok = false;
   fsph_status s = set_device(c);
   if(s)
@@ -909,6 +912,8 @@ fsph_status fsph_compute_alpha(fsph_ctx * c) {
   return FSPH_OK;
 }
 
+static bool wendland(int k);
+
 static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
@@ -940,6 +945,8 @@ static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   double * t = c->P.f[F_CS];
   c->P.f[F_CS] = c->cs_new;
   c->cs_new = t;
+  // the float-float density pass (Wendland kernels) wrote the fv records
+  c->fv_ok = c->mixed && wendland(c->pp.kernel);
   return FSPH_OK;
 }
 
@@ -961,12 +968,16 @@ static fsph_status accel_impl(fsph_ctx * c, int kick, int fused_vsig = 0) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ACCEL);
   if(c->mixed)
-    CK(launch_accel_mixed(L, c->P, c->pp, c->Ls, c->K, kick, c->d_time, fused_vsig));
+    CK(launch_accel_mixed(L, c->P, c->pp, c->Ls, c->K, kick, c->d_time, fused_vsig,
+      c->fv_ok ? 1 : 0));
   else
     CK(launch_accel_fp64(L, c->P, c->pp, c->Ls, kick, c->d_time));
   // the float-float pass (Wendland kernels) leaves the pressure-only
-  // acceleration in K.ahyd for the de/dt pass
+  // acceleration in K.ahyd for the de/dt pass, and with the kick the
+  // {v - v_half, m} records of the kicked velocities
   c->ahyd_ok = c->mixed && c->K.ahyd && wendland(c->pp.kernel);
+  c->fv_ok = c->fv_ok || (c->mixed && wendland(c->pp.kernel));
+  c->fdv_ok = c->mixed && wendland(c->pp.kernel) && kick;
   return FSPH_OK;
 }
 
@@ -981,7 +992,8 @@ fsph_status fsph_dudt(fsph_ctx * c) {
   Launch L = c->L();
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
-    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, 0));
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, 0, c->fv_ok ? 1 : 0,
+      c->fdv_ok ? 1 : 0));
   else
     CK(launch_dudt_fp64(L, c->P, c->pp, c->Ls, c->d_time));
   return FSPH_OK;
@@ -997,7 +1009,7 @@ fsph_status fsph_dedt(fsph_ctx * c) {
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(c->mixed)
     CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, 0, c->d_time, c->d_status,
-      c->ahyd_ok ? 1 : 0));
+      c->ahyd_ok ? 1 : 0, c->fdv_ok ? 1 : 0));
   else
     CK(launch_dedt_fp64(L, c->P, c->pp, c->Ls));
   return FSPH_OK;
@@ -1021,11 +1033,13 @@ static fsph_status energy_then(fsph_ctx * c, bool thermo, int op) {
   Phase ph(c, FSPH_TIMER_ENERGY);
   if(thermo)
     CK(launch_dedt_mixed(L, c->P, c->pp, c->Ls, c->K, op, c->d_time, c->d_status,
-      c->ahyd_ok ? 1 : 0));
+      c->ahyd_ok ? 1 : 0, c->fdv_ok ? 1 : 0));
   else
-    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, op));
-  // the pressure update of `op` changes P/rho^2
+    CK(launch_dudt_mixed(L, c->P, c->pp, c->Ls, c->K, c->d_time, op, c->fv_ok ? 1 : 0,
+      c->fdv_ok ? 1 : 0));
+  // the pressure update of `op` changes P/rho^2 and c_s
   c->ahyd_ok = false;
+  c->fv_ok = false;
   return FSPH_OK;
 }
 
@@ -1058,10 +1072,13 @@ static fsph_status elem(fsph_ctx * c, int op, int phase) {
     return FSPH_ERR_STATE;
   // every update of positions, P/rho^2, v_half, alpha or h outdates the
   // pressure-only acceleration the de/dt pass would reuse
+  // (and the fv records), and any change of v the fdv records
   if(op != OP_KICK_V && op != OP_KICK_E && op != OP_KICK_U &&
      op != OP_SET_TOTAL_ENERGY && op != OP_DRAG_ACC && op != OP_DRAG_DEDT &&
      op != OP_DRAG_DUDT && op != OP_CHECK_NANS && op != OP_CHECK_NEGATIVITY)
-    c->ahyd_ok = false;
+    c->ahyd_ok = c->fv_ok = c->fdv_ok = false;
+  if(op == OP_KICK_V)
+    c->fdv_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;

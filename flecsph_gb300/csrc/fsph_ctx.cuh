@@ -57,6 +57,12 @@ struct fsph_ctx {
   // P/rho^2, v_half and alpha (set by the float-float acceleration pass,
   // cleared by every call that changes one of them)
   bool ahyd_ok = false;
+  // K.fv1/fv2 hold v_half (high and low words), rho and c_s of the current
+  // state (written by the float-float density pass); K.fdv holds v - v_half
+  // and m (written by the float-float acceleration pass with the kick).
+  // Cleared by every call that changes one of those fields.
+  bool fv_ok = false;
+  bool fdv_ok = false;
   bool uploaded = false;
   long long launches = 0;
   // timers

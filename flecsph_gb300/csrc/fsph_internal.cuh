@@ -260,15 +260,17 @@ cudaError_t launch_alpha_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 cudaError_t launch_vsig_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K);
+// fv_current / fdv_current: the fv1/fv2 (fdv) records already hold the
+// current state (the caller tracks it), so the pass does not repack them.
 cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
-  const DevTime * t, int fused_vsig);
+  const DevTime * t, int fused_vsig, int fv_current);
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
-  int then_op);
+  int then_op, int fv_current, int fdv_current);
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st, int use_ahyd);
+  const DevTime * t, DevStatus * st, int use_ahyd, int fdv_current);
 
 // ---- fsph_gravity.cu ----
 cudaError_t launch_let_export(const Launch & L, const Particles & P, int dim,

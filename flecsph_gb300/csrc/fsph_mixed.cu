@@ -80,9 +80,12 @@ __global__ void k_pack_pos(Particles P, int dim,
 // PACK_DEDT: the FP32 de/dt pass's {v, P/rho^2} and {rho, c_s} records;
 // PACK_FV: v_half's high and low words with rho and c_s (the float-float
 // acceleration pass, the energy passes); PACK_FDV: {v - v_half, m} (the
-// energy passes).  Each pass packs only what its kernels read.
+// energy passes); PACK_VEL_V: v alone into the PACK_VEL record, its c_s
+// slot left as the density pass found it (the alpha pass, between the
+// density pass and the acceleration pass that reads that slot).  Each pass
+// packs only what its kernels read.
 enum { PACK_VHM = 1, PACK_VEL = 2, PACK_THERMO = 4, PACK_AV_IN = 8, PACK_AV = 16,
-       PACK_DEDT = 32, PACK_FV = 64, PACK_FDV = 128 };
+       PACK_DEDT = 32, PACK_FV = 64, PACK_FDV = 128, PACK_VEL_V = 256 };
 
 // Refresh the packed records a pass reads from the FP64 state, so every
 // pass sees the current v_half, v, rho, P and c_s whatever the caller did
@@ -116,6 +119,12 @@ __global__ void k_pack_state(Particles P, int dim, Packed K, int what) {
   if(what & PACK_VEL)
     K.vel[i] = make_float4((float)P.f[F_VX][i], (float)P.f[F_VY][i],
       dim == 3 ? (float)P.f[F_VZ][i] : 0.f, (float)P.f[F_CS][i]);
+  if(what & PACK_VEL_V) {
+    float * v = (float *)&K.vel[i];
+    v[0] = (float)P.f[F_VX][i];
+    v[1] = (float)P.f[F_VY][i];
+    v[2] = dim == 3 ? (float)P.f[F_VZ][i] : 0.f;
+  }
   if(what & PACK_THERMO) {
     const double rho = P.f[F_RHO][i], cs = P.f[F_CS][i];
     const double A = P.f[F_P][i] / (rho * rho);
@@ -212,7 +221,7 @@ cudaError_t launch_alpha_mixed(const Launch & L, const Particles & P,
   // current velocities and masses; sound speeds and div v signs of the
   // neighbours
   k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_VHM | PACK_VEL | PACK_AV_IN);
+    PACK_VHM | PACK_VEL_V | PACK_AV_IN);
   *L.counter += 1;
   run_alpha_mixed(L, P, pp, Ls, K, t);
   return cudaGetLastError();
@@ -231,16 +240,18 @@ cudaError_t launch_vsig_mixed(const Launch & L, const Particles & P,
 
 cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int kick,
-  const DevTime * t, int fused_vsig) {
+  const DevTime * t, int fused_vsig, int fv_current) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   // v_half of this step (set by the caller's save_velocityhalf); the thermo
   // records are refreshed unless they come straight from the density pass
   // (fused signal speed needs their previous-sound-speed slot)
   const int av = pp.cullen ? PACK_AV : 0;
-  const int vh = wendland_kernel(pp.kernel) ? PACK_FV : PACK_VHM;
-  k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    (fused_vsig ? vh : (vh | PACK_THERMO)) | av);
-  *L.counter += 1;
+  const int vh = wendland_kernel(pp.kernel) ? (fv_current ? 0 : PACK_FV) : PACK_VHM;
+  const int what = (fused_vsig ? vh : (vh | PACK_THERMO)) | av;
+  if(what) {
+    k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K, what);
+    *L.counter += 1;
+  }
   if(pp.cullen)
     run_accel_mixed_cullen(L, P, pp, Ls, K, kick, t, fused_vsig);
   else
@@ -250,11 +261,14 @@ cudaError_t launch_accel_mixed(const Launch & L, const Particles & P,
 
 cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t,
-  int then_op) {
+  int then_op, int fv_current, int fdv_current) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
-  k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    PACK_FV | PACK_FDV | (pp.cullen ? PACK_AV : 0));
-  *L.counter += 1;
+  const int what = (fv_current ? 0 : PACK_FV) | (fdv_current ? 0 : PACK_FDV) |
+                   (pp.cullen ? PACK_AV : 0);
+  if(what) {
+    k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K, what);
+    *L.counter += 1;
+  }
   if(pp.cullen)
     run_dudt_mixed_cullen(L, P, pp, Ls, K, t, then_op);
   else
@@ -264,15 +278,18 @@ cudaError_t launch_dudt_mixed(const Launch & L, const Particles & P,
 
 cudaError_t launch_dedt_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, int then_op,
-  const DevTime * t, DevStatus * st, int use_ahyd) {
+  const DevTime * t, DevStatus * st, int use_ahyd, int fdv_current) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
   // through a^P, v_half, rho and c_s are those the acceleration pass packed
-  // (the caller's flag says so): only v - v_half is new
-  const int what = use_ahyd && wendland_kernel(pp.kernel) ? PACK_FDV
-                                                          : PACK_VHM | PACK_DEDT;
-  k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    what | (pp.cullen ? PACK_AV : 0));
-  *L.counter += 1;
+  // (the caller's flag says so): only v - v_half is new, and not even that
+  // when the acceleration pass's kick wrote it
+  const int what = (use_ahyd && wendland_kernel(pp.kernel)
+                      ? (fdv_current ? 0 : PACK_FDV) : PACK_VHM | PACK_DEDT) |
+                   (pp.cullen ? PACK_AV : 0);
+  if(what) {
+    k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K, what);
+    *L.counter += 1;
+  }
   if(pp.cullen)
     run_dedt_mixed_cullen(L, P, pp, Ls, K, then_op, t, st, use_ahyd);
   else

@@ -864,6 +864,18 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
   Kp.thermo[a] = make_float4((float)rho, (float)A, (float)cs, (float)P.f[F_CS][a]);
   const float Ah = (float)A;
   ((float2 *)Kp.fmA)[2 * a + 1] = make_float2(Ah, (float)(A - (double)Ah));
+  {
+    // the acceleration and energy passes' v_half records (high and low
+    // words) with this pass's rho and new c_s
+    float vh[3] = {0.f, 0.f, 0.f}, vl[3] = {0.f, 0.f, 0.f};
+    for(int d = 0; d < D; ++d) {
+      const double v = P.f[F_VHX + d][a];
+      vh[d] = (float)v;
+      vl[d] = (float)(v - (double)vh[d]);
+    }
+    Kp.fv1[a] = make_float4(vh[0], vh[1], vh[2], (float)rho);
+    Kp.fv2[a] = make_float4(vl[0], vl[1], vl[2], (float)cs);
+  }
   if(CULL) {
     double div_v = 0.0;
     for(int d = 0; d < D; ++d)
@@ -1031,12 +1043,19 @@ __global__ void __launch_bounds__(FSPH_ACCEL_FF_THREADS, FSPH_ACCEL_FF_BLOCKS) k
       acc[d] += ext[d];
   }
   const double half_dt = kick ? 0.5 * tm->dt : 0.0;
+  float dv[3] = {0.f, 0.f, 0.f};
   for(int d = 0; d < D; ++d) {
     P.f[F_AX + d][a] = acc[d];
     P.f[F_GAX + d][a] = 0.0;
-    if(kick)
-      P.f[F_VX + d][a] = P.f[F_VX + d][a] + acc[d] * half_dt;
+    if(kick) {
+      const double v = P.f[F_VX + d][a] + acc[d] * half_dt;
+      P.f[F_VX + d][a] = v;
+      dv[d] = (float)(v - P.f[F_VHX + d][a]);
+    }
   }
+  // the energy passes' {v - v_half, m} record of the kicked velocity
+  if(kick)
+    Kp.fdv[a] = make_float4(dv[0], dv[1], dv[2], (float)P.f[F_M][a]);
   P.f[F_GPOT][a] = 0.0;
   if(VSIG)
     P.f[F_VSIG][a] = (double)r.vsig;

@@ -525,9 +525,37 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
 // refboxes: also the reference's x +- h/2 node boxes (box2, fbox2), which
 // the walk's node tests read: with varying h, or in the ordered (FP64) mode
 // where equal-h ties take them too.
-__global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
-  const unsigned long long * rbits, int refboxes) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Shared-memory layout of one k_bounds block (dynamic): the node data of the
+// internal nodes whose leaf range lies inside the block's own leaves (slot =
+// node index - first leaf of the block: such a node's index is one end of
+// its range), and their arrival counters.
+#define BOUNDS_THREADS 256
+__host__ __device__ constexpr size_t bounds_smem(bool gmom) {
+  return (size_t)BOUNDS_THREADS * (2 * sizeof(int4) + 6 * sizeof(double) + sizeof(unsigned) +
+                                   (gmom ? 10 * sizeof(double) : 0));
+}
+
+// The bottom-up pass: each leaf's thread climbs while it is the second of a
+// node's two children to finish.  A node whose leaf range lies inside the
+// block's 256 leaves has both subtrees finished by threads of this block,
+// so its arrival count and its children's data live in shared memory (the
+// bulk of the nodes: a range straddles a block boundary with probability
+// ~size/256); only the nodes above those go through device memory.  Node
+// data are combined in the same order either way (left child, then right),
+// so the sums do not depend on where a node was combined.
+template<int dim>
+__global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds(Particles P, Tree T,
+  const int4 * qpos, const unsigned long long * rbits, int refboxes) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  int4 * sq = (int4 *)bsm;                                // lo, hi per slot
+  double * sb = (double *)(sq + 2 * BOUNDS_THREADS);      // box2 lo xyz, hi xyz
+  unsigned * scnt = (unsigned *)(sb + 6 * BOUNDS_THREADS);
+  double * sg = (double *)(scnt + BOUNDS_THREADS);        // ten moments (gravity)
+  const int b0 = blockIdx.x * BOUNDS_THREADS;
+  const int b1 = min(b0 + BOUNDS_THREADS, P.n) - 1;
+  scnt[threadIdx.x] = 0u;
+  __syncthreads();
+  const int i = b0 + threadIdx.x;
   if(i >= P.n)
     return;
   const bool nonuni = refboxes || rbits[6] != rbits[7];
@@ -538,20 +566,29 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       rc[d] = 0.5 * (r0[d] + ord_dec(rbits[3 + d]));
   }
   int p = T.leaf_parent[i];
-  // Leaves write nothing here.  The arrival count at the parent is an
-  // acquire-release atomic at device scope: it publishes this thread's
-  // node data (release) to the sibling's thread, which reads it after its
-  // own arrival (acquire; the reads go through L2 with __ldcg), so no
-  // full fence is needed per level.
   while(p >= 0) {
+    const bool local = T.first[p] >= b0 && T.last[p] <= b1;
     unsigned prior;
-    asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
-                 : "=r"(prior) : "l"(T.counter + p) : "memory");
+    if(local) {
+      // shared-memory count at block scope: the fences order this thread's
+      // node data before the count (release) and the sibling's after it
+      // (acquire)
+      __threadfence_block();
+      prior = atomicAdd(&scnt[p - b0], 1u);
+      __threadfence_block();
+    }
+    else {
+      // device-scope acquire-release count: publishes this thread's node
+      // data (release) to the sibling's thread, which reads it after its
+      // own arrival (acquire; the reads go through L2 with __ldcg)
+      asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
+                   : "=r"(prior) : "l"(T.counter + p) : "memory");
+    }
     if(prior == 0)
       return;  // the sibling subtree is not finished yet
+    const int cg[2] = {T.left[p], T.right[p]};
     if(T.gmom) {
       double S[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-      const int cg[2] = {T.left[p], T.right[p]};
       for(int c = 0; c < 2; ++c) {
         if(cg[c] < 0) {
           const int j = ~cg[c];
@@ -571,6 +608,11 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
           S[8] += my[0] * y[2];
           S[9] += my[1] * y[2];
         }
+        else if(local) {
+          const double * cs = sg + (cg[c] - b0);
+          for(int k = 0; k < 10; ++k)
+            S[k] += cs[k * BOUNDS_THREADS];
+        }
         else {
           const double * cs = T.gmom + 10 * (size_t)cg[c];
           for(int k = 0; k < 10; ++k)
@@ -580,6 +622,9 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       double * out = T.gmom + 10 * (size_t)p;
       for(int k = 0; k < 10; ++k)
         out[k] = S[k];
+      if(local)
+        for(int k = 0; k < 10; ++k)
+          sg[k * BOUNDS_THREADS + (p - b0)] = S[k];
     }
     int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
     int hi[3] = {-1, -1, -1};
@@ -591,10 +636,9 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
       n2.lo[d] = 1e308;
       n2.hi[d] = -1e308;
     }
-    int ch[2] = {T.left[p], T.right[p]};
     for(int c = 0; c < 2; ++c) {
-      if(ch[c] < 0) {
-        const int j = ~ch[c];
+      if(cg[c] < 0) {
+        const int j = ~cg[c];
         const int4 q = qpos[j];
         lo[0] = min(lo[0], q.x); hi[0] = max(hi[0], q.x);
         lo[1] = min(lo[1], q.y); hi[1] = max(hi[1], q.y);
@@ -610,31 +654,59 @@ __global__ void k_bounds(Particles P, int dim, Tree T, const int4 * qpos,
         }
       }
       else {
-        const int4 * cq = &T.qbox[2 * ch[c]];
-        const int4 a = __ldcg(cq), b = __ldcg(cq + 1);
+        int4 a, b;
+        if(local) {
+          a = sq[2 * (cg[c] - b0)];
+          b = sq[2 * (cg[c] - b0) + 1];
+        }
+        else {
+          const int4 * cq = &T.qbox[2 * cg[c]];
+          a = __ldcg(cq);
+          b = __ldcg(cq + 1);
+        }
         lo[0] = min(lo[0], a.x); lo[1] = min(lo[1], a.y); lo[2] = min(lo[2], a.z);
         hi[0] = max(hi[0], b.x); hi[1] = max(hi[1], b.y); hi[2] = max(hi[2], b.z);
         hm = fmaxf(hm, __int_as_float(a.w));
         if(nonuni) {
-          const double * cb2 = (const double *)&T.box2[ch[c]];
-          for(int d = 0; d < dim; ++d) {
-            n2.lo[d] = fmin(n2.lo[d], __ldcg(cb2 + d));
-            n2.hi[d] = fmax(n2.hi[d], __ldcg(cb2 + 4 + d));
+          if(local) {
+            const double * cb2 = sb + (cg[c] - b0);
+            for(int d = 0; d < dim; ++d) {
+              n2.lo[d] = fmin(n2.lo[d], cb2[d * BOUNDS_THREADS]);
+              n2.hi[d] = fmax(n2.hi[d], cb2[(3 + d) * BOUNDS_THREADS]);
+            }
+          }
+          else {
+            const double * cb2 = (const double *)&T.box2[cg[c]];
+            for(int d = 0; d < dim; ++d) {
+              n2.lo[d] = fmin(n2.lo[d], __ldcg(cb2 + d));
+              n2.hi[d] = fmax(n2.hi[d], __ldcg(cb2 + 4 + d));
+            }
           }
         }
       }
     }
     // children of a radix-tree node are always (split, split + 1): store
     // split and the two leaf flags with the box, so the walk needs one load
-    const int l = T.left[p], r = T.right[p];
+    const int l = cg[0], r = cg[1];
     const int split = l < 0 ? ~l : l;
     const int code = (split << 2) | ((l < 0) << 1) | (r < 0);
-    T.qbox[2 * p] = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
-    T.qbox[2 * p + 1] = make_int4(hi[0], hi[1], hi[2], code);
+    const int4 qlo = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
+    const int4 qhi = make_int4(hi[0], hi[1], hi[2], code);
+    T.qbox[2 * p] = qlo;
+    T.qbox[2 * p + 1] = qhi;
+    if(local) {
+      sq[2 * (p - b0)] = qlo;
+      sq[2 * (p - b0) + 1] = qhi;
+    }
     if(nonuni) {
       if(dim == 2)
         n2.lo[2] = n2.hi[2] = 0;
       T.box2[p] = n2;
+      if(local)
+        for(int d = 0; d < 3; ++d) {
+          sb[d * BOUNDS_THREADS + (p - b0)] = n2.lo[d];
+          sb[(3 + d) * BOUNDS_THREADS + (p - b0)] = n2.hi[d];
+        }
       float fl[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
       for(int d = 0; d < dim; ++d) {
         fl[d] = __double2float_rd(n2.lo[d] - r0[d]);
@@ -751,7 +823,12 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   k_karras<<<(n + 254) / 256, 256, 0, L.stream>>>(P.key, n, T);
   if(ordered)  // reference octree depths order the FP64 lists
     k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
-  k_bounds<<<(n + 255) / 256, 256, 0, L.stream>>>(P, pp.dim, T, qpos, rbits, ordered);
+  const int nbb = (n + BOUNDS_THREADS - 1) / BOUNDS_THREADS;
+  const size_t bsm = bounds_smem(T.gmom != nullptr);
+  if(pp.dim == 3)
+    k_bounds<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+  else
+    k_bounds<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max, pp.dim, qscale,
     rbits);
   k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits,
