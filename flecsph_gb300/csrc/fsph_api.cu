@@ -575,7 +575,7 @@ static fsph_status upload_impl(fsph_ctx * c, const fsph_soa_view * v,
      (c->p.dimension == 3 && !v->z) || !v->m || !v->h || !v->id)
     return FSPH_ERR_ARG;
   c->ahyd_ok = false;
-  c->fv_ok = c->fdv_ok = false;
+  c->fv_ok = c->fdv_ok = c->vel_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -636,7 +636,7 @@ static fsph_status upload_fields_impl(fsph_ctx * c, const fsph_soa_view * v,
   if(!c || !v || !c->uploaded || v->n != c->n)
     return FSPH_ERR_ARG;
   c->ahyd_ok = false;
-  c->fv_ok = c->fdv_ok = false;
+  c->fv_ok = c->fdv_ok = c->vel_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;
@@ -808,11 +808,13 @@ fsph_status fsph_get_range(fsph_ctx * c, double * range) {
 }
 
 // ------------------------------------------------------------ body_system
+static bool wendland(int k);
+
 fsph_status fsph_update_iteration(fsph_ctx * c) {
   if(!c || !c->uploaded)
     return FSPH_ERR_STATE;
   c->ahyd_ok = false;
-  c->fv_ok = c->fdv_ok = false;
+  c->fv_ok = c->fdv_ok = c->vel_ok = false;
   c->grav_nodes_ok = false;
   fsph_status s = set_device(c);
   if(s)
@@ -852,7 +854,11 @@ fsph_status fsph_update_iteration(fsph_ctx * c) {
       CK(cudaStreamWaitEvent(c->stream, c->io.ev[0], 0));
       c->io.h2d_pending = false;
     }
-    CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys, c->permute_skip));
+    // the mixed float-float path's {v, c_s} records come out of the permute
+    float4 * vel = c->mixed && wendland(c->pp.kernel) ? c->K.vel : nullptr;
+    CK(launch_permute(L, c->P, c->Palt, c->svals, c->skeys, c->permute_skip, vel,
+      c->pp.dim));
+    c->vel_ok = vel != nullptr;
     Particles t = c->P;
     c->P = c->Palt;
     c->Palt = t;
@@ -912,8 +918,6 @@ fsph_status fsph_compute_alpha(fsph_ctx * c) {
   return FSPH_OK;
 }
 
-static bool wendland(int k);
-
 static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   if(!c || !c->tree_ok)
     return FSPH_ERR_STATE;
@@ -926,7 +930,7 @@ static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
     {
       Phase ph(c, FSPH_TIMER_DENSITY);
       CK(launch_density_mixed(L, c->P, c->pp, c->Ls, c->K, c->cs_new, c->d_status,
-        c->d_time));
+        c->d_time, c->vel_ok ? 1 : 0));
     }
     if(with_vsig) {
       Phase ph(c, FSPH_TIMER_VSIG);
@@ -945,8 +949,10 @@ static fsph_status density_impl(fsph_ctx * c, bool with_vsig) {
   double * t = c->P.f[F_CS];
   c->P.f[F_CS] = c->cs_new;
   c->cs_new = t;
-  // the float-float density pass (Wendland kernels) wrote the fv records
+  // the float-float density pass (Wendland kernels) wrote the fv records;
+  // the sound speeds in K.vel are now the previous ones
   c->fv_ok = c->mixed && wendland(c->pp.kernel);
+  c->vel_ok = false;
   return FSPH_OK;
 }
 
@@ -1039,7 +1045,7 @@ static fsph_status energy_then(fsph_ctx * c, bool thermo, int op) {
       c->fdv_ok ? 1 : 0));
   // the pressure update of `op` changes P/rho^2 and c_s
   c->ahyd_ok = false;
-  c->fv_ok = false;
+  c->fv_ok = c->vel_ok = false;
   return FSPH_OK;
 }
 
@@ -1076,9 +1082,9 @@ static fsph_status elem(fsph_ctx * c, int op, int phase) {
   if(op != OP_KICK_V && op != OP_KICK_E && op != OP_KICK_U &&
      op != OP_SET_TOTAL_ENERGY && op != OP_DRAG_ACC && op != OP_DRAG_DEDT &&
      op != OP_DRAG_DUDT && op != OP_CHECK_NANS && op != OP_CHECK_NEGATIVITY)
-    c->ahyd_ok = c->fv_ok = c->fdv_ok = false;
+    c->ahyd_ok = c->fv_ok = c->fdv_ok = c->vel_ok = false;
   if(op == OP_KICK_V)
-    c->fdv_ok = false;
+    c->fdv_ok = c->vel_ok = false;
   fsph_status s = set_device(c);
   if(s)
     return s;

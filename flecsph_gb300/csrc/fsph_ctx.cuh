@@ -63,6 +63,9 @@ struct fsph_ctx {
   // Cleared by every call that changes one of those fields.
   bool fv_ok = false;
   bool fdv_ok = false;
+  // K.vel holds v and c_s of the current state (written by the permute of
+  // update_iteration on the mixed path)
+  bool vel_ok = false;
   bool uploaded = false;
   long long launches = 0;
   // timers

@@ -241,7 +241,7 @@ cudaError_t launch_check_duplicates(const Launch & L,
   const unsigned long long * keys, int n, DevStatus * st);
 cudaError_t launch_permute(const Launch & L, const Particles & src,
   const Particles & dst, const int * perm, const unsigned long long * keys,
-  unsigned skip);
+  unsigned skip, float4 * vel = nullptr, int dim = 3);
 struct Packed;
 cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const PhysParams & pp, Tree & T, int group_max,
@@ -255,7 +255,7 @@ cudaError_t launch_pack_positions(const Launch & L, const Particles & P,
   const PhysParams & pp, const unsigned long long * rbits, const Packed & K);
 cudaError_t launch_density_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
-  DevStatus * st, const DevTime * tm);
+  DevStatus * st, const DevTime * tm, int vel_current);
 cudaError_t launch_alpha_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, const DevTime * t);
 cudaError_t launch_vsig_mixed(const Launch & L, const Particles & P,

@@ -201,13 +201,17 @@ __global__ void __launch_bounds__(MIX_THREADS) k_vsig_mixed(Particles P,
 
 cudaError_t launch_density_mixed(const Launch & L, const Particles & P,
   const PhysParams & pp, const Lists & Ls, const Packed & K, double * cs_new,
-  DevStatus * st, const DevTime * tm) {
+  DevStatus * st, const DevTime * tm, int vel_current) {
   const int nb = (P.n + MIX_THREADS - 1) / MIX_THREADS;
-  // velocities of this step for the signal speed; masses for the FP32
-  // density pass (the float-float one reads them from the position packing)
-  k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K,
-    wendland_kernel(pp.kernel) ? PACK_VEL : PACK_VHM | PACK_VEL);
-  *L.counter += 1;
+  // velocities of this step for the signal speed (unless the permute of
+  // update_iteration wrote them); masses for the FP32 density pass (the
+  // float-float one reads them from the position packing)
+  const int what = wendland_kernel(pp.kernel) ? (vel_current ? 0 : PACK_VEL)
+                                              : PACK_VHM | PACK_VEL;
+  if(what) {
+    k_pack_state<<<nb, MIX_THREADS, 0, L.stream>>>(P, pp.dim, K, what);
+    *L.counter += 1;
+  }
   if(pp.cullen)
     run_density_mixed_cullen(L, P, pp, Ls, K, cs_new, st, tm);
   else

@@ -420,9 +420,11 @@ cudaError_t launch_check_duplicates(const Launch & L,
 }
 
 // Fields whose bit is set in `skip` are left behind: the caller overwrites
-// them before anything reads them.
+// them before anything reads them.  With `vel`, the mixed path's
+// {v, c_s} record of the new order is written on the way (what the density
+// pass would otherwise pack).
 __global__ void k_permute(Particles src, Particles dst, const int * perm,
-  const unsigned long long * keys, unsigned skip) {
+  const unsigned long long * keys, unsigned skip, float4 * vel, int dim) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= src.n)
     return;
@@ -433,12 +435,16 @@ __global__ void k_permute(Particles src, Particles dst, const int * perm,
       dst.f[k][i] = src.f[k][p];
   dst.id[i] = src.id[p];
   dst.key[i] = keys[i];
+  if(vel)
+    vel[i] = make_float4((float)src.f[F_VX][p], (float)src.f[F_VY][p],
+      dim == 3 ? (float)src.f[F_VZ][p] : 0.f, (float)src.f[F_CS][p]);
 }
 
 cudaError_t launch_permute(const Launch & L, const Particles & src,
   const Particles & dst, const int * perm, const unsigned long long * keys,
-  unsigned skip) {
-  k_permute<<<(src.n + 255) / 256, 256, 0, L.stream>>>(src, dst, perm, keys, skip);
+  unsigned skip, float4 * vel, int dim) {
+  k_permute<<<(src.n + 255) / 256, 256, 0, L.stream>>>(src, dst, perm, keys, skip, vel,
+    dim);
   *L.counter += 1;
   return cudaGetLastError();
 }
@@ -528,43 +534,213 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
 // Shared-memory layout of one k_bounds block (dynamic): the node data of the
 // internal nodes whose leaf range lies inside the block's own leaves (slot =
 // node index - first leaf of the block: such a node's index is one end of
-// its range), and their arrival counters.
+// its range), their arrival counters, two work queues and the list of the
+// block's topmost nodes (and leaves) whose parents lie outside it.
 #define BOUNDS_THREADS 256
 __host__ __device__ constexpr size_t bounds_smem(bool gmom) {
   return (size_t)BOUNDS_THREADS * (2 * sizeof(int4) + 6 * sizeof(double) + sizeof(unsigned) +
-                                   (gmom ? 10 * sizeof(double) : 0));
+                                   3 * sizeof(int) + (gmom ? 10 * sizeof(double) : 0)) +
+         4 * sizeof(int);
 }
 
-// The bottom-up pass: each leaf's thread climbs while it is the second of a
-// node's two children to finish.  A node whose leaf range lies inside the
-// block's 256 leaves has both subtrees finished by threads of this block,
-// so its arrival count and its children's data live in shared memory (the
-// bulk of the nodes: a range straddles a block boundary with probability
-// ~size/256); only the nodes above those go through device memory.  Node
-// data are combined in the same order either way (left child, then right),
-// so the sums do not depend on where a node was combined.
+struct BoundsShared {
+  int4 * sq;        // lo, hi per slot
+  double * sb;      // box2 lo xyz, hi xyz per slot
+  unsigned * scnt;  // arrival counts per slot
+  int * queue;      // 2 x 256: nodes whose two children are done, this round and next
+  int * exits;      // nodes (~leaf for a leaf) whose parent is outside the block
+  int * counts;     // queue lengths [2], exit count
+  double * sg;      // ten moments per slot (gravity)
+};
+
+// Node p's data from its two children, written to device memory and, for a
+// node inside the block (local), to its shared-memory slot.  A local node's
+// inner children are local too and are read from shared memory; the
+// children of other nodes from device memory through L2.  Children combine
+// in a fixed order (left, then right), so the sums do not depend on which
+// thread or path combined a node.
 template<int dim>
-__global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds(Particles P, Tree T,
+__device__ __forceinline__ void bounds_node(const Particles & P, const Tree & T, const int4 * qpos,
+  const BoundsShared & S, int p, bool local, int b0, bool nonuni, const double * rc,
+  const double * r0) {
+  const int cg[2] = {T.left[p], T.right[p]};
+  if(T.gmom) {
+    double M[10];
+    for(int c = 0; c < 2; ++c) {
+      double C[10];
+      if(cg[c] < 0) {
+        const int j = ~cg[c];
+        const double m = P.f[F_M][j];
+        double y[3] = {0.0, 0.0, 0.0};
+        for(int d = 0; d < dim; ++d)
+          y[d] = P.f[F_X + d][j] - rc[d];
+        const double my[3] = {m * y[0], m * y[1], m * y[2]};
+        C[0] = m;
+        C[1] = my[0];
+        C[2] = my[1];
+        C[3] = my[2];
+        C[4] = my[0] * y[0];
+        C[5] = my[1] * y[1];
+        C[6] = my[2] * y[2];
+        C[7] = my[0] * y[1];
+        C[8] = my[0] * y[2];
+        C[9] = my[1] * y[2];
+      }
+      else if(local) {
+        const double * cs = S.sg + (cg[c] - b0);
+        for(int k = 0; k < 10; ++k)
+          C[k] = cs[k * BOUNDS_THREADS];
+      }
+      else {
+        const double * cs = T.gmom + 10 * (size_t)cg[c];
+        for(int k = 0; k < 10; ++k)
+          C[k] = __ldcg(cs + k);
+      }
+      for(int k = 0; k < 10; ++k)
+        M[k] = c == 0 ? C[k] : M[k] + C[k];
+    }
+    double * out = T.gmom + 10 * (size_t)p;
+    for(int k = 0; k < 10; ++k)
+      out[k] = M[k];
+    if(local)
+      for(int k = 0; k < 10; ++k)
+        S.sg[k * BOUNDS_THREADS + (p - b0)] = M[k];
+  }
+  int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
+  int hi[3] = {-1, -1, -1};
+  float hm = 0.f;
+  double blo[3] = {1e308, 1e308, 1e308}, bhi[3] = {-1e308, -1e308, -1e308};
+  for(int c = 0; c < 2; ++c) {
+    if(cg[c] < 0) {
+      const int j = ~cg[c];
+      const int4 q = qpos[j];
+      lo[0] = min(lo[0], q.x); hi[0] = max(hi[0], q.x);
+      lo[1] = min(lo[1], q.y); hi[1] = max(hi[1], q.y);
+      lo[2] = min(lo[2], q.z); hi[2] = max(hi[2], q.z);
+      hm = fmaxf(hm, __int_as_float(q.w));
+      if(nonuni) {
+        const double hj = P.f[F_H][j];
+        for(int d = 0; d < dim; ++d) {
+          double x = P.f[F_X + d][j];
+          blo[d] = fmin(blo[d], x - hj / 2.);
+          bhi[d] = fmax(bhi[d], x + hj / 2.);
+        }
+      }
+    }
+    else {
+      int4 a, b;
+      if(local) {
+        a = S.sq[2 * (cg[c] - b0)];
+        b = S.sq[2 * (cg[c] - b0) + 1];
+      }
+      else {
+        const int4 * cq = &T.qbox[2 * cg[c]];
+        a = __ldcg(cq);
+        b = __ldcg(cq + 1);
+      }
+      lo[0] = min(lo[0], a.x); lo[1] = min(lo[1], a.y); lo[2] = min(lo[2], a.z);
+      hi[0] = max(hi[0], b.x); hi[1] = max(hi[1], b.y); hi[2] = max(hi[2], b.z);
+      hm = fmaxf(hm, __int_as_float(a.w));
+      if(nonuni) {
+        if(local) {
+          const double * cb2 = S.sb + (cg[c] - b0);
+          for(int d = 0; d < dim; ++d) {
+            blo[d] = fmin(blo[d], cb2[d * BOUNDS_THREADS]);
+            bhi[d] = fmax(bhi[d], cb2[(3 + d) * BOUNDS_THREADS]);
+          }
+        }
+        else {
+          const double * cb2 = (const double *)&T.box2[cg[c]];
+          for(int d = 0; d < dim; ++d) {
+            blo[d] = fmin(blo[d], __ldcg(cb2 + d));
+            bhi[d] = fmax(bhi[d], __ldcg(cb2 + 4 + d));
+          }
+        }
+      }
+    }
+  }
+  // children of a radix-tree node are always (split, split + 1): store
+  // split and the two leaf flags with the box, so the walk needs one load
+  const int l = cg[0], r = cg[1];
+  const int split = l < 0 ? ~l : l;
+  const int code = (split << 2) | ((l < 0) << 1) | (r < 0);
+  const int4 qlo = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
+  const int4 qhi = make_int4(hi[0], hi[1], hi[2], code);
+  T.qbox[2 * p] = qlo;
+  T.qbox[2 * p + 1] = qhi;
+  if(local) {
+    S.sq[2 * (p - b0)] = qlo;
+    S.sq[2 * (p - b0) + 1] = qhi;
+  }
+  if(nonuni) {
+    if(dim == 2)
+      blo[2] = bhi[2] = 0;
+    // NodeBox: lo xyz, hmax (0), hi xyz, pad (0)
+    double4 * bx = (double4 *)&T.box2[p];
+    bx[0] = make_double4(blo[0], blo[1], blo[2], 0.0);
+    bx[1] = make_double4(bhi[0], bhi[1], bhi[2], 0.0);
+    if(local)
+      for(int d = 0; d < 3; ++d) {
+        S.sb[d * BOUNDS_THREADS + (p - b0)] = blo[d];
+        S.sb[(3 + d) * BOUNDS_THREADS + (p - b0)] = bhi[d];
+      }
+    float fl[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
+    for(int d = 0; d < dim; ++d) {
+      fl[d] = __double2float_rd(blo[d] - r0[d]);
+      fh[d] = __double2float_ru(bhi[d] - r0[d]);
+    }
+    T.fbox2[2 * p] = make_float4(fl[0], fl[1], fl[2], 0.f);
+    T.fbox2[2 * p + 1] = make_float4(fh[0], fh[1], fh[2], 0.f);
+  }
+}
+
+__device__ __forceinline__ BoundsShared bounds_shared(unsigned char * bsm) {
+  BoundsShared S;
+  S.sq = (int4 *)bsm;
+  S.sb = (double *)(S.sq + 2 * BOUNDS_THREADS);
+  S.scnt = (unsigned *)(S.sb + 6 * BOUNDS_THREADS);
+  S.queue = (int *)(S.scnt + BOUNDS_THREADS);
+  S.exits = S.queue + 2 * BOUNDS_THREADS;
+  S.counts = S.exits + BOUNDS_THREADS;
+  S.sg = (double *)(S.counts + 4);
+  return S;
+}
+
+// The bottom-up pass comes in two variants; both are launched and the one
+// the run does not select returns at once.
+//
+// With gravity or varying h (FP64 moments and x +- h/2 boxes per node):
+// inside a block (its 256 leaves), rounds separated by block barriers, each
+// combining the nodes whose two children finished in earlier rounds, taken
+// from a compacted queue so that whole warps do the FP64 node arithmetic (a
+// thread per leaf climbing the tree keeps ~1/3 of its lanes busy, and the
+// FP64 pipe, not the lanes, is what the node arithmetic waits on); a
+// shared-memory count per node finds the round in which its second child
+// finishes.  Above the block -- nodes whose range straddles a block
+// boundary, a few per block -- the classic chain: the thread arriving second
+// at a node (a device-scope acquire-release count) combines it and climbs
+// on.  4M polytrope: 5.03 -> 2.84 ms per tree phase.
+//
+// Equal h without gravity (integer boxes only): the chain from every leaf,
+// with the counts and node data of the nodes inside the block in shared
+// memory (block-scope fences order them); there the barriers of the round
+// variant cost more than the idle lanes (Sedov 128^3 tree phase 0.48 ms
+// against 0.58).
+template<int dim>
+__global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds_chain(Particles P, Tree T,
   const int4 * qpos, const unsigned long long * rbits, int refboxes) {
+  if(T.gmom || refboxes || rbits[6] != rbits[7])
+    return;  // the round variant's run
   extern __shared__ __align__(16) unsigned char bsm[];
-  int4 * sq = (int4 *)bsm;                                // lo, hi per slot
-  double * sb = (double *)(sq + 2 * BOUNDS_THREADS);      // box2 lo xyz, hi xyz
-  unsigned * scnt = (unsigned *)(sb + 6 * BOUNDS_THREADS);
-  double * sg = (double *)(scnt + BOUNDS_THREADS);        // ten moments (gravity)
+  const BoundsShared S = bounds_shared(bsm);
   const int b0 = blockIdx.x * BOUNDS_THREADS;
   const int b1 = min(b0 + BOUNDS_THREADS, P.n) - 1;
-  scnt[threadIdx.x] = 0u;
+  S.scnt[threadIdx.x] = 0u;
   __syncthreads();
   const int i = b0 + threadIdx.x;
   if(i >= P.n)
     return;
-  const bool nonuni = refboxes || rbits[6] != rbits[7];
-  double rc[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0};
-  for(int d = 0; d < dim; ++d) {
-    r0[d] = ord_dec(rbits[d]);
-    if(T.gmom)
-      rc[d] = 0.5 * (r0[d] + ord_dec(rbits[3 + d]));
-  }
+  const double rc[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0};
   int p = T.leaf_parent[i];
   while(p >= 0) {
     const bool local = T.first[p] >= b0 && T.last[p] <= b1;
@@ -574,7 +750,7 @@ __global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds(Particles P, Tree T,
       // node data before the count (release) and the sibling's after it
       // (acquire)
       __threadfence_block();
-      prior = atomicAdd(&scnt[p - b0], 1u);
+      prior = atomicAdd(&S.scnt[p - b0], 1u);
       __threadfence_block();
     }
     else {
@@ -586,136 +762,80 @@ __global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds(Particles P, Tree T,
     }
     if(prior == 0)
       return;  // the sibling subtree is not finished yet
-    const int cg[2] = {T.left[p], T.right[p]};
-    if(T.gmom) {
-      double S[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-      for(int c = 0; c < 2; ++c) {
-        if(cg[c] < 0) {
-          const int j = ~cg[c];
-          const double m = P.f[F_M][j];
-          double y[3] = {0.0, 0.0, 0.0};
-          for(int d = 0; d < dim; ++d)
-            y[d] = P.f[F_X + d][j] - rc[d];
-          const double my[3] = {m * y[0], m * y[1], m * y[2]};
-          S[0] += m;
-          S[1] += my[0];
-          S[2] += my[1];
-          S[3] += my[2];
-          S[4] += my[0] * y[0];
-          S[5] += my[1] * y[1];
-          S[6] += my[2] * y[2];
-          S[7] += my[0] * y[1];
-          S[8] += my[0] * y[2];
-          S[9] += my[1] * y[2];
-        }
-        else if(local) {
-          const double * cs = sg + (cg[c] - b0);
-          for(int k = 0; k < 10; ++k)
-            S[k] += cs[k * BOUNDS_THREADS];
-        }
-        else {
-          const double * cs = T.gmom + 10 * (size_t)cg[c];
-          for(int k = 0; k < 10; ++k)
-            S[k] += __ldcg(cs + k);
-        }
-      }
-      double * out = T.gmom + 10 * (size_t)p;
-      for(int k = 0; k < 10; ++k)
-        out[k] = S[k];
-      if(local)
-        for(int k = 0; k < 10; ++k)
-          sg[k * BOUNDS_THREADS + (p - b0)] = S[k];
-    }
-    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
-    int hi[3] = {-1, -1, -1};
-    float hm = 0.f;
-    NodeBox n2;
-    n2.hmax = 0;
-    n2.pad = 0;
-    for(int d = 0; d < 3; ++d) {
-      n2.lo[d] = 1e308;
-      n2.hi[d] = -1e308;
-    }
-    for(int c = 0; c < 2; ++c) {
-      if(cg[c] < 0) {
-        const int j = ~cg[c];
-        const int4 q = qpos[j];
-        lo[0] = min(lo[0], q.x); hi[0] = max(hi[0], q.x);
-        lo[1] = min(lo[1], q.y); hi[1] = max(hi[1], q.y);
-        lo[2] = min(lo[2], q.z); hi[2] = max(hi[2], q.z);
-        hm = fmaxf(hm, __int_as_float(q.w));
-        if(nonuni) {
-          const double hj = P.f[F_H][j];
-          for(int d = 0; d < dim; ++d) {
-            double x = P.f[F_X + d][j];
-            n2.lo[d] = fmin(n2.lo[d], x - hj / 2.);
-            n2.hi[d] = fmax(n2.hi[d], x + hj / 2.);
-          }
-        }
-      }
-      else {
-        int4 a, b;
-        if(local) {
-          a = sq[2 * (cg[c] - b0)];
-          b = sq[2 * (cg[c] - b0) + 1];
-        }
-        else {
-          const int4 * cq = &T.qbox[2 * cg[c]];
-          a = __ldcg(cq);
-          b = __ldcg(cq + 1);
-        }
-        lo[0] = min(lo[0], a.x); lo[1] = min(lo[1], a.y); lo[2] = min(lo[2], a.z);
-        hi[0] = max(hi[0], b.x); hi[1] = max(hi[1], b.y); hi[2] = max(hi[2], b.z);
-        hm = fmaxf(hm, __int_as_float(a.w));
-        if(nonuni) {
-          if(local) {
-            const double * cb2 = sb + (cg[c] - b0);
-            for(int d = 0; d < dim; ++d) {
-              n2.lo[d] = fmin(n2.lo[d], cb2[d * BOUNDS_THREADS]);
-              n2.hi[d] = fmax(n2.hi[d], cb2[(3 + d) * BOUNDS_THREADS]);
-            }
-          }
-          else {
-            const double * cb2 = (const double *)&T.box2[cg[c]];
-            for(int d = 0; d < dim; ++d) {
-              n2.lo[d] = fmin(n2.lo[d], __ldcg(cb2 + d));
-              n2.hi[d] = fmax(n2.hi[d], __ldcg(cb2 + 4 + d));
-            }
-          }
-        }
-      }
-    }
-    // children of a radix-tree node are always (split, split + 1): store
-    // split and the two leaf flags with the box, so the walk needs one load
-    const int l = cg[0], r = cg[1];
-    const int split = l < 0 ? ~l : l;
-    const int code = (split << 2) | ((l < 0) << 1) | (r < 0);
-    const int4 qlo = make_int4(lo[0], lo[1], lo[2], __float_as_int(hm));
-    const int4 qhi = make_int4(hi[0], hi[1], hi[2], code);
-    T.qbox[2 * p] = qlo;
-    T.qbox[2 * p + 1] = qhi;
-    if(local) {
-      sq[2 * (p - b0)] = qlo;
-      sq[2 * (p - b0) + 1] = qhi;
-    }
-    if(nonuni) {
-      if(dim == 2)
-        n2.lo[2] = n2.hi[2] = 0;
-      T.box2[p] = n2;
-      if(local)
-        for(int d = 0; d < 3; ++d) {
-          sb[d * BOUNDS_THREADS + (p - b0)] = n2.lo[d];
-          sb[(3 + d) * BOUNDS_THREADS + (p - b0)] = n2.hi[d];
-        }
-      float fl[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
-      for(int d = 0; d < dim; ++d) {
-        fl[d] = __double2float_rd(n2.lo[d] - r0[d]);
-        fh[d] = __double2float_ru(n2.hi[d] - r0[d]);
-      }
-      T.fbox2[2 * p] = make_float4(fl[0], fl[1], fl[2], 0.f);
-      T.fbox2[2 * p + 1] = make_float4(fh[0], fh[1], fh[2], 0.f);
-    }
+    bounds_node<dim>(P, T, qpos, S, p, local, b0, false, rc, r0);
     p = T.parent[p];
+  }
+}
+
+template<int dim>
+__global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds_rounds(Particles P, Tree T,
+  const int4 * qpos, const unsigned long long * rbits, int refboxes) {
+  const bool nonuni = refboxes || rbits[6] != rbits[7];
+  if(!T.gmom && !nonuni)
+    return;  // the chain variant's run
+  extern __shared__ __align__(16) unsigned char bsm[];
+  const BoundsShared S = bounds_shared(bsm);
+  const int t = threadIdx.x;
+  const int b0 = blockIdx.x * BOUNDS_THREADS;
+  const int b1 = min(b0 + BOUNDS_THREADS, P.n) - 1;
+  S.scnt[t] = 0u;
+  if(t < 4)
+    S.counts[t] = 0;
+  double rc[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0};
+  for(int d = 0; d < dim; ++d) {
+    r0[d] = ord_dec(rbits[d]);
+    if(T.gmom)
+      rc[d] = 0.5 * (r0[d] + ord_dec(rbits[3 + d]));
+  }
+  auto is_local = [&](int v) { return T.first[v] >= b0 && T.last[v] <= b1; };
+  // a node (or ~leaf) whose data are final: count its arrival at the parent
+  auto arrive = [&](int v, int next) {
+    const int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
+    if(p < 0)
+      return;
+    if(is_local(p)) {
+      if(atomicAdd(&S.scnt[p - b0], 1u) == 1u)
+        S.queue[next * BOUNDS_THREADS + atomicAdd(&S.counts[next], 1)] = p;
+    }
+    else
+      S.exits[atomicAdd(&S.counts[2], 1)] = v;
+  };
+  __syncthreads();
+  if(b0 + t <= b1)
+    arrive(~(b0 + t), 0);
+  __syncthreads();
+  for(int cur = 0;; cur ^= 1) {
+    const int len = S.counts[cur];
+    if(len == 0)
+      break;
+    __syncthreads();  // every thread has read len
+    if(t == 0)
+      S.counts[cur] = 0;  // the queue after next reuses this one
+    if(t < len) {
+      const int p = S.queue[cur * BOUNDS_THREADS + t];
+      bounds_node<dim>(P, T, qpos, S, p, true, b0, nonuni, rc, r0);
+      arrive(p, cur ^ 1);
+    }
+    __syncthreads();
+  }
+  const int nex = S.counts[2];
+  if(nex == 0)
+    return;
+  // the exits' data (written by any thread of the block before the last
+  // barrier) become visible device-wide before this thread's counts
+  __threadfence();
+  for(int e = t; e < nex; e += BOUNDS_THREADS) {
+    const int v = S.exits[e];
+    int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
+    while(p >= 0) {
+      unsigned prior;
+      asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
+                   : "=r"(prior) : "l"(T.counter + p) : "memory");
+      if(prior == 0)
+        break;  // the sibling subtree is not finished yet
+      bounds_node<dim>(P, T, qpos, S, p, false, b0, nonuni, rc, r0);
+      p = T.parent[p];
+    }
   }
 }
 
@@ -825,15 +945,19 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
     k_edepth<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T.edepth);
   const int nbb = (n + BOUNDS_THREADS - 1) / BOUNDS_THREADS;
   const size_t bsm = bounds_smem(T.gmom != nullptr);
-  if(pp.dim == 3)
-    k_bounds<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
-  else
-    k_bounds<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+  if(pp.dim == 3) {
+    k_bounds_chain<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+    k_bounds_rounds<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+  }
+  else {
+    k_bounds_chain<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+    k_bounds_rounds<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
+  }
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max, pp.dim, qscale,
     rbits);
   k_refgroups<<<(n + 255) / 256, 256, 0, L.stream>>>(P.key, n, pp.dim, T, rbits,
     ordered);
-  *L.counter += 5;
+  *L.counter += ordered ? 6 : 5;
   return cudaGetLastError();
 }
 
