@@ -719,7 +719,10 @@ __device__ __forceinline__ BoundsShared bounds_shared(unsigned char * bsm) {
 // finishes.  Above the block -- nodes whose range straddles a block
 // boundary, a few per block -- the classic chain: the thread arriving second
 // at a node (a device-scope acquire-release count) combines it and climbs
-// on.  4M polytrope: 5.03 -> 2.84 ms per tree phase.
+// on.  4M polytrope: 5.03 -> 2.84 ms per tree phase.  One block per 256
+// leaves: a smaller grid striding over the leaf blocks (so that equal-h runs
+// skip the variant in one wave) measured 4.30 ms, as each block's climb
+// above its leaves then holds back its next leaves.
 //
 // Equal h without gravity (integer boxes only): the chain from every leaf,
 // with the counts and node data of the nodes inside the block in shared
@@ -776,82 +779,67 @@ __global__ void __launch_bounds__(BOUNDS_THREADS) k_bounds_rounds(Particles P, T
   extern __shared__ __align__(16) unsigned char bsm[];
   const BoundsShared S = bounds_shared(bsm);
   const int t = threadIdx.x;
+  const int b0 = blockIdx.x * BOUNDS_THREADS;
+  const int b1 = min(b0 + BOUNDS_THREADS, P.n) - 1;
+  S.scnt[t] = 0u;
+  if(t < 4)
+    S.counts[t] = 0;
   double rc[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0};
   for(int d = 0; d < dim; ++d) {
     r0[d] = ord_dec(rbits[d]);
     if(T.gmom)
       rc[d] = 0.5 * (r0[d] + ord_dec(rbits[3 + d]));
   }
-  // the grid strides over the blocks of 256 leaves (a grid of a few blocks
-  // per SM, so that a run the chain variant serves returns in one wave)
-  const int nlb = (P.n + BOUNDS_THREADS - 1) / BOUNDS_THREADS;
-  for(int lb = blockIdx.x; lb < nlb; lb += gridDim.x) {
-    const int b0 = lb * BOUNDS_THREADS;
-    const int b1 = min(b0 + BOUNDS_THREADS, P.n) - 1;
-    S.scnt[t] = 0u;
-    if(t < 4)
-      S.counts[t] = 0;
-    auto is_local = [&](int v) { return T.first[v] >= b0 && T.last[v] <= b1; };
-    // a node (or ~leaf) whose data are final: count its arrival at the parent
-    auto arrive = [&](int v, int next) {
-      const int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
-      if(p < 0)
-        return;
-      if(is_local(p)) {
-        if(atomicAdd(&S.scnt[p - b0], 1u) == 1u)
-          S.queue[next * BOUNDS_THREADS + atomicAdd(&S.counts[next], 1)] = p;
-      }
-      else
-        S.exits[atomicAdd(&S.counts[2], 1)] = v;
-    };
-    __syncthreads();
-    if(b0 + t <= b1)
-      arrive(~(b0 + t), 0);
-    __syncthreads();
-    for(int cur = 0;; cur ^= 1) {
-      const int len = S.counts[cur];
-      if(len == 0)
-        break;
-      __syncthreads();  // every thread has read len
-      if(t == 0)
-        S.counts[cur] = 0;  // the queue after next reuses this one
-      if(t < len) {
-        const int p = S.queue[cur * BOUNDS_THREADS + t];
-        bounds_node<dim>(P, T, qpos, S, p, true, b0, nonuni, rc, r0);
-        arrive(p, cur ^ 1);
-      }
-      __syncthreads();
+  auto is_local = [&](int v) { return T.first[v] >= b0 && T.last[v] <= b1; };
+  // a node (or ~leaf) whose data are final: count its arrival at the parent
+  auto arrive = [&](int v, int next) {
+    const int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
+    if(p < 0)
+      return;
+    if(is_local(p)) {
+      if(atomicAdd(&S.scnt[p - b0], 1u) == 1u)
+        S.queue[next * BOUNDS_THREADS + atomicAdd(&S.counts[next], 1)] = p;
     }
-    const int nex = S.counts[2];
-    if(nex > 0) {
-      // the exits' data (written by any thread of the block before the
-      // last barrier) become visible device-wide before this thread's counts
-      __threadfence();
-      for(int e = t; e < nex; e += BOUNDS_THREADS) {
-        const int v = S.exits[e];
-        int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
-        while(p >= 0) {
-          unsigned prior;
-          asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
-                       : "=r"(prior) : "l"(T.counter + p) : "memory");
-          if(prior == 0)
-            break;  // the sibling subtree is not finished yet
-          bounds_node<dim>(P, T, qpos, S, p, false, b0, nonuni, rc, r0);
-          p = T.parent[p];
-        }
-      }
+    else
+      S.exits[atomicAdd(&S.counts[2], 1)] = v;
+  };
+  __syncthreads();
+  if(b0 + t <= b1)
+    arrive(~(b0 + t), 0);
+  __syncthreads();
+  for(int cur = 0;; cur ^= 1) {
+    const int len = S.counts[cur];
+    if(len == 0)
+      break;
+    __syncthreads();  // every thread has read len
+    if(t == 0)
+      S.counts[cur] = 0;  // the queue after next reuses this one
+    if(t < len) {
+      const int p = S.queue[cur * BOUNDS_THREADS + t];
+      bounds_node<dim>(P, T, qpos, S, p, true, b0, nonuni, rc, r0);
+      arrive(p, cur ^ 1);
     }
-    __syncthreads();  // the shared memory serves the next block of leaves
+    __syncthreads();
   }
-}
-
-// Blocks of the round variant: a few per SM (its registers allow four).
-static int bounds_rounds_grid(int nlb) {
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int g = 4 * (nsm > 0 ? nsm : 152);
-  return nlb < g ? nlb : g;
+  const int nex = S.counts[2];
+  if(nex == 0)
+    return;
+  // the exits' data (written by any thread of the block before the last
+  // barrier) become visible device-wide before this thread's counts
+  __threadfence();
+  for(int e = t; e < nex; e += BOUNDS_THREADS) {
+    const int v = S.exits[e];
+    int p = v < 0 ? T.leaf_parent[~v] : T.parent[v];
+    while(p >= 0) {
+      unsigned prior;
+      asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;"
+                   : "=r"(prior) : "l"(T.counter + p) : "memory");
+      if(prior == 0)
+        break;  // the sibling subtree is not finished yet
+      bounds_node<dim>(P, T, qpos, S, p, false, b0, nonuni, rc, r0);
+      p = T.parent[p];
+    }
+  }
 }
 
 // Groups: maximal subtrees with at most `gmax` particles.  Each group also
@@ -962,13 +950,11 @@ cudaError_t launch_build_tree(const Launch & L, const Particles & P,
   const size_t bsm = bounds_smem(T.gmom != nullptr);
   if(pp.dim == 3) {
     k_bounds_chain<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
-    k_bounds_rounds<3><<<bounds_rounds_grid(nbb), BOUNDS_THREADS, bsm, L.stream>>>(P, T,
-      qpos, rbits, ordered);
+    k_bounds_rounds<3><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
   }
   else {
     k_bounds_chain<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
-    k_bounds_rounds<2><<<bounds_rounds_grid(nbb), BOUNDS_THREADS, bsm, L.stream>>>(P, T,
-      qpos, rbits, ordered);
+    k_bounds_rounds<2><<<nbb, BOUNDS_THREADS, bsm, L.stream>>>(P, T, qpos, rbits, ordered);
   }
   k_groups<<<(n + 255) / 256, 256, 0, L.stream>>>(n, T, group_max, pp.dim, qscale,
     rbits);
