@@ -547,7 +547,7 @@ struct BoundsShared {
   int4 * sq;        // lo, hi per slot
   double * sb;      // box2 lo xyz, hi xyz per slot
   unsigned * scnt;  // arrival counts per slot
-  int * queue;      // 2 x 256: nodes whose two children are done, this round and next
+  int * queue;      // 2 x 256: nodes whose two children are done (current pass, next pass)
   int * exits;      // nodes (~leaf for a leaf) whose parent is outside the block
   int * counts;     // queue lengths [2], exit count
   double * sg;      // ten moments per slot (gravity)
