@@ -531,7 +531,7 @@ __global__ void k_edepth(const unsigned long long * K, int n, int dim,
 // refboxes: also the reference's x +- h/2 node boxes (box2, fbox2), which
 // the walk's node tests read: with varying h, or in the ordered (FP64) mode
 // where equal-h ties take them too.
-// Shared-memory layout of one k_bounds block (dynamic): the node data of the
+// Shared-memory layout of one k_bounds_* block (dynamic): the node data of the
 // internal nodes whose leaf range lies inside the block's own leaves (slot =
 // node index - first leaf of the block: such a node's index is one end of
 // its range), their arrival counters, two work queues and the list of the
@@ -1260,7 +1260,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32,
     float4 fglo = make_float4(0.f, 0.f, 0.f, 0.f), fghi = fglo;
     float cax = 0.f, cay = 0.f, caz = 0.f;
     // the reference's group and boxes exist with varying h, and in the
-    // ordered mode (k_bounds, k_refgroups)
+    // ordered mode (k_bounds_rounds, k_refgroups)
     if(mem && (nonuni || ORDERED)) {
       gnode = T.gref[a];
       if(gnode >= 0) {
