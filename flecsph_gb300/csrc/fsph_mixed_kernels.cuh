@@ -894,9 +894,11 @@ __global__ void __launch_bounds__(MIX_THREADS, 3) k_density_ff(Particles P,
 // UNI (every h equal) 1/h^(D+2) multiplies the finished sums instead of
 // every pair.  The pressure sum alone is the pressure-only acceleration the
 // de/dt pass takes.
-// pairs of a four-slot list chunk the acceleration pass unrolls
+// pairs of a four-slot list chunk the acceleration pass unrolls: all four
+// (128 registers, no spills) measured 2 % faster than two at Sedov 128^3
+// (2.01 against 2.05 ms per pass), one 10 % slower
 #ifndef FSPH_ACCEL_FF_UNROLL
-#define FSPH_ACCEL_FF_UNROLL 2
+#define FSPH_ACCEL_FF_UNROLL 4
 #endif
 constexpr int accel_ff_unroll = FSPH_ACCEL_FF_UNROLL;
 
